@@ -1,0 +1,166 @@
+/*
+ * kapdqmc.h — C ABI of libkapdqmc_gpu.so, the GB300 (sm_103a) projector-DQMC
+ * sweep for KAPDQMC's t-U, t-V and t-UV models.
+ *
+ * The reference exposes the sweep as Julia methods; each entry point below
+ * names the reference interface it replaces (paths are inside the KAPDQMC
+ * project).  A Julia wrapper calls these through `ccall`; arrays are passed
+ * in Julia's column-major layout, complex numbers as interleaved (re, im)
+ * doubles.  Plain pointers and sizes only: the caller owns every host
+ * array, the library copies what it needs during the call and keeps no host
+ * pointer.  The library owns all device memory of a handle.
+ *
+ * Every function returns KDQ_OK (0) or a KDQ_ERR_* code; the message of the
+ * last failure of a handle is returned by kdq_last_error().  A handle is not
+ * thread-safe; distinct handles may be used from distinct threads.
+ */
+#ifndef KAPDQMC_H
+#define KAPDQMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  KDQ_OK = 0,
+  KDQ_ERR_ARG = 1,      /* invalid argument or size (reference: @assert / error()) */
+  KDQ_ERR_CUDA = 2,     /* CUDA runtime failure */
+  KDQ_ERR_NUMERIC = 3,  /* NaN/Inf ratio, singular pivot, or drift above limit */
+  KDQ_ERR_STATE = 4,    /* call out of order (e.g. tape exhausted) */
+  KDQ_ERR_NOGPU = 5     /* no usable CUDA device */
+};
+
+enum { KDQ_TU = 0, KDQ_TV = 1, KDQ_TUV = 2 };
+
+enum { KDQ_SQUARE45 = 0, KDQ_SQUARE90 = 1, KDQ_HONEYCOMB120 = 2, KDQ_HONEYCOMB60 = 3 };
+
+/* Model description: the fields of tU_Hubbard_Para_ / tV_Hubbard_Para_ /
+ * tUV_Hubbard_Para_ that the sweep reads (src/tU/model.jl:14-37,
+ * src/tV/model.jl:3-28, src/tUV/model.jl:3-27).  Matrices are Ns x Ns
+ * column-major; Pt is Ns x Ns/2.  eK, eKinv, HalfeK, HalfeKinv and K are
+ * complex (interleaved) iff k_complex; Pt is complex iff g_complex. */
+typedef struct kdq_model_desc {
+  int32_t kind;        /* KDQ_TU, KDQ_TV or KDQ_TUV */
+  int32_t lattice;     /* KDQ_SQUARE45 ... KDQ_HONEYCOMB60 */
+  int32_t site[2];     /* unit cells per direction */
+  int32_t Ns;          /* sites (even) */
+  int32_t Nt;          /* imaginary-time slices */
+  int32_t z;           /* bond directions (tV, tUV); 1 for tU */
+  int32_t g_complex;   /* sweep arithmetic: 1 complex128, 0 float64 */
+  int32_t k_complex;   /* 1 if the kinetic matrices carry imaginary parts */
+  int32_t n_nodes;     /* length of nodes */
+  const int64_t* nodes;/* stabilisation nodes, 0 = nodes[0] < ... = Nt */
+  const double* alpha; /* Nt coupling per slice (tU, tV); may be NULL for tUV */
+  const double* gamma; /* 4 HS weights */
+  const double* eta;   /* 4 HS fields */
+  double a;            /* tUV: weight of a bond's second site */
+  double Ht;           /* hopping */
+  double U;            /* tUV interaction U (energy prefactor) */
+  double V;            /* tUV interaction V (energy prefactor) */
+  const double* eK;
+  const double* eKinv;
+  const double* HalfeK;
+  const double* HalfeKinv;
+  const double* K;
+  const double* Pt;
+  const int32_t* bonds;/* 1-based (x, y) pairs in nnidx's column-major order:
+                          tV (Ns/2)*z pairs, tUV Ns*z pairs, NULL for tU */
+} kdq_model_desc;
+
+typedef struct kdq_handle kdq_handle;
+
+typedef struct kdq_stats {
+  int64_t proposals;   /* proposals made by all chains in the last call */
+  int64_t accepted;    /* accepted proposals */
+  int64_t recomputes;  /* stabilisation recomputes of G */
+  double max_drift;    /* max ||G_wrap - G_recompute||_F / ||G_recompute||_F */
+  double seconds;      /* wall time of the last kdq_phy_update / kdq_sweep */
+} kdq_stats;
+
+/* Create a handle with n_chains independent Markov chains of one model on a
+ * CUDA device, uploading the model (replaces the per-call buffer set-up of
+ * phy_update: PhyBuffer, src/tU/model.jl:151-165; src/public/Buffer.jl:3-19). */
+int kdq_create(kdq_handle** out, const kdq_model_desc* model, int32_t n_chains, int32_t device);
+
+/* Free all device memory of the handle. */
+void kdq_destroy(kdq_handle* h);
+
+/* Message of the last failure on h (or of the last kdq_create failure when
+ * h is NULL).  Valid until the next call on h. */
+const char* kdq_last_error(const kdq_handle* h);
+
+/* HS fields of all chains: n_chains consecutive arrays, each in the layout of
+ * the reference's `s` (tU: Ns x Nt, src/tU/GreenMatrix.jl:1-8; tV:
+ * (Ns/2) x z x Nt, src/tV/GreenMatrix.jl:1-10; tUV: Ns*z x Nt,
+ * src/tUV/GreenMatrix.jl:1-8), values in {1,2,3,4}.  nbytes must equal
+ * n_chains * Nt * n_field. */
+int kdq_set_fields(kdq_handle* h, const uint8_t* s, size_t nbytes);
+int kdq_get_fields(kdq_handle* h, uint8_t* s, size_t nbytes);
+
+/* Random stream: Philox4x32-10, key = seed, counter = (proposal index in
+ * sweep, sweep index, chain, stream id).  sweep_offset is the sweep index of
+ * the next sweep; it advances by one per sweep.  Replaces the reference's
+ * unseedable MersenneTwister(threadid()+time_ns()) (src/tU/phy_update.jl:31). */
+int kdq_set_rng(kdq_handle* h, uint64_t seed, uint64_t sweep_offset);
+
+/* Explicit proposal tape in the reference's consumption order
+ * (src/tU/phy_update.jl:259,262): per proposal a choice index k in {0,1,2}
+ * among the three values other than the current one (ascending) and a
+ * uniform u in [0,1).  n_per_chain entries per chain, chain-major.  The next
+ * kdq_phy_update/kdq_sweep consumes it from its start; a tape shorter than
+ * the sweeps need fails with KDQ_ERR_STATE.  kdq_set_rng switches back to
+ * the Philox stream. */
+int kdq_set_tape(kdq_handle* h, const uint8_t* k, const double* u, size_t n_per_chain);
+
+/* The reference's phy_update(path, model, s, Sweeps, record) for all chains:
+ * rebuild the left B chain and G from the current fields, run `sweeps`
+ * forward+backward sweeps with local updates and QR stabilisation, and
+ * return the per-sweep measurement rows when record != 0 (tU: Ek Eu CDW0
+ * CDW1 SDW0 SDW1; tV: Ek Ev R0[4] R1[4]; tUV: Ek Eu Ev CDW0 CDW1 SDW0 SDW1).
+ * obs may be NULL when record == 0; otherwise obs_len must be at least
+ * n_chains * sweeps * kdq_n_obs(h), filled chain-major.
+ * Replaces src/tU/phy_update.jl:3-152, src/tV/phy_update.jl:1-188,
+ * src/tUV/phy_update.jl:1-186 (the CSV append is left to the caller). */
+int kdq_phy_update(kdq_handle* h, int32_t sweeps, int32_t record, double* obs, size_t obs_len);
+
+/* Split form of kdq_phy_update for callers that keep the state resident:
+ * kdq_init rebuilds the B chain and G from the current fields
+ * (src/tU/phy_update.jl:39-50); kdq_sweep continues from the current state
+ * without host copies (asynchronous on the handle's stream; observables stay
+ * on the device until kdq_get_obs). */
+int kdq_init(kdq_handle* h);
+int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record);
+int kdq_get_obs(kdq_handle* h, double* obs, size_t obs_len);
+int kdq_synchronize(kdq_handle* h);
+
+/* Number of measurement columns per sweep row (6, 10 or 7). */
+int kdq_n_obs(const kdq_handle* h);
+
+/* Equal-time Green's function of one chain at the current slice (Ns x Ns,
+ * column-major, interleaved complex iff g_complex).  len counts doubles. */
+int kdq_get_green(kdq_handle* h, int32_t chain, double* G, size_t len);
+
+/* Statistics of the last kdq_phy_update / kdq_sweep call. */
+int kdq_get_stats(kdq_handle* h, kdq_stats* st);
+
+/* Debug record of accept decisions (1 byte per proposal, chain-major, in
+ * tape order) of the next calls; enable before kdq_phy_update.  Replaces the
+ * reference's commented-out checks (src/tV/phy_update.jl:74-90). */
+int kdq_enable_accept_log(kdq_handle* h, size_t n_per_chain);
+int kdq_get_accept_log(kdq_handle* h, uint8_t* flags, size_t nbytes);
+
+/* Drift ||G_wrap - G_recompute||_F / ||G_recompute||_F at every recompute of
+ * the last call, chain-major, 2*(n_nodes-1) per sweep (the reference's
+ * "Batchsize Wrap Error" check, src/tU/phy_update.jl:89-97). */
+int kdq_get_drift(kdq_handle* h, double* drift, size_t len);
+
+/* CUDA stream (cudaStream_t) of the handle, for event timing by callers. */
+void* kdq_stream(kdq_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KAPDQMC_H */

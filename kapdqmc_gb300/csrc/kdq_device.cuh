@@ -1,0 +1,282 @@
+// Device building blocks of the sweep: complex arithmetic, block-level
+// FP64 GEMM, Householder orthonormalisation, LU solve and reductions.
+//
+// Every routine here is executed by a whole CTA (all threads call it, with
+// identical arguments) and works on column-major matrices addressed through
+// generic pointers, so the same code runs on shared or global memory.  A
+// routine ends with __syncthreads() so its result is visible to the caller.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kdq {
+
+// ---------------------------------------------------------------- complex
+struct cd {
+  double x, y;
+};
+
+__host__ __device__ inline cd mkc(double x, double y) { return cd{x, y}; }
+__device__ inline cd operator+(cd a, cd b) { return {a.x + b.x, a.y + b.y}; }
+__device__ inline cd operator-(cd a, cd b) { return {a.x - b.x, a.y - b.y}; }
+__device__ inline cd operator-(cd a) { return {-a.x, -a.y}; }
+__device__ inline cd operator*(cd a, cd b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ inline cd operator*(cd a, double b) { return {a.x * b, a.y * b}; }
+__device__ inline cd operator*(double a, cd b) { return {a * b.x, a * b.y}; }
+__device__ inline cd operator/(cd a, cd b) {
+  // Smith's algorithm (scaled division), avoids overflow of |b|^2.
+  if (fabs(b.x) >= fabs(b.y)) {
+    double r = b.y / b.x, d = b.x + r * b.y;
+    return {(a.x + a.y * r) / d, (a.y - a.x * r) / d};
+  }
+  double r = b.x / b.y, d = b.y + r * b.x;
+  return {(a.x * r + a.y) / d, (a.y * r - a.x) / d};
+}
+__device__ inline cd operator/(cd a, double b) { return {a.x / b, a.y / b}; }
+__device__ inline cd conjg(cd a) { return {a.x, -a.y}; }
+__device__ inline double conjg(double a) { return a; }
+__device__ inline double re(cd a) { return a.x; }
+__device__ inline double re(double a) { return a; }
+__device__ inline double abs2(cd a) { return a.x * a.x + a.y * a.y; }
+__device__ inline double abs2(double a) { return a * a; }
+__device__ inline bool finite(cd a) { return isfinite(a.x) && isfinite(a.y); }
+__device__ inline bool finite(double a) { return isfinite(a); }
+
+template <class T> __device__ inline T zero();
+template <> __device__ inline double zero<double>() { return 0.0; }
+template <> __device__ inline cd zero<cd>() { return {0.0, 0.0}; }
+template <class T> __device__ inline T one();
+template <> __device__ inline double one<double>() { return 1.0; }
+template <> __device__ inline cd one<cd>() { return {1.0, 0.0}; }
+template <class T> __device__ inline T from_real(double v);
+template <> __device__ inline double from_real<double>(double v) { return v; }
+template <> __device__ inline cd from_real<cd>(double v) { return {v, 0.0}; }
+
+// acc += a * b for every mix of real and complex operands
+__device__ inline void madd(double& acc, double a, double b) { acc = fma(a, b, acc); }
+__device__ inline void madd(cd& acc, cd a, double b) { acc.x = fma(a.x, b, acc.x); acc.y = fma(a.y, b, acc.y); }
+__device__ inline void madd(cd& acc, double a, cd b) { acc.x = fma(a, b.x, acc.x); acc.y = fma(a, b.y, acc.y); }
+__device__ inline void madd(cd& acc, cd a, cd b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+
+template <class T> struct conv;
+template <> struct conv<double> {
+  __device__ static double from(double v) { return v; }
+};
+template <> struct conv<cd> {
+  __device__ static cd from(double v) { return {v, 0.0}; }
+  __device__ static cd from(cd v) { return v; }
+};
+
+// ------------------------------------------------------------- reductions
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ inline cd warp_sum(cd v) { return {warp_sum(v.x), warp_sum(v.y)}; }
+
+// Block-wide sum; `red` is shared scratch of >= 32 doubles.  All threads
+// receive the result.
+__device__ inline double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < nw; ++w) t += red[w];
+  __syncthreads();
+  return t;
+}
+
+// ------------------------------------------------------------------- GEMM
+// C[M x N] = A[M x K] * B[K x N] (column-major, C must not alias A or B).
+// Lane l of a warp owns rows l, l+32, ..., l+32*(MAXRM-1); warps own groups
+// of CB columns.  Each k step loads MAXRM coalesced A values and CB
+// broadcast B values for MAXRM*CB multiply-adds.
+// An optional epilogue scales the result: C[i,j] = rs[i] * acc * cs[j].
+template <int MAXRM, class TA, class TB, class TC, class TS = double>
+__device__ void bgemm(int M, int N, int K, const TA* __restrict__ A, int lda,
+                      const TB* __restrict__ B, int ldb, TC* __restrict__ C, int ldc,
+                      const TS* rs = nullptr, const TS* cs = nullptr) {
+  constexpr int CB = 4;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j0 = warp * CB; j0 < N; j0 += nw * CB) {
+    TC acc[MAXRM][CB];
+#pragma unroll
+    for (int r = 0; r < MAXRM; ++r)
+#pragma unroll
+      for (int c = 0; c < CB; ++c) acc[r][c] = zero<TC>();
+    const TB* Bp[CB];
+#pragma unroll
+    for (int c = 0; c < CB; ++c) Bp[c] = B + (size_t)min(j0 + c, N - 1) * ldb;
+    for (int k = 0; k < K; ++k) {
+      TB b[CB];
+#pragma unroll
+      for (int c = 0; c < CB; ++c) b[c] = Bp[c][k];
+      const TA* Ak = A + (size_t)k * lda;
+#pragma unroll
+      for (int r = 0; r < MAXRM; ++r) {
+        const int i = lane + 32 * r;
+        if (i < M) {
+          TA a = Ak[i];
+#pragma unroll
+          for (int c = 0; c < CB; ++c) madd(acc[r][c], a, b[c]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < CB; ++c) {
+      const int j = j0 + c;
+      if (j >= N) break;
+#pragma unroll
+      for (int r = 0; r < MAXRM; ++r) {
+        const int i = lane + 32 * r;
+        if (i < M) {
+          TC v = acc[r][c];
+          if (rs) v = rs[i] * v;
+          if (cs) v = v * cs[j];
+          C[i + (size_t)j * ldc] = v;
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------ Householder QR (thin Q)
+// Overwrites Q (N x n, column-major, ld N) with an orthonormal basis of the
+// column space of Y (N x n, ld N), destroying Y.  Reflectors
+// H = I - w w^H * (2 / w^H w) with w = x + e^{i arg x0} |x| e1 (Householder
+// 1958; the LAPACK ?geqrf + ?orgqr pair restated with Hermitian reflectors).
+// Scratch: wn (n doubles: 2/(w^H w)), red (>= 32 doubles) in shared memory.
+template <class T>
+__device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red, T* w0) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int j = 0; j < n; ++j) {
+    T* x = Y + (size_t)j * N;
+    double s = 0.0;
+    for (int i = j + tid; i < N; i += nt) s += abs2(x[i]);
+    const double nrm2 = block_sum(s, red);
+    const double nrm = sqrt(nrm2);
+    if (tid == 0) {
+      T a = x[j];
+      double aa = sqrt(abs2(a));
+      T ph = aa > 0.0 ? a / aa : one<T>();
+      T wj = a + ph * nrm;                    // w_j
+      double ww = 2.0 * nrm * (nrm + aa);     // w^H w
+      wn[j] = ww > 0.0 ? 2.0 / ww : 0.0;
+      x[j] = wj;
+      *w0 = wj;
+    }
+    __syncthreads();
+    // trailing columns c > j: A[:,c] -= (2/ww) w (w^H A[:,c])
+    for (int c = j + 1 + warp; c < n; c += nw) {
+      T* y = Y + (size_t)c * N;
+      T t = zero<T>();
+      for (int i = j + lane; i < N; i += 32) madd(t, conjg(x[i]), y[i]);
+      t = warp_sum(t);
+      t = t * wn[j];
+      for (int i = j + lane; i < N; i += 32) y[i] = y[i] - x[i] * t;
+    }
+    __syncthreads();
+  }
+  // Q = H_0 H_1 ... H_{n-1} [I; 0]
+  for (int e = tid; e < N * n; e += nt) {
+    const int i = e % N, c = e / N;
+    Q[e] = i == c ? one<T>() : zero<T>();
+  }
+  __syncthreads();
+  for (int j = n - 1; j >= 0; --j) {
+    const T* x = Y + (size_t)j * N;
+    for (int c = j + warp; c < n; c += nw) {
+      T* q = Q + (size_t)c * N;
+      T t = zero<T>();
+      for (int i = j + lane; i < N; i += 32) madd(t, conjg(x[i]), q[i]);
+      t = warp_sum(t);
+      t = t * wn[j];
+      for (int i = j + lane; i < N; i += 32) q[i] = q[i] - x[i] * t;
+    }
+    __syncthreads();
+  }
+}
+
+// --------------------------------------------------------- LU and solves
+// In-place LU with partial pivoting of the n x n matrix M (ld n); piv[j]
+// receives the row swapped with j (the ?getrf convention).  Returns false
+// through *bad when a zero pivot is met.
+template <class T>
+__device__ void lu_factor(int n, T* M, int* piv, int* bad) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ int sp;
+  for (int j = 0; j < n; ++j) {
+    if (tid < 32) {
+      double best = -1.0;
+      int bi = j;
+      for (int i = j + tid; i < n; i += 32) {
+        double v = abs2(M[i + (size_t)j * n]);
+        if (v > best) { best = v; bi = i; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (tid == 0) {
+        sp = bi;
+        piv[j] = bi;
+        if (!(best > 0.0)) *bad = 1;
+      }
+    }
+    __syncthreads();
+    const int p = sp;
+    if (p != j)
+      for (int c = tid; c < n; c += nt) {
+        T t = M[j + (size_t)c * n];
+        M[j + (size_t)c * n] = M[p + (size_t)c * n];
+        M[p + (size_t)c * n] = t;
+      }
+    __syncthreads();
+    const T d = M[j + (size_t)j * n];
+    for (int i = j + 1 + tid; i < n; i += nt) M[i + (size_t)j * n] = M[i + (size_t)j * n] / d;
+    __syncthreads();
+    const int m = n - j - 1;
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = j + 1 + e % m, c = j + 1 + e / m;
+      M[i + (size_t)c * n] = M[i + (size_t)c * n] - M[i + (size_t)j * n] * M[j + (size_t)c * n];
+    }
+    __syncthreads();
+  }
+}
+
+// X (n x N, ld n) <- M^{-1} X using the LU factors of lu_factor (?getrs).
+// Each thread solves whole columns, so no synchronisation is needed inside.
+template <class T>
+__device__ void lu_solve(int n, int N, const T* M, const int* piv, T* X) {
+  for (int c = threadIdx.x; c < N; c += blockDim.x) {
+    T* x = X + (size_t)c * n;
+    for (int j = 0; j < n; ++j) {
+      const int p = piv[j];
+      if (p != j) { T t = x[j]; x[j] = x[p]; x[p] = t; }
+    }
+    for (int j = 0; j < n; ++j) {
+      const T v = x[j];
+      for (int i = j + 1; i < n; ++i) x[i] = x[i] - M[i + (size_t)j * n] * v;
+    }
+    for (int j = n - 1; j >= 0; --j) {
+      const T v = x[j] / M[j + (size_t)j * n];
+      x[j] = v;
+      for (int i = 0; i < j; ++i) x[i] = x[i] - M[i + (size_t)j * n] * v;
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace kdq

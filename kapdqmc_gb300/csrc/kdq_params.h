@@ -1,0 +1,92 @@
+// Launch parameters and per-chain control words shared by the host runtime
+// and the sweep kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/kapdqmc.h"
+
+#define KDQ_MAX_NS 192          // largest lattice (6 row groups of 32 per lane)
+#define KDQ_MAX_OBS 10          // measurement columns per sweep row
+#define KDQ_THREADS 256         // threads per CTA (one CTA per chain)
+
+// device error flags (ChainCtl::err)
+#define KDQ_FLAG_NAN 1          // non-finite acceptance ratio
+#define KDQ_FLAG_SINGULAR 2     // zero pivot in the G recompute
+#define KDQ_FLAG_TAPE 4         // explicit tape exhausted
+
+enum { KDQ_MODE_INIT = 0, KDQ_MODE_FWD = 1, KDQ_MODE_BWD = 2 };
+
+struct ChainCtl {
+  int idx;              // current stabilisation index (1-based, as the reference)
+  int err;              // KDQ_FLAG_* bits
+  long long sweep;      // Philox sweep counter
+  long long n_prop, n_acc, n_recompute;
+  long long tape_pos;   // explicit-tape cursor
+  long long log_pos;    // accept-log cursor
+  int drift_pos;        // drift-log cursor
+  int obs_slot;         // next measurement row of this call
+  int obs_cnt;          // measurements accumulated in the current sweep
+  int pad;
+  double max_drift;
+  double obs_acc[KDQ_MAX_OBS];
+};
+
+struct SweepParams {
+  // model
+  int kind, Ns, Nt, z, n_field, NN, n_obs, record;
+  int lattice, L1, L2;
+  int site_nb;                  // tUV: entries per site in site_bonds
+  const int64_t* nodes;         // NN
+  const double* rtab;           // ratio tables (layout per model, see runtime)
+  const double* dtab;           // tU diagonal tables
+  const double* vtab;           // tV exponential tables
+  const double* gratio;         // 16: gamma[new]/gamma[old], index old*4+new
+  const double* xtab;           // 16: tUV real-type extra weight
+  const double* cosr;           // L1*L2 structure-factor phases
+  const double* eta;            // 4
+  double a, Ht, U, V;
+  const int* bx;                // 0-based bond ends
+  const int* by;
+  const int* site_bonds;        // tUV: per site, bond*2 + role (0 first, 1 second), -1 padded
+  const void* eK;
+  const void* eKinv;
+  const void* HalfeK;
+  const void* HalfeKinv;
+  const void* K;
+  const void* Pt;
+  // chain state (chain-major)
+  void* G;
+  void* W1;
+  void* W2;
+  void* Y;
+  void* Y2;
+  void* Mss;
+  void* X;
+  void* BLs_;
+  void* BRs_;
+  int* piv;
+  uint8_t* s;
+  ChainCtl* ctl;
+  size_t sz_NN, sz_Nn, sz_nn, sz_chainB;   // element strides per chain
+  // random stream
+  uint64_t seed;
+  const uint8_t* tape_k;
+  const double* tape_u;
+  size_t tape_len;
+  // outputs
+  double* obs;                  // chain-major rows of n_obs
+  int obs_cap;                  // rows per chain
+  uint8_t* acc_log;
+  long long acc_log_cap;
+  double* drift;
+  int drift_cap;
+
+  template <class T> __host__ __device__ T* BLs(int c) const { return static_cast<T*>(BLs_) + (size_t)c * sz_chainB; }
+  template <class T> __host__ __device__ T* BRs(int c) const { return static_cast<T*>(BRs_) + (size_t)c * sz_chainB; }
+};
+
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#endif

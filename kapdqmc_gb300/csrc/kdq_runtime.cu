@@ -1,0 +1,691 @@
+// Host runtime of libkapdqmc_gpu.so: handle lifecycle, model upload,
+// precomputed slice tables, launch sequencing of the sweep, and the C ABI
+// declared in include/kapdqmc.h.
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kdq_launch.h"
+#include "kdq_params.h"
+
+using cplx = std::complex<double>;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t b) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (b == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct kdq_handle {
+  int device = 0;
+  int nchains = 0;
+  int kind = 0, Ns = 0, ns = 0, Nt = 0, z = 1, n_field = 0, NN = 0, n_obs = 0;
+  bool gc = true, kc = false;
+  int maxrm = 1;
+  size_t esz = 16;   // bytes per G element
+  size_t dyn = 0;    // dynamic shared memory per CTA
+  cudaStream_t stream = nullptr;
+  std::string err;
+  SweepParams P{};
+  // model buffers
+  DevBuf nodes, rtab, dtab, vtab, gratio, xtab, cosr, eta, bx, by, site_bonds;
+  DevBuf eK, eKinv, HalfeK, HalfeKinv, K, Pt, PtH;
+  // chain buffers
+  DevBuf G, W1, W2, Y, Y2, Mss, X, piv, BLs, BRs, s, ctl;
+  // outputs
+  DevBuf obs, acc_log, drift, tape_k, tape_u;
+  int obs_rows = 0;      // rows recorded since kdq_init
+  int obs_capacity = 0;  // rows allocated
+  long long acc_log_cap = 0;
+  int drift_cap = 0;
+  uint64_t seed = 0;
+  bool use_tape = false;
+  size_t tape_len = 0;
+  double last_seconds = 0.0;
+  bool initialised = false;
+};
+
+namespace {
+
+int fail(kdq_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(kdq_handle* h, cudaError_t e, const char* what) {
+  return fail(h, KDQ_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define KDQ_CUDA(h, call)                                    \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return cuda_fail((h), _e, #call); \
+  } while (0)
+
+template <class V>
+cudaError_t upload(DevBuf& b, const V& v) {
+  cudaError_t e = b.alloc(v.size() * sizeof(v[0]));
+  if (e != cudaSuccess || v.empty()) return e;
+  return cudaMemcpy(b.p, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
+}
+
+// Model matrices as delivered: n x m, complex interleaved iff cplx_in; stored
+// on the device as complex (to_c) or real.
+cudaError_t upload_mat(DevBuf& b, const double* src, size_t n, bool cplx_in, bool to_c) {
+  std::vector<double> v(n * (to_c ? 2 : 1));
+  for (size_t i = 0; i < n; ++i) {
+    const double re = cplx_in ? src[2 * i] : src[i];
+    const double im = cplx_in ? src[2 * i + 1] : 0.0;
+    if (to_c) {
+      v[2 * i] = re;
+      v[2 * i + 1] = im;
+    } else {
+      v[i] = re;
+    }
+  }
+  return upload(b, v);
+}
+
+// Launch one stabilisation block for all chains.
+cudaError_t launch(kdq_handle* h, int mode, int k) {
+  switch (h->kind) {
+    case KDQ_TU:
+      return kdq::launch_tu(h->P, mode, k, h->maxrm, h->kc, h->nchains, h->dyn, h->stream);
+    case KDQ_TV:
+      return kdq::launch_tv(h->P, mode, k, h->maxrm, h->nchains, h->dyn, h->stream);
+    default:
+      return kdq::launch_tuv(h->P, mode, k, h->maxrm, h->gc, h->nchains, h->dyn, h->stream);
+  }
+}
+
+__global__ void k_seed_chains(void* BRs, void* BLs, const void* Pt, const void* PtH, size_t fs,
+                              size_t chainB, int NN, size_t esz) {
+  // BRs[1] = Pt, BLs[NN] = Pt^H for chain blockIdx.x (byte copies)
+  const size_t bytes = fs * esz;
+  uint8_t* br = static_cast<uint8_t*>(BRs) + (size_t)blockIdx.x * chainB * esz;
+  uint8_t* bl = static_cast<uint8_t*>(BLs) + ((size_t)blockIdx.x * chainB + (size_t)(NN - 1) * fs) * esz;
+  const uint8_t* pt = static_cast<const uint8_t*>(Pt);
+  const uint8_t* ph = static_cast<const uint8_t*>(PtH);
+  for (size_t i = threadIdx.x; i < bytes; i += blockDim.x) {
+    br[i] = pt[i];
+    bl[i] = ph[i];
+  }
+}
+
+__global__ void k_reset_ctl(ChainCtl* ctl, int n, int full) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  ChainCtl& x = ctl[c];
+  if (full) {
+    x.idx = 1;
+    x.obs_slot = 0;
+    x.obs_cnt = 0;
+    for (int q = 0; q < KDQ_MAX_OBS; ++q) x.obs_acc[q] = 0.0;
+  }
+  x.err = 0;
+  x.n_prop = x.n_acc = x.n_recompute = 0;
+  x.log_pos = 0;
+  x.drift_pos = 0;
+  x.max_drift = 0.0;
+}
+
+__global__ void k_set_sweep(ChainCtl* ctl, int n, long long sweep, int reset_tape) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  ctl[c].sweep = sweep;
+  if (reset_tape) ctl[c].tape_pos = 0;
+}
+
+int validate(const kdq_model_desc* m, int nchains, std::string& why) {
+  if (!m) { why = "model is NULL"; return 1; }
+  if (m->kind < KDQ_TU || m->kind > KDQ_TUV) { why = "unknown model kind"; return 1; }
+  if (m->Ns < 2 || (m->Ns & 1) || m->Ns > KDQ_MAX_NS) {
+    why = "Ns must be even and in [2, " + std::to_string(KDQ_MAX_NS) + "]";
+    return 1;
+  }
+  if (m->Nt < 1 || m->n_nodes < 2 || !m->nodes) { why = "need Nt >= 1 and >= 2 nodes"; return 1; }
+  if (m->nodes[0] != 0 || m->nodes[m->n_nodes - 1] != m->Nt) { why = "nodes must run from 0 to Nt"; return 1; }
+  for (int i = 1; i < m->n_nodes; ++i)
+    if (m->nodes[i] <= m->nodes[i - 1]) { why = "nodes must increase strictly"; return 1; }
+  if (nchains < 1) { why = "n_chains must be >= 1"; return 1; }
+  if (!m->eK || !m->eKinv || !m->HalfeK || !m->HalfeKinv || !m->K || !m->Pt || !m->gamma || !m->eta) {
+    why = "missing model array";
+    return 1;
+  }
+  if (m->kind != KDQ_TUV && !m->alpha) { why = "alpha is required for tU and tV"; return 1; }
+  if (m->kind != KDQ_TU && (!m->bonds || m->z < 1)) { why = "bonds and z are required for tV and tUV"; return 1; }
+  if (m->kind == KDQ_TU && !m->g_complex) { why = "the tU sweep is complex"; return 1; }
+  if (m->kind == KDQ_TV && (m->g_complex || m->k_complex)) { why = "the tV sweep is real"; return 1; }
+  if (m->kind == KDQ_TUV && m->k_complex) { why = "tUV kinetic matrices are real"; return 1; }
+  const int nb = m->kind == KDQ_TV ? (m->Ns / 2) * m->z : m->Ns * m->z;
+  if (m->kind != KDQ_TU)
+    for (int b = 0; b < 2 * nb; ++b)
+      if (m->bonds[b] < 1 || m->bonds[b] > m->Ns) { why = "bond index out of range"; return 1; }
+  if (m->kind == KDQ_TV) {
+    // every direction must be a perfect matching (the 2x2 block rotations
+    // rely on it; src/tV/model.jl:103-110 builds UV from such bonds)
+    std::vector<int> seen(m->Ns);
+    for (int j = 0; j < m->z; ++j) {
+      std::fill(seen.begin(), seen.end(), 0);
+      for (int i = 0; i < m->Ns / 2; ++i) {
+        const int* bnd = m->bonds + 2 * (j * (m->Ns / 2) + i);
+        if (seen[bnd[0] - 1]++ || seen[bnd[1] - 1]++) { why = "tV bond direction is not a perfect matching"; return 1; }
+      }
+    }
+  }
+  const bool hc = m->lattice == KDQ_HONEYCOMB120 || m->lattice == KDQ_HONEYCOMB60;
+  if (hc && 2 * m->site[0] * m->site[1] != m->Ns) { why = "site does not match Ns"; return 1; }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* kdq_last_error(const kdq_handle* h) {
+  if (h) return h->err.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_create_err.c_str();
+}
+
+void kdq_destroy(kdq_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+void* kdq_stream(kdq_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int kdq_n_obs(const kdq_handle* h) { return h ? h->n_obs : 0; }
+
+int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32_t device) {
+  auto set_err = [](int code, const std::string& msg) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = msg;
+    return code;
+  };
+  if (!out) return set_err(KDQ_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  std::string why;
+  if (validate(m, nchains, why)) return set_err(KDQ_ERR_ARG, why);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return set_err(KDQ_ERR_NOGPU, "no CUDA device");
+  if (device < 0 || device >= ndev) return set_err(KDQ_ERR_ARG, "device out of range");
+  cudaError_t ce = cudaSetDevice(device);
+  if (ce != cudaSuccess) return set_err(KDQ_ERR_CUDA, cudaGetErrorString(ce));
+
+  kdq_handle* h = new kdq_handle();
+  h->device = device;
+  h->nchains = nchains;
+  h->kind = m->kind;
+  h->Ns = m->Ns;
+  h->ns = m->Ns / 2;
+  h->Nt = m->Nt;
+  h->z = m->kind == KDQ_TU ? 1 : m->z;
+  h->NN = m->n_nodes;
+  h->gc = m->g_complex != 0;
+  h->kc = m->k_complex != 0;
+  h->esz = h->gc ? 16 : 8;
+  h->n_field = m->kind == KDQ_TU ? m->Ns : (m->kind == KDQ_TV ? (m->Ns / 2) * h->z : m->Ns * h->z);
+  h->n_obs = m->kind == KDQ_TU ? 6 : (m->kind == KDQ_TV ? 10 : 7);
+  h->maxrm = m->Ns <= 32 ? 1 : (m->Ns <= 96 ? 3 : 6);
+  h->dyn = ((size_t)h->n_field * 9 + 15) & ~(size_t)15;
+  auto bail = [&](int code) {
+    int rc = set_err(code, h->err);
+    kdq_destroy(h);
+    return rc;
+  };
+#define KDQ_CK(call)                                 \
+  do {                                               \
+    cudaError_t _e = (call);                         \
+    if (_e != cudaSuccess) {                         \
+      cuda_fail(h, _e, #call);                       \
+      return bail(KDQ_ERR_CUDA);                     \
+    }                                                \
+  } while (0)
+  KDQ_CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+
+  const int N = h->Ns, ns = h->ns, Nt = h->Nt;
+  const double* g = m->gamma;
+  const double* eta = m->eta;
+  // ---- tables
+  std::vector<double> gr(16), xt(16, 1.0);
+  for (int o = 0; o < 4; ++o)
+    for (int v = 0; v < 4; ++v) gr[o * 4 + v] = g[v] / g[o];
+  std::vector<int64_t> nodes(m->nodes, m->nodes + m->n_nodes);
+  KDQ_CK(upload(h->nodes, nodes));
+  KDQ_CK(upload(h->gratio, gr));
+  KDQ_CK(upload(h->eta, std::vector<double>(eta, eta + 4)));
+  if (m->kind == KDQ_TU) {
+    // D = cis(α η), 1 ./ D, cis(-α η), 1 ./ cis(-α η)  (src/tU/phy_update.jl:61-63,123-125)
+    std::vector<double> dt((size_t)Nt * 16 * 2), rt((size_t)Nt * 16 * 2);
+    for (int lt = 0; lt < Nt; ++lt) {
+      const double al = m->alpha[lt];
+      for (int v = 0; v < 4; ++v) {
+        const cplx dp = std::polar(1.0, al * eta[v]);
+        const cplx dm = std::polar(1.0, -al * eta[v]);
+        const cplx e4[4] = {dp, 1.0 / dp, dm, 1.0 / dm};
+        for (int q = 0; q < 4; ++q) {
+          dt[((size_t)lt * 16 + q * 4 + v) * 2] = e4[q].real();
+          dt[((size_t)lt * 16 + q * 4 + v) * 2 + 1] = e4[q].imag();
+        }
+      }
+      // get_r!: Δ = cis(α(η_new - η_old)) - 1  (src/tU/GreenMatrix.jl:49-54)
+      for (int o = 0; o < 4; ++o)
+        for (int v = 0; v < 4; ++v) {
+          const cplx d = std::polar(1.0, al * (eta[v] - eta[o])) - 1.0;
+          rt[((size_t)lt * 16 + o * 4 + v) * 2] = d.real();
+          rt[((size_t)lt * 16 + o * 4 + v) * 2 + 1] = d.imag();
+        }
+    }
+    KDQ_CK(upload(h->dtab, dt));
+    KDQ_CK(upload(h->rtab, rt));
+  } else if (m->kind == KDQ_TV) {
+    // bond exponentials (src/tV/phy_update.jl:64-71,133-138) and
+    // Δ entries exp(±Δs) - 1 (src/tV/GreenMatrix.jl:76-78)
+    std::vector<double> vt((size_t)Nt * 32), rt((size_t)Nt * 16 * 2);
+    for (int lt = 0; lt < Nt; ++lt) {
+      const double al = m->alpha[lt];
+      for (int v = 0; v < 4; ++v) {
+        const double x = al * eta[v];
+        const double fx = std::exp(x), fy = std::exp(-al * eta[v]);
+        double* t = vt.data() + (size_t)lt * 32;
+        t[v] = fx; t[4 + v] = fy; t[8 + v] = 1.0 / fx; t[12 + v] = 1.0 / fy;
+        const double bx_ = std::exp(-x), by_ = std::exp(-(-al * eta[v]));
+        t[16 + v] = bx_; t[20 + v] = by_; t[24 + v] = 1.0 / bx_; t[28 + v] = 1.0 / by_;
+      }
+      for (int o = 0; o < 4; ++o)
+        for (int v = 0; v < 4; ++v) {
+          const double ds = al * (eta[v] - eta[o]);
+          rt[((size_t)lt * 16 + o * 4 + v) * 2] = std::exp(ds) - 1.0;
+          rt[((size_t)lt * 16 + o * 4 + v) * 2 + 1] = std::exp(-ds) - 1.0;
+        }
+    }
+    KDQ_CK(upload(h->vtab, vt));
+    KDQ_CK(upload(h->rtab, rt));
+  } else {
+    // Δ = diag(e^{iΔs}-1, e^{iaΔs}-1) or the real exponentials, and the
+    // real-type weight exp((η_old-η_new)(a+1))  (src/tUV/GreenMatrix.jl:73-89,
+    // src/tUV/phy_update.jl:195-197)
+    std::vector<double> rt(16 * 2 * (h->gc ? 2 : 1));
+    for (int o = 0; o < 4; ++o)
+      for (int v = 0; v < 4; ++v) {
+        const double ds = eta[v] - eta[o];
+        const double t2[2] = {ds, ds * m->a};
+        for (int q = 0; q < 2; ++q) {
+          if (h->gc) {
+            const cplx d = std::polar(1.0, t2[q]) - 1.0;
+            rt[((o * 4 + v) * 2 + q) * 2] = d.real();
+            rt[((o * 4 + v) * 2 + q) * 2 + 1] = d.imag();
+          } else {
+            rt[(o * 4 + v) * 2 + q] = std::exp(t2[q]) - 1.0;
+          }
+        }
+        if (!h->gc) xt[o * 4 + v] = std::exp((eta[o] - eta[v]) * (m->a + 1.0));
+      }
+    KDQ_CK(upload(h->rtab, rt));
+  }
+  KDQ_CK(upload(h->xtab, xt));
+  // structure-factor phases cos(2π/L1 rx + 2π/L2 ry)
+  const int L1 = m->site[0] > 0 ? m->site[0] : 1, L2 = m->site[1] > 0 ? m->site[1] : 1;
+  std::vector<double> cr((size_t)L1 * L2);
+  for (int ry = 1; ry <= L2; ++ry)
+    for (int rx = 1; rx <= L1; ++rx)
+      cr[(rx - 1) + (size_t)(ry - 1) * L1] = std::cos(2 * M_PI / L1 * rx + 2 * M_PI / L2 * ry);
+  KDQ_CK(upload(h->cosr, cr));
+  // bonds (0-based) and the tUV per-site bond lists
+  int site_nb = 0;
+  if (m->kind != KDQ_TU) {
+    const int nb = m->kind == KDQ_TV ? (N / 2) * h->z : N * h->z;
+    std::vector<int> bx(nb), by(nb);
+    for (int b = 0; b < nb; ++b) {
+      bx[b] = m->bonds[2 * b] - 1;
+      by[b] = m->bonds[2 * b + 1] - 1;
+    }
+    KDQ_CK(upload(h->bx, bx));
+    KDQ_CK(upload(h->by, by));
+    if (m->kind == KDQ_TUV) {
+      std::vector<std::vector<int>> lists(N);
+      for (int b = 0; b < nb; ++b) {
+        lists[bx[b]].push_back(2 * b);
+        lists[by[b]].push_back(2 * b + 1);
+      }
+      for (auto& l : lists) site_nb = std::max<int>(site_nb, (int)l.size());
+      std::vector<int> flat((size_t)N * site_nb, -1);
+      for (int x = 0; x < N; ++x)
+        for (size_t q = 0; q < lists[x].size(); ++q) flat[(size_t)x * site_nb + q] = lists[x][q];
+      KDQ_CK(upload(h->site_bonds, flat));
+    }
+  }
+  // ---- model matrices
+  const size_t NNe = (size_t)N * N;
+  KDQ_CK(upload_mat(h->eK, m->eK, NNe, h->kc, h->kc));
+  KDQ_CK(upload_mat(h->eKinv, m->eKinv, NNe, h->kc, h->kc));
+  KDQ_CK(upload_mat(h->HalfeK, m->HalfeK, NNe, h->kc, h->kc));
+  KDQ_CK(upload_mat(h->HalfeKinv, m->HalfeKinv, NNe, h->kc, h->kc));
+  KDQ_CK(upload_mat(h->K, m->K, NNe, h->kc, h->kc));
+  KDQ_CK(upload_mat(h->Pt, m->Pt, (size_t)N * ns, h->gc, h->gc));
+  {  // Pt^H (ns x N)
+    std::vector<double> ph((size_t)N * ns * (h->gc ? 2 : 1));
+    for (int i = 0; i < N; ++i)
+      for (int c = 0; c < ns; ++c) {
+        const size_t src = i + (size_t)c * N, dst = c + (size_t)i * ns;
+        if (h->gc) {
+          ph[2 * dst] = m->Pt[2 * src];
+          ph[2 * dst + 1] = -m->Pt[2 * src + 1];
+        } else {
+          ph[dst] = m->Pt[src];
+        }
+      }
+    KDQ_CK(upload(h->PtH, ph));
+  }
+  // ---- chain state
+  const size_t C = nchains, e = h->esz;
+  const size_t chainB = (size_t)h->NN * N * ns;
+  KDQ_CK(h->G.alloc(C * NNe * e));
+  KDQ_CK(h->W1.alloc(C * NNe * e));
+  KDQ_CK(h->W2.alloc(C * NNe * e));
+  KDQ_CK(h->Y.alloc(C * N * ns * e));
+  KDQ_CK(h->Y2.alloc(C * N * ns * e));
+  KDQ_CK(h->X.alloc(C * N * ns * e));
+  KDQ_CK(h->Mss.alloc(C * ns * ns * e));
+  KDQ_CK(h->piv.alloc(C * ns * sizeof(int)));
+  KDQ_CK(h->BLs.alloc(C * chainB * e));
+  KDQ_CK(h->BRs.alloc(C * chainB * e));
+  KDQ_CK(h->s.alloc(C * Nt * h->n_field));
+  KDQ_CK(h->ctl.alloc(C * sizeof(ChainCtl)));
+  KDQ_CK(cudaMemset(h->ctl.p, 0, C * sizeof(ChainCtl)));
+  KDQ_CK(cudaMemset(h->G.p, 0, C * NNe * e));
+  KDQ_CK(h->obs.alloc(8));
+
+  SweepParams& P = h->P;
+  P.kind = h->kind; P.Ns = N; P.Nt = Nt; P.z = h->z; P.n_field = h->n_field; P.NN = h->NN;
+  P.n_obs = h->n_obs; P.record = 0; P.lattice = m->lattice; P.L1 = L1; P.L2 = L2; P.site_nb = site_nb;
+  P.nodes = h->nodes.as<int64_t>(); P.rtab = h->rtab.as<double>(); P.dtab = h->dtab.as<double>();
+  P.vtab = h->vtab.as<double>(); P.gratio = h->gratio.as<double>(); P.xtab = h->xtab.as<double>();
+  P.cosr = h->cosr.as<double>(); P.eta = h->eta.as<double>();
+  P.a = m->a; P.Ht = m->Ht; P.U = m->U; P.V = m->V;
+  P.bx = h->bx.as<int>(); P.by = h->by.as<int>(); P.site_bonds = h->site_bonds.as<int>();
+  P.eK = h->eK.p; P.eKinv = h->eKinv.p; P.HalfeK = h->HalfeK.p; P.HalfeKinv = h->HalfeKinv.p;
+  P.K = h->K.p; P.Pt = h->Pt.p;
+  P.G = h->G.p; P.W1 = h->W1.p; P.W2 = h->W2.p; P.Y = h->Y.p; P.Y2 = h->Y2.p; P.Mss = h->Mss.p;
+  P.X = h->X.p; P.BLs_ = h->BLs.p; P.BRs_ = h->BRs.p; P.piv = h->piv.as<int>();
+  P.s = h->s.as<uint8_t>(); P.ctl = h->ctl.as<ChainCtl>();
+  P.sz_NN = NNe; P.sz_Nn = (size_t)N * ns; P.sz_nn = (size_t)ns * ns; P.sz_chainB = chainB;
+  P.seed = 0; P.tape_k = nullptr; P.tape_u = nullptr; P.tape_len = 0;
+  P.obs = h->obs.as<double>(); P.obs_cap = 0;
+  P.acc_log = nullptr; P.acc_log_cap = 0; P.drift = nullptr; P.drift_cap = 0;
+  KDQ_CK(cudaDeviceSynchronize());
+#undef KDQ_CK
+  *out = h;
+  return KDQ_OK;
+}
+
+int kdq_set_fields(kdq_handle* h, const uint8_t* s, size_t nbytes) {
+  if (!h || !s) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  const size_t want = (size_t)h->nchains * h->Nt * h->n_field;
+  if (nbytes != want) return fail(h, KDQ_ERR_ARG, "field size mismatch: expected " + std::to_string(want));
+  for (size_t i = 0; i < nbytes; ++i)
+    if (s[i] < 1 || s[i] > 4) return fail(h, KDQ_ERR_ARG, "HS field values must be in 1..4");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaMemcpyAsync(h->s.p, s, nbytes, cudaMemcpyHostToDevice, h->stream));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->initialised = false;
+  return KDQ_OK;
+}
+
+int kdq_get_fields(kdq_handle* h, uint8_t* s, size_t nbytes) {
+  if (!h || !s) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  const size_t want = (size_t)h->nchains * h->Nt * h->n_field;
+  if (nbytes != want) return fail(h, KDQ_ERR_ARG, "field size mismatch: expected " + std::to_string(want));
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaMemcpyAsync(s, h->s.p, nbytes, cudaMemcpyDeviceToHost, h->stream));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  return KDQ_OK;
+}
+
+int kdq_set_rng(kdq_handle* h, uint64_t seed, uint64_t sweep_offset) {
+  if (!h) return KDQ_ERR_ARG;
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  h->seed = seed;
+  h->use_tape = false;
+  h->P.seed = seed;
+  h->P.tape_k = nullptr;
+  h->P.tape_u = nullptr;
+  h->P.tape_len = 0;
+  k_set_sweep<<<(h->nchains + 127) / 128, 128, 0, h->stream>>>(h->ctl.as<ChainCtl>(), h->nchains,
+                                                              (long long)sweep_offset, 1);
+  KDQ_CUDA(h, cudaGetLastError());
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  return KDQ_OK;
+}
+
+int kdq_set_tape(kdq_handle* h, const uint8_t* k, const double* u, size_t n_per_chain) {
+  if (!h || !k || !u) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  for (size_t i = 0; i < n_per_chain * h->nchains; ++i) {
+    if (k[i] > 2) return fail(h, KDQ_ERR_ARG, "tape choice index must be 0, 1 or 2");
+    if (!(u[i] >= 0.0 && u[i] < 1.0)) return fail(h, KDQ_ERR_ARG, "tape uniforms must lie in [0, 1)");
+  }
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  const size_t n = n_per_chain * h->nchains;
+  KDQ_CUDA(h, h->tape_k.alloc(n));
+  KDQ_CUDA(h, h->tape_u.alloc(n * sizeof(double)));
+  KDQ_CUDA(h, cudaMemcpy(h->tape_k.p, k, n, cudaMemcpyHostToDevice));
+  KDQ_CUDA(h, cudaMemcpy(h->tape_u.p, u, n * sizeof(double), cudaMemcpyHostToDevice));
+  h->use_tape = true;
+  h->tape_len = n_per_chain;
+  h->P.tape_k = h->tape_k.as<uint8_t>();
+  h->P.tape_u = h->tape_u.as<double>();
+  h->P.tape_len = n_per_chain;
+  k_set_sweep<<<(h->nchains + 127) / 128, 128, 0, h->stream>>>(h->ctl.as<ChainCtl>(), h->nchains, 0, 1);
+  KDQ_CUDA(h, cudaGetLastError());
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  return KDQ_OK;
+}
+
+int kdq_enable_accept_log(kdq_handle* h, size_t n_per_chain) {
+  if (!h) return KDQ_ERR_ARG;
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, h->acc_log.alloc(n_per_chain * h->nchains));
+  if (n_per_chain) KDQ_CUDA(h, cudaMemset(h->acc_log.p, 0xff, n_per_chain * h->nchains));
+  h->acc_log_cap = (long long)n_per_chain;
+  h->P.acc_log = n_per_chain ? h->acc_log.as<uint8_t>() : nullptr;
+  h->P.acc_log_cap = h->acc_log_cap;
+  return KDQ_OK;
+}
+
+int kdq_get_accept_log(kdq_handle* h, uint8_t* flags, size_t nbytes) {
+  if (!h || !flags) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  if (nbytes != (size_t)h->acc_log_cap * h->nchains) return fail(h, KDQ_ERR_ARG, "accept-log size mismatch");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  KDQ_CUDA(h, cudaMemcpy(flags, h->acc_log.p, nbytes, cudaMemcpyDeviceToHost));
+  return KDQ_OK;
+}
+
+int kdq_init(kdq_handle* h) {
+  if (!h) return KDQ_ERR_ARG;
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  const size_t fs = (size_t)h->Ns * h->ns;
+  k_seed_chains<<<h->nchains, 256, 0, h->stream>>>(h->BRs.p, h->BLs.p, h->Pt.p, h->PtH.p, fs,
+                                                   h->P.sz_chainB, h->NN, h->esz);
+  KDQ_CUDA(h, cudaGetLastError());
+  k_reset_ctl<<<(h->nchains + 127) / 128, 128, 0, h->stream>>>(h->ctl.as<ChainCtl>(), h->nchains, 1);
+  KDQ_CUDA(h, cudaGetLastError());
+  h->obs_rows = 0;
+  // left chain BLs[NN-1..1] and G at tau = 0  (src/tU/phy_update.jl:39-50)
+  for (int k = h->NN - 1; k >= 1; --k) KDQ_CUDA(h, launch(h, KDQ_MODE_INIT, k));
+  h->initialised = true;
+  return KDQ_OK;
+}
+
+int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
+  if (!h) return KDQ_ERR_ARG;
+  if (sweeps < 0) return fail(h, KDQ_ERR_ARG, "sweeps must be >= 0");
+  if (!h->initialised) return fail(h, KDQ_ERR_STATE, "kdq_init must precede kdq_sweep");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  if (h->use_tape) {
+    // host-side check of the tape length against what the sweeps consume
+    std::vector<ChainCtl> ctl(h->nchains);
+    KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    KDQ_CUDA(h, cudaMemcpy(ctl.data(), h->ctl.p, ctl.size() * sizeof(ChainCtl), cudaMemcpyDeviceToHost));
+    const size_t need = (size_t)sweeps * 2 * h->Nt * h->n_field;
+    if ((size_t)ctl[0].tape_pos + need > h->tape_len)
+      return fail(h, KDQ_ERR_STATE, "proposal tape too short for the requested sweeps");
+  }
+  k_reset_ctl<<<(h->nchains + 127) / 128, 128, 0, h->stream>>>(h->ctl.as<ChainCtl>(), h->nchains, 0);
+  KDQ_CUDA(h, cudaGetLastError());
+  // drift log for this call
+  const int dcap = sweeps * 2 * (h->NN - 1);
+  if ((size_t)dcap * h->nchains * sizeof(double) > h->drift.bytes) {
+    KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    KDQ_CUDA(h, h->drift.alloc((size_t)dcap * h->nchains * sizeof(double)));
+  }
+  h->drift_cap = dcap;
+  h->P.drift = h->drift.as<double>();
+  h->P.drift_cap = dcap;
+  // observables: rows for every sweep recorded since kdq_init (chain-major,
+  // obs_cap rows per chain); grown by copying the old rows over
+  if (record) {
+    const int need_rows = h->obs_rows + sweeps;
+    if (need_rows > h->obs_capacity) {
+      const int cap = std::max(need_rows, 2 * h->obs_capacity);
+      DevBuf nb;
+      KDQ_CUDA(h, nb.alloc((size_t)cap * h->nchains * h->n_obs * sizeof(double)));
+      KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+      if (h->obs_rows > 0)
+        KDQ_CUDA(h, cudaMemcpy2D(nb.p, (size_t)cap * h->n_obs * sizeof(double), h->obs.p,
+                                 (size_t)h->obs_capacity * h->n_obs * sizeof(double),
+                                 (size_t)h->obs_rows * h->n_obs * sizeof(double), h->nchains,
+                                 cudaMemcpyDeviceToDevice));
+      std::swap(h->obs.p, nb.p);
+      std::swap(h->obs.bytes, nb.bytes);
+      h->obs_capacity = cap;
+    }
+    h->P.obs = h->obs.as<double>();
+    h->P.obs_cap = h->obs_capacity;
+  }
+  h->P.record = record ? 1 : 0;
+  auto t0 = std::chrono::steady_clock::now();
+  for (int w = 0; w < sweeps; ++w) {
+    for (int k = 1; k <= h->NN - 1; ++k) KDQ_CUDA(h, launch(h, KDQ_MODE_FWD, k));
+    for (int k = h->NN - 1; k >= 1; --k) KDQ_CUDA(h, launch(h, KDQ_MODE_BWD, k));
+  }
+  if (record) h->obs_rows += sweeps;
+  h->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return KDQ_OK;
+}
+
+int kdq_synchronize(kdq_handle* h) {
+  if (!h) return KDQ_ERR_ARG;
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<ChainCtl> ctl(h->nchains);
+  KDQ_CUDA(h, cudaMemcpy(ctl.data(), h->ctl.p, ctl.size() * sizeof(ChainCtl), cudaMemcpyDeviceToHost));
+  int flags = 0;
+  for (auto& c : ctl) flags |= c.err;
+  if (flags & KDQ_FLAG_TAPE) return fail(h, KDQ_ERR_STATE, "proposal tape exhausted");
+  if (flags & KDQ_FLAG_NAN) return fail(h, KDQ_ERR_NUMERIC, "non-finite acceptance ratio");
+  if (flags & KDQ_FLAG_SINGULAR) return fail(h, KDQ_ERR_NUMERIC, "singular BL*BR in the G recompute");
+  return KDQ_OK;
+}
+
+int kdq_get_obs(kdq_handle* h, double* obs, size_t obs_len) {
+  if (!h || !obs) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  const size_t want = (size_t)h->nchains * h->obs_rows * h->n_obs;
+  if (obs_len < want) return fail(h, KDQ_ERR_ARG, "obs buffer too small: need " + std::to_string(want));
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (want == 0) return KDQ_OK;
+  KDQ_CUDA(h, cudaMemcpy2D(obs, (size_t)h->obs_rows * h->n_obs * sizeof(double), h->obs.p,
+                           (size_t)h->obs_capacity * h->n_obs * sizeof(double),
+                           (size_t)h->obs_rows * h->n_obs * sizeof(double), h->nchains,
+                           cudaMemcpyDeviceToHost));
+  return KDQ_OK;
+}
+
+int kdq_phy_update(kdq_handle* h, int32_t sweeps, int32_t record, double* obs, size_t obs_len) {
+  if (!h) return KDQ_ERR_ARG;
+  if (record && (!obs || obs_len < (size_t)h->nchains * sweeps * h->n_obs))
+    return fail(h, KDQ_ERR_ARG, "obs buffer too small");
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = kdq_init(h);
+  if (rc) return rc;
+  rc = kdq_sweep(h, sweeps, record);
+  if (rc) return rc;
+  rc = kdq_synchronize(h);
+  if (rc) return rc;
+  if (record) {
+    rc = kdq_get_obs(h, obs, obs_len);
+    if (rc) return rc;
+  }
+  h->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return KDQ_OK;
+}
+
+int kdq_get_green(kdq_handle* h, int32_t chain, double* G, size_t len) {
+  if (!h || !G) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  if (chain < 0 || chain >= h->nchains) return fail(h, KDQ_ERR_ARG, "chain out of range");
+  const size_t n = (size_t)h->Ns * h->Ns * (h->gc ? 2 : 1);
+  if (len != n) return fail(h, KDQ_ERR_ARG, "G buffer must hold " + std::to_string(n) + " doubles");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  KDQ_CUDA(h, cudaMemcpy(G, static_cast<uint8_t*>(h->G.p) + (size_t)chain * h->Ns * h->Ns * h->esz,
+                         n * sizeof(double), cudaMemcpyDeviceToHost));
+  return KDQ_OK;
+}
+
+int kdq_get_drift(kdq_handle* h, double* drift, size_t len) {
+  if (!h || !drift) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  const size_t n = (size_t)h->drift_cap * h->nchains;
+  if (len != n) return fail(h, KDQ_ERR_ARG, "drift buffer must hold " + std::to_string(n) + " doubles");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (n) KDQ_CUDA(h, cudaMemcpy(drift, h->drift.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return KDQ_OK;
+}
+
+int kdq_get_stats(kdq_handle* h, kdq_stats* st) {
+  if (!h || !st) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<ChainCtl> ctl(h->nchains);
+  KDQ_CUDA(h, cudaMemcpy(ctl.data(), h->ctl.p, ctl.size() * sizeof(ChainCtl), cudaMemcpyDeviceToHost));
+  std::memset(st, 0, sizeof(*st));
+  for (auto& c : ctl) {
+    st->proposals += c.n_prop;
+    st->accepted += c.n_acc;
+    st->recomputes += c.n_recompute;
+    if (!(c.max_drift <= st->max_drift)) st->max_drift = c.max_drift;
+  }
+  st->seconds = h->last_seconds;
+  return KDQ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,791 @@
+// Sweep kernels: one CTA per Markov chain, one launch per stabilisation
+// block.  A launch runs the block's time slices (wrap, local updates,
+// optional measurement) and then the QR-stabilised recompute of G at the
+// block's closing node, so a full sweep is 2*(NN-1) launches of the same
+// kernel (NN = number of nodes).  All arithmetic is FP64 (complex128 or
+// float64, as the model's sweep requires).
+//
+// Reference (KAPDQMC): src/tU/phy_update.jl:3-267, src/tU/GreenMatrix.jl,
+// src/tV/phy_update.jl:1-314, src/tV/GreenMatrix.jl,
+// src/tUV/phy_update.jl:1-355, src/tUV/GreenMatrix.jl, src/public/Gupdate.jl.
+#pragma once
+#include "kdq_device.cuh"
+#include "kdq_params.h"
+
+namespace kdq {
+
+constexpr uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u;
+constexpr uint32_t PH_W0 = 0x9E3779B9u, PH_W1 = 0xBB67AE85u;
+constexpr uint32_t TAPE_STREAM = 0x4B445131u;
+
+// Philox4x32-10 (Salmon et al., SC'11).
+__device__ inline uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += PH_W0; k1 += PH_W1; }
+    const uint32_t hi0 = __umulhi(PH_M0, c.x), lo0 = PH_M0 * c.x;
+    const uint32_t hi1 = __umulhi(PH_M1, c.z), lo1 = PH_M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+  }
+  return c;
+}
+
+// Per-CTA shared scratch (static part; the tape slice is dynamic).
+template <class T>
+struct Smem {
+  double red[32];
+  double wn[KDQ_MAX_NS / 2];
+  T w0;
+  T dvec[KDQ_MAX_NS];   // row scaling of the current slice
+  T dinv[KDQ_MAX_NS];   // column scaling
+  T ucol[2][KDQ_MAX_NS];
+  T wrow[2][KDQ_MAX_NS];
+  T rr[4];
+  int accept[2];
+  int newv;
+  int bad;
+};
+
+template <int KIND, class T, class KT>
+struct Ctx {
+  const SweepParams& P;
+  Smem<T>& sm;
+  uint8_t* tk;     // tape slice: choice index
+  double* tu;      // tape slice: uniform
+  int chain;
+  ChainCtl* ctl;
+  T* G;
+  T* W1;
+  T* W2;
+  T* Y;
+  T* Y2;
+  T* Mss;
+  T* X;
+  int* piv;
+  uint8_t* s;      // this chain's field, Nt x n_field
+  const KT* eK;
+  const KT* eKinv;
+  const KT* HalfeK;
+  const KT* HalfeKinv;
+  const KT* Kmat;
+  const T* Pt;
+};
+
+// ---------------------------------------------------------------- tables
+// Forward (sign=+1) / backward (sign=-1) diagonal factor of slice lt
+// (1-based) into sm.dvec, and its elementwise inverse into sm.dinv.
+template <int KIND, class T, class KT>
+__device__ void slice_diag(Ctx<KIND, T, KT>& c, int lt, int sign) {
+  const SweepParams& P = c.P;
+  const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field;
+  if constexpr (KIND == KDQ_TU) {
+    // D = cis(±α η_s), 1 ./ D  (src/tU/phy_update.jl:61-63,123-125)
+    const cd* tab = reinterpret_cast<const cd*>(P.dtab) + (size_t)(lt - 1) * 16 + (sign > 0 ? 0 : 8);
+    for (int i = threadIdx.x; i < P.Ns; i += blockDim.x) {
+      const int v = sl[i] - 1;
+      c.sm.dvec[i] = tab[v];
+      c.sm.dinv[i] = tab[4 + v];
+    }
+  } else if constexpr (KIND == KDQ_TUV) {
+    // phase per site: Σ η over bonds starting at x + a Σ η over bonds ending
+    // at x, accumulated in bond order (src/tUV/phy_update.jl:68-78)
+    for (int x = threadIdx.x; x < P.Ns; x += blockDim.x) {
+      double th = 0.0;
+      const int* lst = P.site_bonds + (size_t)x * P.site_nb;
+      for (int m = 0; m < P.site_nb; ++m) {
+        const int e = lst[m];
+        if (e < 0) break;
+        const double ev = P.eta[sl[e >> 1] - 1];
+        th += (e & 1) ? P.a * ev : ev;
+      }
+      T d, di;
+      if constexpr (sizeof(T) == sizeof(cd)) {
+        double sn, cs;
+        sincos(sign * th, &sn, &cs);
+        cd dd{cs, sn};
+        d = dd;
+        di = cd{1.0, 0.0} / dd;
+      } else {
+        const double dd = exp(sign * th);
+        d = dd;
+        di = 1.0 / dd;
+      }
+      c.sm.dvec[x] = d;
+      c.sm.dinv[x] = di;
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ wraps
+// G <- B_lt G B_lt^{-1}, B = D eK (tU, tUV): WrapKV!("Forward","B"),
+// src/tU/GreenMatrix.jl:64-69.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void wrap_fwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
+  const int N = c.P.Ns;
+  slice_diag(c, lt, +1);
+  bgemm<MAXRM>(N, N, N, c.eK, N, G, N, W, N);                       // eK G
+  bgemm<MAXRM>(N, N, N, W, N, c.eKinv, N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
+}
+
+// G <- B_lt^{-1} G B_lt: WrapKV!("Backward","B"), src/tU/GreenMatrix.jl:78-83.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void wrap_bwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
+  const int N = c.P.Ns;
+  slice_diag(c, lt, -1);
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+    const int i = e % N, j = e / N;
+    G[e] = (c.sm.dvec[i] * G[e]) * c.sm.dinv[j];
+  }
+  __syncthreads();
+  bgemm<MAXRM>(N, N, N, c.eKinv, N, G, N, W, N);
+  bgemm<MAXRM>(N, N, N, W, N, c.eK, N, G, N);
+}
+
+// tV bond rotation of direction j on both sides of G:
+// G <- UV D UV G UV D^-1 UV with UV a direct sum of 2x2 blocks
+// u = [-c -c; -c c]: WrapV!(..,"B"), src/tV/GreenMatrix.jl:110-118.  Every
+// 2x2 block of G (bond i rows, bond i' columns) transforms independently.
+template <int KIND, class T, class KT>
+__device__ void tv_rotate(Ctx<KIND, T, KT>& c, T* G, int lt, int j, int sign) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, nb = N / 2;
+  const double h = 0.70710678118654752440;  // 2^0.5/2
+  const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * nb;
+  // vtab per slice: [D_x | D_y | 1/D_x | 1/D_y] forward, then the same backward
+  const double* tab = P.vtab + (size_t)(lt - 1) * 32 + (sign > 0 ? 0 : 16);
+  const int* bx = P.bx + (size_t)j * nb;
+  const int* by = P.by + (size_t)j * nb;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e % nb, ip = e / nb;
+    const int x = bx[i], y = by[i], xp = bx[ip], yp = by[ip];
+    const double dx = tab[sl[i] - 1], dy = tab[4 + sl[i] - 1];          // D on rows x, y
+    const double cxp = tab[8 + sl[ip] - 1], cyp = tab[12 + sl[ip] - 1]; // 1 ./ D on columns x', y'
+    double g00 = re(G[x + (size_t)xp * N]), g01 = re(G[x + (size_t)yp * N]);
+    double g10 = re(G[y + (size_t)xp * N]), g11 = re(G[y + (size_t)yp * N]);
+    // UV * G
+    double a00 = -h * g00 - h * g10, a01 = -h * g01 - h * g11;
+    double a10 = -h * g00 + h * g10, a11 = -h * g01 + h * g11;
+    // * UV
+    g00 = -h * a00 - h * a01; g01 = -h * a00 + h * a01;
+    g10 = -h * a10 - h * a11; g11 = -h * a10 + h * a11;
+    // D * G * D^-1
+    g00 = (dx * g00) * cxp; g01 = (dx * g01) * cyp;
+    g10 = (dy * g10) * cxp; g11 = (dy * g11) * cyp;
+    // UV * G * UV
+    a00 = -h * g00 - h * g10; a01 = -h * g01 - h * g11;
+    a10 = -h * g00 + h * g10; a11 = -h * g01 + h * g11;
+    g00 = -h * a00 - h * a01; g01 = -h * a00 + h * a01;
+    g10 = -h * a10 - h * a11; g11 = -h * a10 + h * a11;
+    G[x + (size_t)xp * N] = from_real<T>(g00);
+    G[x + (size_t)yp * N] = from_real<T>(g01);
+    G[y + (size_t)xp * N] = from_real<T>(g10);
+    G[y + (size_t)yp * N] = from_real<T>(g11);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------- local updates
+// Proposal decision and rank-k update (k = 1 for tU, 2 for tV and tUV).
+// Warp 0 evaluates the acceptance ratio (get_r!) and, on acceptance,
+// u' = G[:,S] r into shared memory while the other warps stage the rows
+// G[S,:]; then every thread applies G -= u' (E_S - G[S,:]) (Gupdate!,
+// src/public/Gupdate.jl:5-11).
+template <int KIND, class T, class KT>
+__device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t* sfield,
+                        uint8_t tk, double tu, int logpos, int par) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int RK = (KIND == KDQ_TU) ? 1 : 2;
+  Smem<T>& sm = c.sm;
+  if (warp == 0) {
+    const int sold = *sfield;
+    const int sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
+    const int o = sold - 1, nv = sx - 1;
+    double p;
+    T r00, r01 = zero<T>(), r10 = zero<T>(), r11 = zero<T>();
+    if constexpr (KIND == KDQ_TU) {
+      // get_r!, src/tU/GreenMatrix.jl:49-54; γ ratio src/tU/phy_update.jl:261
+      const cd Δ = reinterpret_cast<const cd*>(P.rtab)[(size_t)(lt - 1) * 16 + o * 4 + nv];
+      const cd g = G[x + (size_t)x * N];
+      const cd pc = cd{1.0, 0.0} + Δ * (cd{1.0, 0.0} - g);
+      r00 = Δ / pc;
+      p = abs2(pc) * P.gratio[o * 4 + nv];
+    } else if constexpr (KIND == KDQ_TV) {
+      // get_r!, src/tV/GreenMatrix.jl:76-89
+      const double h = 0.70710678118654752440;
+      const double* t2 = P.rtab + ((size_t)(lt - 1) * 16 + o * 4 + nv) * 2;
+      // Δ = uv diag(t2) uv, uv = [-h -h; -h h]
+      const double q00 = -h * t2[0], q01 = -h * t2[1], q10 = -h * t2[0], q11 = h * t2[1];
+      const double d00 = q00 * -h + q01 * -h, d01 = q00 * -h + q01 * h;
+      const double d10 = q10 * -h + q11 * -h, d11 = q10 * -h + q11 * h;
+      const double gxx = re(G[x + (size_t)x * N]), gxy = re(G[x + (size_t)y * N]);
+      const double gyx = re(G[y + (size_t)x * N]), gyy = re(G[y + (size_t)y * N]);
+      double a00 = d00 - (d00 * gxx + d01 * gyx), a01 = d01 - (d00 * gxy + d01 * gyy);
+      double a10 = d10 - (d10 * gxx + d11 * gyx), a11 = d11 - (d10 * gxy + d11 * gyy);
+      a00 += 1.0;
+      a11 += 1.0;
+      const double det = a00 * a11 - a01 * a10;
+      const double i00 = a11 / det, i01 = -a01 / det, i10 = -a10 / det, i11 = a00 / det;
+      r00 = from_real<T>(i00 * d00 + i01 * d10);
+      r01 = from_real<T>(i00 * d01 + i01 * d11);
+      r10 = from_real<T>(i10 * d00 + i11 * d10);
+      r11 = from_real<T>(i10 * d01 + i11 * d11);
+      p = det * P.gratio[o * 4 + nv];
+    } else {
+      // get_r!, src/tUV/GreenMatrix.jl:73-89; weight src/tUV/phy_update.jl:193-197
+      const T* t2 = reinterpret_cast<const T*>(P.rtab) + (size_t)(o * 4 + nv) * 2;
+      const T gxx = G[x + (size_t)x * N], gxy = G[x + (size_t)y * N];
+      const T gyx = G[y + (size_t)x * N], gyy = G[y + (size_t)y * N];
+      T a00 = t2[0] - t2[0] * gxx, a01 = zero<T>() - t2[0] * gxy;
+      T a10 = zero<T>() - t2[1] * gyx, a11 = t2[1] - t2[1] * gyy;
+      a00 = a00 + one<T>();
+      a11 = a11 + one<T>();
+      const T det = a00 * a11 - a01 * a10;
+      const T i00 = a11 / det, i01 = (zero<T>() - a01) / det;
+      const T i10 = (zero<T>() - a10) / det, i11 = a00 / det;
+      r00 = i00 * t2[0];
+      r01 = i01 * t2[1];
+      r10 = i10 * t2[0];
+      r11 = i11 * t2[1];
+      p = abs2(det) * P.gratio[o * 4 + nv] * P.xtab[o * 4 + nv];
+    }
+    int acc = tu < p;
+    if (!isfinite(p)) {
+      acc = 0;
+      if (lane == 0) atomicOr(&c.ctl->err, KDQ_FLAG_NAN);
+    }
+    if (acc) {
+      // u' = G[:,S] r
+      for (int a = lane; a < N; a += 32) {
+        const T gx = G[a + (size_t)x * N];
+        if constexpr (RK == 1) {
+          sm.ucol[0][a] = gx * r00;
+        } else {
+          const T gy = G[a + (size_t)y * N];
+          sm.ucol[0][a] = gx * r00 + gy * r10;
+          sm.ucol[1][a] = gx * r01 + gy * r11;
+        }
+      }
+    }
+    if (lane == 0) {
+      sm.accept[par] = acc;
+      sm.newv = sx;
+      if (c.P.acc_log && logpos >= 0 && logpos < c.P.acc_log_cap)
+        c.P.acc_log[(size_t)c.chain * c.P.acc_log_cap + logpos] = (uint8_t)acc;
+      c.ctl->n_prop += 1;
+      c.ctl->n_acc += acc;
+    }
+  } else {
+    for (int b = tid - 32; b < N; b += blockDim.x - 32) {
+      sm.wrow[0][b] = G[x + (size_t)b * N];
+      if constexpr (RK == 2) sm.wrow[1][b] = G[y + (size_t)b * N];
+    }
+  }
+  __syncthreads();
+  if (sm.accept[par]) {
+    for (int e = tid; e < N * N; e += blockDim.x) {
+      const int a = e % N, b = e / N;
+      T v = G[e];
+      const T w0 = (b == x ? one<T>() : zero<T>()) - sm.wrow[0][b];
+      v = v - sm.ucol[0][a] * w0;
+      if constexpr (RK == 2) {
+        const T w1 = (b == y ? one<T>() : zero<T>()) - sm.wrow[1][b];
+        v = v - sm.ucol[1][a] * w1;
+      }
+      G[e] = v;
+    }
+    if (tid == 0) *sfield = (uint8_t)sm.newv;
+    __syncthreads();
+  }
+}
+
+// Fill the shared tape slice with n proposals starting at sweep-relative
+// index q0 (Philox) or at the chain's explicit-tape cursor.
+template <int KIND, class T, class KT>
+__device__ void load_tape(Ctx<KIND, T, KT>& c, uint32_t q0, int n) {
+  const SweepParams& P = c.P;
+  if (P.tape_k) {
+    const size_t base = (size_t)c.chain * P.tape_len + c.ctl->tape_pos;
+    const bool ok = c.ctl->tape_pos + (size_t)n <= P.tape_len;
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+      c.tk[m] = ok ? P.tape_k[base + m] : 0;
+      c.tu[m] = ok ? P.tape_u[base + m] : 2.0;   // u = 2 rejects
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(&c.ctl->err, KDQ_FLAG_TAPE);
+  } else {
+    const uint32_t sw = (uint32_t)c.ctl->sweep;
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+      const uint4 r = philox(make_uint4(q0 + m, sw, (uint32_t)c.chain, TAPE_STREAM),
+                             (uint32_t)P.seed, (uint32_t)(P.seed >> 32));
+      c.tk[m] = (uint8_t)(((uint64_t)r.x * 3u) >> 32);
+      c.tu[m] = ((double)(r.y >> 5) * 67108864.0 + (double)(r.z >> 6)) * (1.0 / 9007199254740992.0);
+    }
+  }
+  __syncthreads();
+}
+
+template <int KIND, class T, class KT>
+__device__ void finish_tape(Ctx<KIND, T, KT>& c, int n) {
+  if (threadIdx.x == 0 && c.P.tape_k) c.ctl->tape_pos += n;
+}
+
+// All proposals of slice lt (tU, tUV) or of direction j of slice lt (tV).
+template <int KIND, class T, class KT>
+__device__ void update_layer(Ctx<KIND, T, KT>& c, int lt, int j, bool fwd) {
+  const SweepParams& P = c.P;
+  const int Nt = P.Nt, pf = P.n_field;
+  uint8_t* sl = c.s + (size_t)(lt - 1) * pf;
+  // sweep-relative index of the first proposal of this slice
+  const uint32_t qs = fwd ? (uint32_t)(lt - 1) * pf : (uint32_t)(Nt + (Nt - lt)) * pf;
+  int n, off;
+  if constexpr (KIND == KDQ_TV) {
+    n = P.Ns / 2;
+    off = (fwd ? (P.z - 1 - j) : j) * n;
+  } else {
+    n = pf;
+    off = 0;
+  }
+  load_tape(c, qs + off, n);
+  const int logbase = (int)(c.ctl->log_pos);
+  for (int m = 0; m < n; ++m) {
+    int x, y = 0, f;
+    if constexpr (KIND == KDQ_TU) {
+      x = m; f = m;
+    } else if constexpr (KIND == KDQ_TV) {
+      x = P.bx[j * n + m]; y = P.by[j * n + m]; f = j * n + m;
+    } else {
+      x = P.bx[m]; y = P.by[m]; f = m;
+    }
+    propose(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, m & 1);
+  }
+  if (threadIdx.x == 0) c.ctl->log_pos += n;
+  finish_tape(c, n);
+  __syncthreads();
+}
+
+// --------------------------------------------------------- stabilisation
+// Thin-factor block products: instead of forming BM = B_n ... B_m (N x N)
+// and multiplying it into BR (the reference's BM_F! + mul!), the slices are
+// applied directly to the N x ns factor (left) or the ns x N factor (right);
+// same product, half the multiply-adds.
+
+// Y (N x ns) <- B_lt Y, ping-ponging with Y2; returns the buffer holding it.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ T* apply_slice_left(Ctx<KIND, T, KT>& c, T* Y, T* Y2, int lt) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, ns = N / 2;
+  if constexpr (KIND == KDQ_TV) {
+    bgemm<MAXRM>(N, ns, N, c.eK, N, Y, N, Y2, N);
+    const double h = 0.70710678118654752440;
+    for (int j = P.z - 1; j >= 0; --j) {
+      const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * (N / 2);
+      const double* tab = P.vtab + (size_t)(lt - 1) * 32;
+      for (int e = threadIdx.x; e < (N / 2) * ns; e += blockDim.x) {
+        const int i = e % (N / 2), col = e / (N / 2);
+        const int x = P.bx[j * (N / 2) + i], y = P.by[j * (N / 2) + i];
+        const double dx = tab[sl[i] - 1], dy = tab[4 + sl[i] - 1];
+        double vx = re(Y2[x + (size_t)col * N]), vy = re(Y2[y + (size_t)col * N]);
+        double ax = -h * vx - h * vy, ay = -h * vx + h * vy;   // UV *
+        ax *= dx; ay *= dy;                                     // D *
+        vx = -h * ax - h * ay; vy = -h * ax + h * ay;           // UV *
+        Y2[x + (size_t)col * N] = from_real<T>(vx);
+        Y2[y + (size_t)col * N] = from_real<T>(vy);
+      }
+      __syncthreads();
+    }
+  } else {
+    slice_diag(c, lt, +1);
+    bgemm<MAXRM>(N, ns, N, c.eK, N, Y, N, Y2, N, c.sm.dvec, (const T*)nullptr);
+  }
+  return Y2;
+}
+
+// Z (ns x N) <- Z B_lt, ping-ponging with Z2; returns the buffer holding it.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ T* apply_slice_right(Ctx<KIND, T, KT>& c, T* Z, T* Z2, int lt) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, ns = N / 2;
+  if constexpr (KIND == KDQ_TV) {
+    const double h = 0.70710678118654752440;
+    const double* tab = P.vtab + (size_t)(lt - 1) * 32;
+    for (int j = 0; j < P.z; ++j) {        // Z V_1 V_2 ... V_z
+      const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * (N / 2);
+      for (int e = threadIdx.x; e < ns * (N / 2); e += blockDim.x) {
+        const int row = e % ns, i = e / ns;
+        const int x = P.bx[j * (N / 2) + i], y = P.by[j * (N / 2) + i];
+        const double dx = tab[sl[i] - 1], dy = tab[4 + sl[i] - 1];
+        double vx = re(Z[row + (size_t)x * ns]), vy = re(Z[row + (size_t)y * ns]);
+        double ax = -h * vx - h * vy, ay = -h * vx + h * vy;   // * UV
+        ax *= dx; ay *= dy;                                     // * D
+        vx = -h * ax - h * ay; vy = -h * ax + h * ay;           // * UV
+        Z[row + (size_t)x * ns] = from_real<T>(vx);
+        Z[row + (size_t)y * ns] = from_real<T>(vy);
+      }
+      __syncthreads();
+    }
+    bgemm<MAXRM>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
+  } else {
+    slice_diag(c, lt, +1);
+    for (int e = threadIdx.x; e < ns * N; e += blockDim.x) {
+      const int col = e / ns;
+      Z[e] = Z[e] * c.sm.dvec[col];
+    }
+    __syncthreads();
+    bgemm<MAXRM>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
+  }
+  return Z2;
+}
+
+// G = I - BR (BL BR)^-1 BL (get_G!, src/public/Gupdate.jl:139-157); records
+// the drift against the wrapped G when `drift` is set.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void get_G(Ctx<KIND, T, KT>& c, const T* BL, const T* BR, bool drift) {
+  const int N = c.P.Ns, ns = N / 2;
+  bgemm<MAXRM>(ns, ns, N, BL, ns, BR, N, c.Mss, ns);
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  lu_factor(ns, c.Mss, c.piv, &bad);
+  for (int e = threadIdx.x; e < ns * N; e += blockDim.x) c.X[e] = BL[e];
+  __syncthreads();
+  lu_solve(ns, N, c.Mss, c.piv, c.X);
+  bgemm<MAXRM>(N, N, ns, BR, N, c.X, ns, c.W1, N);
+  double d2 = 0.0, n2 = 0.0;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+    const int i = e % N, j = e / N;
+    T g = zero<T>() - c.W1[e];
+    if (i == j) g = g + one<T>();
+    if (drift) {
+      d2 += abs2(c.G[e] - g);
+      n2 += abs2(g);
+    }
+    c.G[e] = g;
+  }
+  if (drift) {
+    d2 = block_sum(d2, c.sm.red);
+    n2 = block_sum(n2, c.sm.red);
+    if (threadIdx.x == 0) {
+      const double dr = sqrt(d2 / n2);
+      if (c.ctl->drift_pos < c.P.drift_cap)
+        c.P.drift[(size_t)c.chain * c.P.drift_cap + c.ctl->drift_pos] = dr;
+      c.ctl->drift_pos += 1;
+      c.ctl->n_recompute += 1;
+      if (!(dr <= c.ctl->max_drift)) c.ctl->max_drift = isfinite(dr) ? fmax(dr, c.ctl->max_drift) : dr;
+    }
+  }
+  if (threadIdx.x == 0 && bad) atomicOr(&c.ctl->err, KDQ_FLAG_SINGULAR);
+  __syncthreads();
+}
+
+// BRs[k+1] = orth_cols(BM(k) BRs[k]) then G recompute at node k+1.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void node_forward(Ctx<KIND, T, KT>& c, int k) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, ns = N / 2;
+  const size_t fs = (size_t)N * ns;
+  T* BRk = P.BRs<T>(c.chain) + (size_t)(k - 1) * fs;
+  T* BRn = BRk + fs;
+  for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Y[e] = BRk[e];
+  __syncthreads();
+  T* cur = c.Y;
+  T* oth = c.Y2;
+  for (int lt = (int)P.nodes[k - 1] + 1; lt <= (int)P.nodes[k]; ++lt) {
+    T* res = apply_slice_left<MAXRM>(c, cur, oth, lt);
+    oth = cur;
+    cur = res;
+  }
+  householder_q(N, ns, cur, BRn, c.sm.wn, c.sm.red, &c.sm.w0);
+  const T* BLn = P.BLs<T>(c.chain) + (size_t)k * fs;
+  get_G<MAXRM>(c, BLn, BRn, true);
+  if (threadIdx.x == 0) c.ctl->idx = k + 1;
+}
+
+// BLs[k] = orth_rows(BLs[k+1] BM(k)) then (optionally) G recompute.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void node_backward(Ctx<KIND, T, KT>& c, int k, bool recompute, bool drift) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, ns = N / 2;
+  const size_t fs = (size_t)N * ns;
+  T* BLk = P.BLs<T>(c.chain) + (size_t)(k - 1) * fs;
+  const T* BLn = BLk + fs;
+  for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Y[e] = BLn[e];
+  __syncthreads();
+  T* cur = c.Y;
+  T* oth = c.Y2;
+  for (int lt = (int)P.nodes[k]; lt > (int)P.nodes[k - 1]; --lt) {
+    T* res = apply_slice_right<MAXRM>(c, cur, oth, lt);
+    oth = cur;
+    cur = res;
+  }
+  // orth_rows: QR of Z^H (N x ns), BL = Q^H
+  for (size_t e = threadIdx.x; e < fs; e += blockDim.x) {
+    const int r = e % ns, col = e / ns;
+    oth[col + (size_t)r * N] = conjg(cur[e]);
+  }
+  __syncthreads();
+  householder_q(N, ns, oth, cur, c.sm.wn, c.sm.red, &c.sm.w0);
+  for (size_t e = threadIdx.x; e < fs; e += blockDim.x) {
+    const int r = e % ns, col = e / ns;
+    BLk[e] = conjg(cur[col + (size_t)r * N]);
+  }
+  __syncthreads();
+  if (recompute) get_G<MAXRM>(c, BLk, P.BRs<T>(c.chain) + (size_t)(k - 1) * fs, drift);
+  if (threadIdx.x == 0) c.ctl->idx = k;
+}
+
+// ------------------------------------------------------------ measurement
+__device__ inline double re_prod(double k, double g) { return k * g; }
+__device__ inline double re_prod(double k, cd g) { return k * g.x; }
+__device__ inline double re_prod(cd k, cd g) { return k.x * g.x - k.y * g.y; }
+
+// Equal-time observables at tau = Nt/2 from G at slice t0 (phy_measure):
+// wrap a copy to Nt/2, symmetrise with HalfeK, accumulate one row.
+// tU: src/tU/phy_update.jl:154-254; tV: src/tV/phy_update.jl:207-314;
+// tUV: src/tUV/phy_update.jl:205-355.  The honeycomb structure factors keep
+// the reference's accumulation (only the first term of each correlator in
+// the complex branch, where the `+adjoint(...)` lines are discarded
+// statements); `xy_i` is called with its real three-argument signature.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void measure(Ctx<KIND, T, KT>& c, int t0) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, Nt = P.Nt, half = Nt / 2;
+  T* G0 = c.W2;
+  T* W = c.W1;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) G0[e] = c.G[e];
+  __syncthreads();
+  if (2 * t0 > Nt) {
+    for (int t = t0; t > half; --t) {
+      if constexpr (KIND == KDQ_TV) {
+        for (int j = 0; j < P.z; ++j) tv_rotate(c, G0, t, j, -1);
+        bgemm<MAXRM>(N, N, N, c.eKinv, N, G0, N, W, N);
+        bgemm<MAXRM>(N, N, N, W, N, c.eK, N, G0, N);
+      } else {
+        wrap_bwd_kv<MAXRM>(c, G0, W, t);
+      }
+    }
+  } else {
+    for (int t = t0 + 1; t <= half; ++t) {
+      if constexpr (KIND == KDQ_TV) {
+        bgemm<MAXRM>(N, N, N, G0, N, c.eKinv, N, W, N);
+        bgemm<MAXRM>(N, N, N, c.eK, N, W, N, G0, N);
+        for (int j = P.z - 1; j >= 0; --j) tv_rotate(c, G0, t, j, +1);
+      } else {
+        wrap_fwd_kv<MAXRM>(c, G0, W, t);
+      }
+    }
+  }
+  bgemm<MAXRM>(N, N, N, c.HalfeK, N, G0, N, W, N);
+  bgemm<MAXRM>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
+
+  double acc[KDQ_MAX_OBS];
+#pragma unroll
+  for (int q = 0; q < KDQ_MAX_OBS; ++q) acc[q] = 0.0;
+  // kinetic energy: Σ K .* G0
+  double ek = 0.0;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) ek += re_prod(c.Kmat[e], G0[e]);
+  // on-site term
+  double eu = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const T d = G0[i + (size_t)i * N];
+    if constexpr (KIND == KDQ_TUV && sizeof(T) == sizeof(double)) {
+      eu += re((one<T>() - d) * (one<T>() - d));
+    } else {
+      eu += re((one<T>() - d) * conjg(d));
+    }
+  }
+  // bond term
+  double ev = 0.0;
+  if constexpr (KIND != KDQ_TU) {
+    const int nbond = KIND == KDQ_TV ? (N / 2) * P.z : N * P.z;
+    for (int b = threadIdx.x; b < nbond; b += blockDim.x) {
+      const int x = P.bx[b], y = P.by[b];
+      const T gxx = G0[x + (size_t)x * N], gyy = G0[y + (size_t)y * N];
+      const T gxy = G0[x + (size_t)y * N], gyx = G0[y + (size_t)x * N];
+      const T ox = one<T>() - gxx, oy = one<T>() - gyy;
+      if constexpr (KIND == KDQ_TV || sizeof(T) == sizeof(double)) {
+        const double v = re(ox * oy - gxy * gyx);
+        ev += KIND == KDQ_TV ? v : 2.0 * v + 2.0 * re(oy * ox);
+      } else {
+        ev += re(ox * oy - gxy * gyx) + re(conjg(gxx * gyy - gxy * gyx)) + re(oy * conjg(gxx)) +
+              re(ox * conjg(gyy));
+      }
+    }
+  }
+  // honeycomb structure factors over (displacement, cell) pairs
+  double sf[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) sf[q] = 0.0;
+  const bool hc = P.lattice == KDQ_HONEYCOMB120 || P.lattice == KDQ_HONEYCOMB60;
+  if (hc) {
+    const int L1 = P.L1, L2 = P.L2, nc = L1 * L2;
+    for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) {
+      const int r = e / nc, cell = e % nc;
+      const int rx = r % L1 + 1, ry = r / L1 + 1;
+      const int ix = cell % L1 + 1, iy = cell / L1 + 1;
+      const int jx = (ix + rx - 1) % L1 + 1, jy = (iy + ry - 1) % L2 + 1;
+      const int a1 = 2 * (ix + (iy - 1) * L1) - 2, a2 = 2 * (jx + (jy - 1) * L1) - 2;
+      const int b1 = a1 + 1, b2 = a2 + 1;
+      const double ph = P.cosr[r];
+      auto g = [&](int i, int j) { return G0[i + (size_t)j * N]; };
+      const T o = one<T>();
+      if constexpr (KIND == KDQ_TV) {
+        double t[4];
+        if (a1 == a2) {
+          t[0] = re(o - g(a1, a1));
+          t[1] = re(o - g(b1, b1));
+        } else {
+          t[0] = re((o - g(a1, a1)) * (o - g(a2, a2)) - g(a1, a2) * g(a2, a1));
+          t[1] = re((o - g(b1, b1)) * (o - g(b2, b2)) - g(b1, b2) * g(b2, b1));
+        }
+        t[2] = re((o - g(b1, b1)) * (o - g(a2, a2)) - g(b1, a2) * g(a2, b1));
+        t[3] = re((o - g(a1, a1)) * (o - g(b2, b2)) - g(a1, b2) * g(b2, a1));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { sf[q] += t[q]; sf[4 + q] += ph * t[q]; }
+      } else {
+        const T del = a1 == a2 ? o : zero<T>();
+        double t1, t2;
+        if constexpr (KIND == KDQ_TUV && sizeof(T) == sizeof(double)) {
+          t1 = 2 * re((o - g(a1, a1)) * (o - g(a2, a2)) + (del - g(a1, a2)) * g(a2, a1)) +
+               2 * re((o - g(b1, b1)) * (o - g(b2, b2)) + (del - g(b1, b2)) * g(b2, b1)) -
+               2 * re((o - g(b1, b1)) * (o - g(a2, a2)) - g(b1, a2) * g(a2, b1)) -
+               2 * re((o - g(a1, a1)) * (o - g(b2, b2)) - g(a1, b2) * g(b2, a1));
+          t2 = 2 * re((o - g(a1, a1)) * (o - g(a2, a2))) + 2 * re((o - g(b1, b1)) * (o - g(b2, b2))) -
+               2 * re((o - g(b1, b1)) * (o - g(a2, a2))) - 2 * re((o - g(a1, a1)) * (o - g(b2, b2)));
+        } else {
+          t1 = re((o - g(a1, a1)) * (o - g(a2, a2)) + (del - g(a1, a2)) * g(a2, a1)) +
+               re((o - g(b1, b1)) * (o - g(b2, b2)) + (del - g(b1, b2)) * g(b2, b1)) -
+               re((o - g(b1, b1)) * (o - g(a2, a2)) - g(b1, a2) * g(a2, b1)) -
+               re((o - g(a1, a1)) * (o - g(b2, b2)) - g(a1, b2) * g(b2, a1));
+          t2 = re((o - g(a1, a1)) * conjg(g(a2, a2))) + re((o - g(b1, b1)) * conjg(g(b2, b2))) -
+               re((o - g(a1, a1)) * conjg(g(b2, b2))) - re((o - g(b1, b1)) * conjg(g(a2, a2)));
+        }
+        sf[0] += t1 + t2;
+        sf[1] += ph * (t1 + t2);
+        sf[2] += t1 - t2;
+        sf[3] += ph * (t1 - t2);
+      }
+    }
+  }
+  ek = block_sum(ek, c.sm.red);
+  eu = block_sum(eu, c.sm.red);
+  ev = block_sum(ev, c.sm.red);
+  const int nsf = KIND == KDQ_TV ? 8 : 4;
+  for (int q = 0; q < nsf; ++q) sf[q] = block_sum(sf[q], c.sm.red);
+  const double n2 = (double)N * N;
+  if constexpr (KIND == KDQ_TU) {
+    acc[0] = -2.0 * P.Ht * ek;
+    acc[1] = eu;
+    for (int q = 0; q < 4; ++q) acc[2 + q] = sf[q] / n2;
+  } else if constexpr (KIND == KDQ_TV) {
+    acc[0] = P.Ht * ek;
+    acc[1] = ev;
+    for (int q = 0; q < 8; ++q) acc[2 + q] = sf[q] * 4.0 / n2;
+  } else {
+    acc[0] = 2.0 * P.Ht * ek;
+    acc[1] = P.U * eu;
+    acc[2] = P.V * ev;
+    for (int q = 0; q < 4; ++q) acc[3 + q] = sf[q] / n2;
+  }
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < P.n_obs; ++q) c.ctl->obs_acc[q] += acc[q];
+    c.ctl->obs_cnt += 1;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ kernel
+// mode KDQ_MODE_INIT: block k of the initial left chain (and G at k == 1);
+// KDQ_MODE_FWD: forward slices node(k)+1 .. node(k+1), then the node;
+// KDQ_MODE_BWD: backward slices node(k+1) .. node(k)+1, then the node.
+template <int KIND, class T, class KT, int MAXRM>
+__global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int mode, int k) {
+  extern __shared__ double dyn_d[];
+  __shared__ Smem<T> sm;
+  const int chain = blockIdx.x;
+  const int N = P.Ns;
+  const size_t cNN = (size_t)chain * P.sz_NN;
+  const size_t cNn = (size_t)chain * P.sz_Nn;
+  Ctx<KIND, T, KT> c{P,
+                     sm,
+                     reinterpret_cast<uint8_t*>(dyn_d + P.n_field),
+                     dyn_d,
+                     chain,
+                     P.ctl + chain,
+                     static_cast<T*>(P.G) + cNN,
+                     static_cast<T*>(P.W1) + cNN,
+                     static_cast<T*>(P.W2) + cNN,
+                     static_cast<T*>(P.Y) + cNn,
+                     static_cast<T*>(P.Y2) + cNn,
+                     static_cast<T*>(P.Mss) + (size_t)chain * P.sz_nn,
+                     static_cast<T*>(P.X) + cNn,
+                     P.piv + (size_t)chain * (N / 2),
+                     P.s + (size_t)chain * P.Nt * P.n_field,
+                     static_cast<const KT*>(P.eK),
+                     static_cast<const KT*>(P.eKinv),
+                     static_cast<const KT*>(P.HalfeK),
+                     static_cast<const KT*>(P.HalfeKinv),
+                     static_cast<const KT*>(P.K),
+                     static_cast<const T*>(P.Pt)};
+  if (mode == KDQ_MODE_INIT) {
+    node_backward<MAXRM>(c, k, k == 1, false);
+    return;
+  }
+  const int Θidx = P.NN / 2 + 1;
+  const int lo = (int)P.nodes[k - 1], hi = (int)P.nodes[k];
+  if (mode == KDQ_MODE_FWD) {
+    // idx == k while these slices run (src/tU/phy_update.jl:53-98)
+    const bool rec = P.record && (KIND == KDQ_TU ? (Θidx - k >= 0 && Θidx - k <= 1) : abs(k - Θidx) <= 1);
+    for (int lt = lo + 1; lt <= hi; ++lt) {
+      if constexpr (KIND == KDQ_TV) {
+        bgemm<MAXRM>(N, N, N, c.G, N, c.eKinv, N, c.W1, N);
+        bgemm<MAXRM>(N, N, N, c.eK, N, c.W1, N, c.G, N);
+        for (int j = P.z - 1; j >= 0; --j) {
+          tv_rotate(c, c.G, lt, j, +1);
+          update_layer(c, lt, j, true);
+        }
+      } else {
+        wrap_fwd_kv<MAXRM>(c, c.G, c.W1, lt);
+        update_layer(c, lt, 0, true);
+      }
+      if (rec) measure<MAXRM>(c, lt);
+    }
+    node_forward<MAXRM>(c, k);
+  } else {
+    // idx == k+1 while these slices run (src/tU/phy_update.jl:101-139)
+    const int idx = k + 1;
+    const bool rec = P.record && (KIND == KDQ_TU ? (idx - Θidx >= 0 && idx - Θidx <= 1) : abs(idx - Θidx) <= 1);
+    for (int lt = hi; lt > lo; --lt) {
+      if constexpr (KIND == KDQ_TV) {
+        for (int j = 0; j < P.z; ++j) {
+          update_layer(c, lt, j, false);
+          tv_rotate(c, c.G, lt, j, -1);
+        }
+        bgemm<MAXRM>(N, N, N, c.eKinv, N, c.G, N, c.W1, N);
+        bgemm<MAXRM>(N, N, N, c.W1, N, c.eK, N, c.G, N);
+        if (rec) measure<MAXRM>(c, lt - 1);
+      } else {
+        update_layer(c, lt, 0, false);
+        if (rec) measure<MAXRM>(c, lt);
+        wrap_bwd_kv<MAXRM>(c, c.G, c.W1, lt);
+      }
+    }
+    node_backward<MAXRM>(c, k, true, true);
+    if (k == 1 && threadIdx.x == 0) {
+      ChainCtl* ctl = c.ctl;
+      if (P.record) {
+        if (ctl->obs_slot < P.obs_cap) {
+          double* row = P.obs + ((size_t)chain * P.obs_cap + ctl->obs_slot) * P.n_obs;
+          for (int q = 0; q < P.n_obs; ++q) row[q] = ctl->obs_acc[q] / ctl->obs_cnt;
+        }
+        ctl->obs_slot += 1;
+        for (int q = 0; q < KDQ_MAX_OBS; ++q) ctl->obs_acc[q] = 0.0;
+        ctl->obs_cnt = 0;
+      }
+      ctl->sweep += 1;
+    }
+  }
+}
+
+}  // namespace kdq

@@ -1,0 +1,276 @@
+"""Host-side mirror of the reference's sweep entry points over the CUDA library.
+
+``phy_update(path, model, s, Sweeps, record)`` keeps the reference's
+signature and semantics (returns the updated field, appends one CSV row per
+sweep when recording); :class:`Sweeper` exposes the batched, resident form
+(many chains per handle, device-resident state between calls).
+
+References (KAPDQMC): src/tU/phy_update.jl:3-152, src/tV/phy_update.jl:1-188,
+src/tUV/phy_update.jl:1-186, src/KAPDQMC.jl:12-28.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import _lib
+from .model import KIND_TU, KIND_TV
+
+_LATTICE_ID = {"SQUARE45": 0, "SQUARE90": 1, "HoneyComb120": 2, "HoneyComb60": 3}
+_CSV_LOCKS: dict = {}
+_CSV_GUARD = threading.Lock()
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _mat(m, as_complex):
+    """Column-major matrix as a flat float64 buffer (interleaved if complex)."""
+    m = np.asarray(m)
+    flat = np.ravel(m, order="F")
+    if as_complex:
+        return np.ascontiguousarray(flat.astype(np.complex128)).view(np.float64)
+    return np.ascontiguousarray(flat.real.astype(np.float64))
+
+
+def model_desc(model):
+    """kdq_model_desc for a model struct; returns (desc, keepalive)."""
+    kind = model.kind
+    gc = bool(model.is_complex)
+    kmats = [model.eK, model.eKinv, model.HalfeK, model.HalfeKinv, model.K]
+    kc = any(np.iscomplexobj(x) and np.any(np.imag(x) != 0) for x in kmats)
+    keep = []
+
+    def ptr(a):
+        keep.append(a)
+        return a.ctypes.data
+
+    d = _lib.ModelDesc()
+    d.kind = kind
+    d.lattice = _LATTICE_ID[model.Lattice]
+    d.site[0], d.site[1] = int(model.site[0]), int(model.site[1]) if len(model.site) > 1 else 1
+    d.Ns, d.Nt = model.Ns, model.Nt
+    d.z = 1 if kind == KIND_TU else int(model.nnidx.shape[1])
+    d.g_complex, d.k_complex = int(gc), int(kc)
+    nodes = _c(model.nodes, np.int64)
+    d.n_nodes = len(nodes)
+    d.nodes = ptr(nodes)
+    d.alpha = ptr(_c(model.α, np.float64)) if kind != 2 else None
+    d.gamma = ptr(_c(model.γ, np.float64))
+    d.eta = ptr(_c(model.η, np.float64))
+    d.a = float(getattr(model, "a", 0.0))
+    d.Ht = float(model.Ht)
+    d.U = float(getattr(model, "U", 0.0))
+    d.V = float(getattr(model, "V", 0.0))
+    d.eK, d.eKinv, d.HalfeK, d.HalfeKinv, d.K = (ptr(_mat(x, kc)) for x in kmats)
+    d.Pt = ptr(_mat(model.Pt, gc))
+    if kind != KIND_TU:
+        b = np.asarray(model.nnidx).transpose(1, 0, 2).reshape(-1, 2)   # column-major bond order
+        d.bonds = ptr(_c(b, np.int32))
+    return d, keep
+
+
+class Sweeper:
+    """A batch of independent Markov chains of one model on one GPU."""
+
+    def __init__(self, model, nchains: int = 1, device: int = 0):
+        self.lib = _lib.load()
+        self.model = model
+        self.nchains = int(nchains)
+        d, keep = model_desc(model)
+        h = C.c_void_p()
+        _lib.check(self.lib.kdq_create(C.byref(h), C.byref(d), self.nchains, device), None)
+        del keep
+        self.h = h
+        self.n_obs = self.lib.kdq_n_obs(h)
+        self.field_size = model.Nt * model.n_field
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.kdq_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _ck(self, rc):
+        _lib.check(rc, self.h)
+
+    # -- state -------------------------------------------------------------
+    def set_fields(self, s):
+        """s: one field (model.field_shape) or a stack (nchains, *field_shape)."""
+        s = np.asarray(s, dtype=np.uint8)
+        if s.shape == tuple(self.model.field_shape):
+            s = s[None]
+        if s.shape[0] != self.nchains:
+            raise ValueError(f"need {self.nchains} fields, got {s.shape[0]}")
+        flat = np.concatenate([np.ravel(x, order="F") for x in s])
+        flat = np.ascontiguousarray(flat)
+        self._ck(self.lib.kdq_set_fields(self.h, flat.ctypes.data, flat.size))
+
+    def get_fields(self):
+        out = np.empty(self.nchains * self.field_size, dtype=np.uint8)
+        self._ck(self.lib.kdq_get_fields(self.h, out.ctypes.data, out.size))
+        shp = tuple(self.model.field_shape)
+        return np.stack([out[c * self.field_size:(c + 1) * self.field_size].reshape(shp, order="F")
+                         for c in range(self.nchains)])
+
+    def set_rng(self, seed: int, sweep_offset: int = 0):
+        self._ck(self.lib.kdq_set_rng(self.h, int(seed) & (2 ** 64 - 1), int(sweep_offset)))
+
+    def set_tape(self, k, u):
+        """Explicit proposal tape, arrays of shape (nchains, n)."""
+        k = np.ascontiguousarray(np.asarray(k, dtype=np.uint8).reshape(self.nchains, -1))
+        u = np.ascontiguousarray(np.asarray(u, dtype=np.float64).reshape(self.nchains, -1))
+        self._keep_tape = (k, u)
+        self._ck(self.lib.kdq_set_tape(self.h, k.ctypes.data, u.ctypes.data, k.shape[1]))
+
+    # -- sweeps ------------------------------------------------------------
+    def phy_update(self, sweeps: int, record: bool = False):
+        """Init from the fields + sweeps; returns obs (nchains, sweeps, n_obs) or None."""
+        if record:
+            obs = np.empty(self.nchains * sweeps * self.n_obs)
+            self._ck(self.lib.kdq_phy_update(self.h, sweeps, 1, obs.ctypes.data, obs.size))
+            return obs.reshape(self.nchains, sweeps, self.n_obs)
+        self._ck(self.lib.kdq_phy_update(self.h, sweeps, 0, None, 0))
+        return None
+
+    def init(self):
+        self._ck(self.lib.kdq_init(self.h))
+
+    def sweep(self, sweeps: int, record: bool = False):
+        self._ck(self.lib.kdq_sweep(self.h, sweeps, int(bool(record))))
+
+    def synchronize(self):
+        self._ck(self.lib.kdq_synchronize(self.h))
+
+    def get_obs(self, rows: int):
+        obs = np.empty(self.nchains * rows * self.n_obs)
+        self._ck(self.lib.kdq_get_obs(self.h, obs.ctypes.data, obs.size))
+        return obs.reshape(self.nchains, rows, self.n_obs)
+
+    @property
+    def stream(self) -> int:
+        return self.lib.kdq_stream(self.h) or 0
+
+    # -- inspection --------------------------------------------------------
+    def green(self, chain: int = 0):
+        N = self.model.Ns
+        gc = self.model.is_complex
+        buf = np.empty(N * N * (2 if gc else 1))
+        self._ck(self.lib.kdq_get_green(self.h, chain, buf.ctypes.data, buf.size))
+        if gc:
+            buf = buf.view(np.complex128)
+        return buf.reshape(N, N, order="F")
+
+    def stats(self):
+        st = _lib.Stats()
+        self._ck(self.lib.kdq_get_stats(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def enable_accept_log(self, n_per_chain: int):
+        self._acc_cap = int(n_per_chain)
+        self._ck(self.lib.kdq_enable_accept_log(self.h, self._acc_cap))
+
+    def accept_log(self):
+        out = np.empty(self.nchains * self._acc_cap, dtype=np.uint8)
+        self._ck(self.lib.kdq_get_accept_log(self.h, out.ctypes.data, out.size))
+        return out.reshape(self.nchains, self._acc_cap)
+
+    def drift(self, sweeps: int):
+        n = sweeps * 2 * (len(self.model.nodes) - 1)
+        out = np.empty(self.nchains * n)
+        self._ck(self.lib.kdq_get_drift(self.h, out.ctypes.data, out.size))
+        return out.reshape(self.nchains, n)
+
+
+# ------------------------------------------------------------------------
+# reference-shaped entry points
+# ------------------------------------------------------------------------
+def _csv_name(path, model):
+    """File name scheme of the reference's CSV output.
+
+    src/tU/phy_update.jl:12-27, src/tV/phy_update.jl:10-23,
+    src/tUV/phy_update.jl:13-22 (the tV/tUV square case is named "□").
+    """
+    def f(x):  # Julia prints whole floats as 1.0
+        return repr(float(x))
+
+    site = "[" + ", ".join(str(int(v)) for v in model.site) + "]"
+    if model.kind == KIND_TU:
+        name = {"SQUARE90": "□90", "SQUARE45": "□45", "HoneyComb60": "HC", "HoneyComb120": "HC120"}[model.Lattice]
+        if model.Θquench == 0.0:
+            return os.path.join(path, f"tUphy{name}_t{f(model.Ht)}U{f(model.Hu1)}size{site}Δt{f(model.Δt)}"
+                                      f"Θ{f(model.Θrelax)}BS{model.BatchSize}.csv")
+        return os.path.join(path, f"tUphy{name}_t{f(model.Ht)}U{f(model.Hu1)}_{f(model.Hu2)}size{site}"
+                                  f"Δt{f(model.Δt)}Θ{f(model.Θrelax)}_{f(model.Θquench)}BS{model.BatchSize}.csv")
+    name = {"SQUARE45": "□", "SQUARE90": "□", "HoneyComb60": "HC", "HoneyComb120": "HC120"}[model.Lattice]
+    if model.kind == KIND_TV:
+        if len(np.unique(model.α)) == 1:
+            return os.path.join(path, f"tVphy{name}_t{f(model.Ht)}V{f(model.Hv1)}size{site}Δt{f(model.Δt)}"
+                                      f"Θ{f(model.Θrelax)}BS{model.BatchSize}.csv")
+        return os.path.join(path, f"tVphy{name}_t{f(model.Ht)}V{f(model.Hv1)}_{f(model.Hv2)}size{site}"
+                                  f"Δt{f(model.Δt)}Θ{f(model.Θrelax)}_{f(model.Θquench)}BS{model.BatchSize}.csv")
+    return os.path.join(path, f"tUVphy{name}_t{f(model.Ht)}U{f(model.U)}V{f(model.V)}size{site}"
+                              f"Δt{f(model.Δt)}Θ{f(model.Θ)}BS{model.BatchSize}.csv")
+
+
+def _append_csv(file, rows):
+    """Append rows under a per-file lock (the reference's lock is per call,
+    src/tU/phy_update.jl:4, so it never serialises concurrent callers)."""
+    with _CSV_GUARD:
+        lk = _CSV_LOCKS.setdefault(os.path.abspath(file), threading.Lock())
+    with lk, open(file, "a") as io:
+        for r in rows:
+            io.write(",".join(repr(float(v)) for v in r) + "\n")
+
+
+def phy_update(path, model, s, Sweeps: int, record: bool = False, *, seed=None, tape=None,
+               device: int = 0, sweeper: Sweeper | None = None):
+    """Sweep the HS field(s) ``s`` and return the updated field(s).
+
+    ``s`` is one field in the reference's layout or a stack of fields (one
+    per chain).  ``seed`` selects the Philox stream (default: time-based,
+    like the reference's unseeded generator); ``tape=(k, u)`` gives an
+    explicit proposal tape instead.  When ``record`` is true one CSV row per
+    sweep (averaged over chains) is appended to the reference's file name
+    under ``path`` and the per-chain rows are also returned as ``s, obs``.
+    """
+    s = np.asarray(s, dtype=np.uint8)
+    single = s.shape == tuple(model.field_shape)
+    stack = s[None] if single else s
+    own = sweeper is None
+    sw = sweeper or Sweeper(model, nchains=stack.shape[0], device=device)
+    try:
+        sw.set_fields(stack)
+        if tape is not None:
+            sw.set_tape(*tape)
+        else:
+            if seed is None:
+                seed = int.from_bytes(os.urandom(8), "little")
+            sw.set_rng(seed)
+        obs = sw.phy_update(Sweeps, record)
+        out = sw.get_fields()
+    finally:
+        if own:
+            sw.close()
+    out = out[0] if single else out
+    if record:
+        if path:
+            _append_csv(_csv_name(path, model), obs.mean(axis=0))
+        return out, obs
+    return out

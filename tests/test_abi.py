@@ -1,0 +1,38 @@
+"""The C-ABI library loads and exports every entry point include/kapdqmc.h declares."""
+import ctypes
+import re
+from pathlib import Path
+
+from kapdqmc_gb300 import _lib
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "kapdqmc.h"
+
+
+def declared():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*[\w\s\*]+?\b(kdq_\w+)\s*\(", text, re.M)))
+
+
+def test_header_symbols_exported():
+    lib = _lib.load()
+    names = declared()
+    assert "kdq_phy_update" in names and "kdq_create" in names
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(_lib._SIGS), set(names) ^ set(_lib._SIGS)
+
+
+def test_struct_layout_matches_header():
+    # kdq_model_desc: 10 int32 (40 bytes) -> 8-aligned pointer block
+    assert ctypes.sizeof(_lib.ModelDesc) == 40 + 4 * 8 + 4 * 8 + 7 * 8
+    assert ctypes.sizeof(_lib.Stats) == 40
+
+
+def test_create_rejects_bad_model_without_gpu_work():
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    d = _lib.ModelDesc()
+    d.kind = 7
+    rc = lib.kdq_create(ctypes.byref(h), ctypes.byref(d), 1, 0)
+    assert rc == _lib.KDQ_ERR_ARG
+    assert b"kind" in lib.kdq_last_error(None)

@@ -1,0 +1,141 @@
+"""Parity of the CUDA sweep (through the C ABI) with the CPU oracle.
+
+Same model, same fields, same Philox proposal stream: the accept/reject
+sequence and the final fields must be identical, G must agree to 1e-10
+(relative Frobenius) and the measurement rows to 1e-9 (relative).
+"""
+import numpy as np
+import pytest
+
+import cases
+import dqmc_oracle as O
+import philox
+from kapdqmc_gb300 import Initial_s
+from kapdqmc_gb300.sweep import Sweeper
+
+pytestmark = pytest.mark.gpu
+
+G_TOL = 1e-10       # relative Frobenius distance of G
+OBS_TOL = 1e-9      # relative distance of each measurement row
+
+
+def _oracle(model, s, seed, chain, sweeps, record):
+    n = O.proposals_per_sweep(model)
+    ks, us = zip(*(philox.tape(seed, chain, w, n) for w in range(sweeps)))
+    return O.phy_update(model, s, sweeps, O.Tape(np.concatenate(ks), np.concatenate(us)), record)
+
+
+def _compare(model, nchains=2, sweeps=2, record=True, seed=1234):
+    fields = np.stack([Initial_s(model, 100 + c) for c in range(nchains)])
+    n = O.proposals_per_sweep(model) * sweeps
+    with Sweeper(model, nchains) as sw:
+        sw.set_fields(fields)
+        sw.set_rng(seed)
+        sw.enable_accept_log(n)
+        obs = sw.phy_update(sweeps, record)
+        s_gpu = sw.get_fields()
+        acc = sw.accept_log()
+        G = [sw.green(c) for c in range(nchains)]
+        st = sw.stats()
+        drift = sw.drift(sweeps)
+    for c in range(nchains):
+        ref = _oracle(model, fields[c], seed, c, sweeps, record)
+        np.testing.assert_array_equal(acc[c].astype(bool), np.array(ref.accepts), err_msg=f"chain {c} accepts")
+        np.testing.assert_array_equal(s_gpu[c], ref.s, err_msg=f"chain {c} fields")
+        rel = np.linalg.norm(G[c] - ref.G) / np.linalg.norm(ref.G)
+        assert rel < G_TOL, f"chain {c}: G rel diff {rel:.3e}"
+        if record:
+            ro = np.array(ref.obs_rows)
+            err = np.abs(obs[c] - ro).max() / max(1.0, np.abs(ro).max())
+            assert err < OBS_TOL, f"chain {c}: obs diff {err:.3e}\n{obs[c]}\n{ro}"
+        np.testing.assert_allclose(drift[c], ref.drift, rtol=0, atol=1e-9)
+    assert st["proposals"] == nchains * n
+    assert st["max_drift"] < 1e-6
+    return st
+
+
+def test_tu_square():
+    _compare(cases.tu_square())
+
+
+def test_tu_honeycomb_structure_factors():
+    _compare(cases.tu_honeycomb())
+
+
+def test_tu_quench_ragged_nodes():
+    # quench profile (slice-dependent α) and the reference's own test model
+    _compare(cases.tu_quench(), sweeps=1)
+
+
+def test_tu_flux_complex_kinetic():
+    _compare(cases.tu_square(flux=np.pi), record=False)
+
+
+def test_tv_honeycomb():
+    _compare(cases.tv_honeycomb())
+
+
+def test_tuv_honeycomb_complex():
+    _compare(cases.tuv_honeycomb())
+
+
+def test_tuv_honeycomb_real():
+    _compare(cases.tuv_honeycomb(U=-4.0, V=0.3))
+
+
+def test_tuv_square_marginal():
+    _compare(cases.tuv_square())
+
+
+def test_c1_config_one_sweep():
+    # t-U 4x4, 100 slices, n_wrap 10: the single-chain configuration
+    _compare(cases.c1(), nchains=1, sweeps=1)
+
+
+def test_explicit_tape_matches_philox():
+    model = cases.tu_square()
+    s0 = Initial_s(model, 5)
+    n = O.proposals_per_sweep(model)
+    k, u = philox.tape(99, 0, 0, n)
+    with Sweeper(model, 1) as sw:
+        sw.set_fields(s0)
+        sw.set_rng(99)
+        sw.phy_update(1)
+        a = sw.get_fields()
+        sw.set_fields(s0)
+        sw.set_tape(k[None], u[None])
+        sw.phy_update(1)
+        b = sw.get_fields()
+    np.testing.assert_array_equal(a, b)
+
+
+def test_tape_too_short_is_an_error():
+    from kapdqmc_gb300._lib import KdqError
+    model = cases.tu_square()
+    n = O.proposals_per_sweep(model)
+    with Sweeper(model, 1) as sw:
+        sw.set_fields(Initial_s(model, 5))
+        sw.set_tape(np.zeros((1, n - 1)), np.full((1, n - 1), 0.5))
+        with pytest.raises(KdqError):
+            sw.phy_update(1)
+
+
+def test_split_api_continues_state():
+    """init + sweep(1) + sweep(1) equals phy_update(2) on the same stream."""
+    model = cases.tv_honeycomb()
+    s0 = np.stack([Initial_s(model, 7), Initial_s(model, 8)])
+    with Sweeper(model, 2) as sw:
+        sw.set_fields(s0)
+        sw.set_rng(5)
+        o2 = sw.phy_update(2, True)
+        g2 = sw.get_fields()
+        sw.set_fields(s0)
+        sw.set_rng(5)
+        sw.init()
+        sw.sweep(1, True)
+        sw.sweep(1, True)
+        sw.synchronize()
+        o11 = sw.get_obs(2)
+        g11 = sw.get_fields()
+    np.testing.assert_array_equal(g2, g11)
+    np.testing.assert_allclose(o2, o11, rtol=1e-12, atol=0)
