@@ -1,0 +1,358 @@
+"""Benchmark of the projector-DQMC sweep on GB300.
+
+Workload: 256 independent Markov chains of the spinless t-V model on the
+6x6 honeycomb lattice (N = 72 sites, V/t = 1, dt = 0.05, 2Θ = 20 -> 400
+slices, n_wrap = 10), FP64 throughout, energy and density structure factor
+measured every sweep.  One step = one forward+backward sweep of every chain.
+
+Metric: effective samples/s = (chain-sweeps/s) / τ_int(E_kin), summed over
+all GPUs.  τ_int is estimated (Sokal window) from the measured energy series
+of the timed sweeps, pooled over the chains.
+
+  value   device-resident: fields and B chains live in HBM, one kdq_sweep
+          per step, timed with CUDA events on the library's stream
+  e2e     through the reference-shaped C-ABI call kdq_phy_update with host
+          buffers: fields uploaded, chain rebuilt, one sweep, fields and
+          measurement rows read back, every step
+
+`--impl reference` times the CPU restatement of the reference algorithm (the
+oracle) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "eff. samples/s (sweeps/s÷τ_int) vs plain FP64 DQMC, 1 GB300, obs within 1σ"
+UNIT = "chain-sweeps/s / tau_int"
+NCHAINS = 256
+TAU_FILE = ROOT / "profiles" / "tau_int_tv_honeycomb_6x6.json"
+
+
+def reference_tau_int():
+    """τ_int of the plain local-update sweep on this workload, from a long
+    committed GPU run (both arms run the same Markov chain algorithm)."""
+    try:
+        return float(json.loads(TAU_FILE.read_text())["tau_int"])
+    except Exception:
+        return None
+
+
+def make_model():
+    from kapdqmc_gb300 import tV_Hubbard_Para
+    return tV_Hubbard_Para(Ht=1.0, Hv1=1.0, Hv2=1.0, Δt=0.05, Θrelax=10.0, Θquench=0.0,
+                           Lattice="HoneyComb120", site=[6, 6], BatchSize=10, Initial="H0")
+
+
+CONFIG = {"workload": "t-V 6x6 honeycomb (N=72), 400 slices, n_wrap=10, V/t=1, dt=0.05, "
+                      "256 independent chains, FP64, energy + density structure factor per sweep",
+          "model": "tV_Hubbard_Para(HoneyComb120, site=[6,6])", "chains_per_gpu": NCHAINS,
+          "Ns": 72, "Nt": 400, "n_wrap": 10,
+          "l2": "no flush: per-GPU chain state (B chains, fields, G) is ~0.5 GB > 129 MB L2"}
+
+
+def tau_int(series: np.ndarray, c: float = 5.0):
+    """Integrated autocorrelation time of (chains, T) series, Sokal window."""
+    x = np.asarray(series, dtype=np.float64)
+    x = x - x.mean()
+    T = x.shape[1]
+    var = np.mean(x * x)
+    if var <= 0 or T < 3:
+        return 0.5
+    tau = 0.5
+    for t in range(1, T - 1):
+        rho = np.mean(x[:, :-t] * x[:, t:]) / var
+        tau += rho
+        if t >= c * tau:
+            break
+    return max(tau, 0.5)
+
+
+def clocks_start(path):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        f = open(path, "w")
+        return subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                 "-lms", "200"], stdout=f, stderr=subprocess.DEVNULL), f
+    except OSError:
+        return None, None
+
+
+def clocks_stop(proc, f, path, device):
+    if proc is None:
+        return None
+    proc.terminate()
+    proc.wait()
+    f.close()
+    sm, mx, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in open(path):
+        p = [v.strip() for v in line.split(",")]
+        if len(p) < 9 or p[0] != str(device):
+            continue
+        try:
+            sm.append(float(p[1]))
+            mx = max(mx, float(p[2]))
+        except ValueError:
+            continue
+        for n, v in zip(names, p[5:9]):
+            if v.lower() == "active":
+                reasons.add(n)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch, dev):
+    """Measured FP64 ceiling: cuBLAS DGEMM 4096^3, best of 5 (CUDA events)."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def hbm_peak_gbs():
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except Exception:
+        return 6800.0
+
+
+# ---------------------------------------------------------------- CPU arm
+def _cpu_worker(args):
+    seed, chain, sweeps = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import dqmc_oracle as O
+    import philox
+    from kapdqmc_gb300 import Initial_s
+    model = make_model()
+    s = Initial_s(model, 1000 + chain)
+    n = O.proposals_per_sweep(model)
+    ks, us = zip(*(philox.tape(seed, chain, w, n) for w in range(sweeps)))
+    t0 = time.perf_counter()
+    O.phy_update(model, s, sweeps, O.Tape(np.concatenate(ks), np.concatenate(us)), record=True)
+    return time.perf_counter() - t0
+
+
+def _cpu_init():
+    for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[v] = "1"
+
+
+def cpu_chain_sweeps_per_s(cores: int, sweeps_per_chain: int = 1):
+    """Oracle (CPU restatement) throughput: one chain per core, all cores busy."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_cpu_init) as pool:
+        t0 = time.perf_counter()
+        pool.map(_cpu_worker, [(7, c, sweeps_per_chain) for c in range(cores)])
+        wall = time.perf_counter() - t0
+    return cores * sweeps_per_chain / wall, wall
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    vals = []
+    for _ in range(max(args.warmup, 0)):
+        pass
+    walls = []
+    for _ in range(max(args.steps, 1)):
+        v, wall = cpu_chain_sweeps_per_s(cores)
+        vals.append(v)
+        walls.append(wall)
+    cs = float(np.median(vals))
+    tau = args.tau_int or reference_tau_int() or 1.0
+    value = cs / tau
+    sample = (f"{cores} chains (one per core) x 1 sweep each per step, numpy/scipy restatement, "
+              f"BLAS threads 1; tau_int={tau:.3g} taken from the GPU arm's estimate")
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": float(np.median(walls)) * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded HS fields and Philox proposal stream)", "config": CONFIG,
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                            "chain_sweeps_per_s": cs},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    from kapdqmc_gb300 import Initial_s
+    from kapdqmc_gb300.flops import sweep_flops
+    from kapdqmc_gb300.sweep import Sweeper
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    global NCHAINS
+    NCHAINS = args.chains
+    model = make_model()
+    sw = Sweeper(model, NCHAINS, device=local)
+    fields = np.stack([Initial_s(model, 1000 + NCHAINS * rank + c) for c in range(NCHAINS)])
+    seed = 20261203 + rank
+    stream = torch.cuda.ExternalStream(sw.stream, device=dev)
+
+    # ---- device-resident throughput
+    sw.set_fields(fields)
+    sw.set_rng(seed)
+    sw.init()
+    sw.sweep(args.warmup, record=True)
+    sw.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk_path = str(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv") if (ROOT / "gpurun_out").is_dir() \
+        else f"/tmp/kdq_clocks_{os.getpid()}.csv"
+    cproc, cfile = clocks_start(clk_path)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sw.sweep(args.steps, record=True)
+    e1.record(stream)
+    e1.synchronize()
+    clocks = clocks_stop(cproc, cfile, clk_path, local)
+    sw.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = sw.stats()
+    obs = sw.get_obs(args.warmup + args.steps)
+    ek = obs[:, args.warmup:, 0]
+    tau_live = tau_int(ek)
+    tau = args.tau_int or reference_tau_int() or tau_live
+    t_max = ms
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    chain_sweeps = NCHAINS * args.steps * world
+    cs_per_s = chain_sweeps / (t_max * 1e-3)
+    value = cs_per_s / tau
+
+    # ---- roofline of the sweep kernel (the only kernel of the timed region)
+    acc_per_chain_sweep = st["accepted"] / (NCHAINS * args.steps)
+    fl = sweep_flops(model, acc_per_chain_sweep, record=True)
+    launches_per_sweep = 2 * (len(model.nodes) - 1) + 1     # block launches + one control reset per call
+    block_launches = args.steps * 2 * (len(model.nodes) - 1)
+    flops_per_launch = fl["total"] * NCHAINS / (2 * (len(model.nodes) - 1))
+    avg_launch_s = ms * 1e-3 / block_launches
+    achieved = flops_per_launch / avg_launch_s / 1e12
+    peak = fp64_peak_tflops(torch, dev)
+    roof = {"bound": "fp64", "pipe": "FP64 DFMA (CUDA cores)", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
+            "traffic": None, "flops_per_launch": flops_per_launch,
+            "flops_per_chain_sweep": fl}
+
+    # ---- end to end through kdq_phy_update with host buffers
+    e2e_steps = max(2, min(args.steps, 5))
+    cur = sw.get_fields()
+    h2d = cur.nbytes
+    d2h = cur.nbytes + NCHAINS * model_nobs(sw) * 8
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e2e_rows = []
+    for _ in range(e2e_steps):
+        sw.set_fields(cur)
+        o = sw.phy_update(1, record=True)
+        cur = sw.get_fields()
+        e2e_rows.append(o[:, 0, 0])
+    wall = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([wall], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall = float(t.item())
+    e2e_value = NCHAINS * world * e2e_steps / wall / tau
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+               "data": "synthetic (seeded HS fields and Philox proposal stream)",
+               "config": dict(CONFIG, parallelism=f"replicas x{world}"),
+               "chain_sweeps_per_s": cs_per_s, "tau_int": tau, "tau_int_live": tau_live,
+               "tau_int_source": "committed long run" if tau != tau_live else "this run",
+               "acceptance": st["accepted"] / max(st["proposals"], 1),
+               "max_drift": st["max_drift"],
+               "energy_mean": float(ek.mean()), "energy_err": float(ek.mean(axis=1).std() / math.sqrt(NCHAINS)),
+               "gpu_launches": args.steps * launches_per_sweep,
+               "roofline": roof, "clocks": clocks,
+               "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                       "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                       "ms_per_step": wall / e2e_steps * 1e3}}
+        print(json.dumps(out), file=sys.stderr, flush=True)
+        if not args.no_cpu and world == 1:
+            cores = os.cpu_count() or 1
+            cs_cpu, wall_cpu = cpu_chain_sweeps_per_s(cores)
+            out["cpu_baseline"] = {"value": cs_cpu / tau, "unit": UNIT, "cores": cores, "kind": "port",
+                                   "chain_sweeps_per_s": cs_cpu,
+                                   "sample": f"{cores} chains x 1 sweep (one chain per core) of the same "
+                                             f"workload, numpy/scipy restatement, {wall_cpu:.1f} s; "
+                                             f"tau_int from this run"}
+        print(json.dumps(out))
+    sw.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def model_nobs(sw):
+    return sw.n_obs
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--tau-int", type=float, default=None,
+                    help="τ_int used to convert chain-sweeps/s (default: the committed long-run value)")
+    ap.add_argument("--chains", type=int, default=NCHAINS,
+                    help="chains per GPU (profiling of small cases only; bench lines use 256)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,89 @@
+"""Algorithmic operation counts of one sweep (roofline numerators).
+
+Counts are real floating-point operations (a complex multiply-add is 8, a
+real one 2; a complex x real multiply-add is 4) of the algorithm as the
+sweep kernels perform it: the slice wraps, the local-update ratios and
+rank-k updates, the thin-factor block products, the Householder
+orthonormalisation, the G recompute and, when recording, the measurement
+wraps.  The reference's dense bond-rotation GEMMs in t-V are not counted
+(the rotations are O(N^2) 2x2 block operations).
+"""
+from __future__ import annotations
+
+from .model import KIND_TU, KIND_TV
+
+
+def _mac(model, left_complex: bool, right_complex: bool) -> int:
+    if left_complex and right_complex:
+        return 8
+    if left_complex or right_complex:
+        return 4
+    return 2
+
+
+def sweep_flops(model, accepted: float, record: bool, k_complex: bool = False) -> dict:
+    """FLOPs of one forward+backward sweep of one chain.
+
+    ``accepted``: accepted proposals per chain-sweep (measured).
+    """
+    N, Nt, ns = model.Ns, model.Nt, model.Ns // 2
+    gc = bool(model.is_complex)
+    kc = bool(k_complex)
+    mgk = _mac(model, gc, kc)                 # G (x) eK
+    mgg = _mac(model, gc, gc)
+    out = {}
+    # two N^3 products per slice and direction
+    wrap = 2 * N ** 3 * mgk
+    rot = 0
+    if model.kind == KIND_TV:
+        rot = model.z * 14 * N * N           # 2x2 block rotations per slice
+    out["wrap"] = 2 * Nt * (wrap + rot)
+    # local updates: rank-k update of G per accepted proposal
+    rank = 1 if model.kind == KIND_TU else 2
+    out["update"] = accepted * (rank * N * N * mgg + N * rank * rank * mgg)
+    # stabilisation: per node crossing (2 (NN-1) per sweep)
+    nodes = list(model.nodes)
+    n_cross = 2 * (len(nodes) - 1)
+    thin = Nt * 2 * (N * N * ns * mgk + (model.z * 14 * N * ns // 2 if model.kind == KIND_TV else 0))
+    hh = 2 * (2 * N * ns * ns - 2 * ns ** 3 // 3) * (mgg // 2)   # geqrf + orgqr (mgg/2 per op pair)
+    getg = (ns * ns * N + ns ** 3 // 3 + ns * ns * N + N * N * ns) * mgg
+    out["stabilise"] = thin + n_cross * (hh + getg)
+    if record:
+        out["measure"] = measure_wraps(model) * (wrap + rot) + measured_slices(model) * 2 * N ** 3 * mgk
+    else:
+        out["measure"] = 0
+    out["total"] = sum(out.values())
+    return out
+
+
+def _window(model):
+    NN = len(model.nodes)
+    Θidx = NN // 2 + 1
+    nodes = list(model.nodes)
+    fwd, bwd = [], []
+    for k in range(1, NN):
+        lo, hi = nodes[k - 1], nodes[k]
+        if model.kind == KIND_TU:
+            f_on = 0 <= Θidx - k <= 1
+            b_on = 0 <= (k + 1) - Θidx <= 1
+        else:
+            f_on = abs(k - Θidx) <= 1
+            b_on = abs(k + 1 - Θidx) <= 1
+        if f_on:
+            fwd += list(range(lo + 1, hi + 1))
+        if b_on:
+            bwd += [lt - 1 if model.kind == KIND_TV else lt for lt in range(hi, lo, -1)]
+    return fwd + bwd
+
+
+def measured_slices(model) -> int:
+    return len(_window(model))
+
+
+def measure_wraps(model) -> int:
+    """Slices wrapped by the measurements of one sweep (each to Nt/2)."""
+    half = model.Nt // 2
+    n = 0
+    for t0 in _window(model):
+        n += (t0 - half) if 2 * t0 > model.Nt else (half - t0)
+    return n
