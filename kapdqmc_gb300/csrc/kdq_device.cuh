@@ -149,6 +149,60 @@ __device__ void bgemm(int M, int N, int K, const TA* __restrict__ A, int lda,
   __syncthreads();
 }
 
+// 2-D register-tiled variant: the M x N output is cut into RS x CS micro-
+// tiles of TM x TN (RS = ceil(M/TM), CS = ceil(N/TN)); thread t owns the
+// micro-tile (t mod RS, t div RS) with rows r + RS*m and columns c + CS*n,
+// so consecutive lanes load consecutive rows of A and the B values of a
+// warp are near-broadcasts.  When RS*CS is a multiple of 32 no FP64 lane is
+// wasted (the FP64 pipe, not memory, bounds these products on GB300).
+template <int TM, int TN, class TA, class TB, class TC, class TS = double>
+__device__ void bgemm_t(int M, int N, int K, const TA* __restrict__ A, int lda,
+                        const TB* __restrict__ B, int ldb, TC* __restrict__ C, int ldc,
+                        const TS* rs = nullptr, const TS* cs = nullptr) {
+  const int RS = (M + TM - 1) / TM, CS = (N + TN - 1) / TN;
+  const int tiles = RS * CS;
+  for (int t = threadIdx.x; t < tiles; t += blockDim.x) {
+    const int r0 = t % RS, c0 = t / RS;
+    TC acc[TM][TN];
+#pragma unroll
+    for (int m = 0; m < TM; ++m)
+#pragma unroll
+      for (int n = 0; n < TN; ++n) acc[m][n] = zero<TC>();
+    int rows[TM], cols[TN];
+#pragma unroll
+    for (int m = 0; m < TM; ++m) rows[m] = min(r0 + RS * m, M - 1);
+#pragma unroll
+    for (int n = 0; n < TN; ++n) cols[n] = min(c0 + CS * n, N - 1);
+    for (int k = 0; k < K; ++k) {
+      TA a[TM];
+      TB b[TN];
+#pragma unroll
+      for (int m = 0; m < TM; ++m) a[m] = A[rows[m] + (size_t)k * lda];
+#pragma unroll
+      for (int n = 0; n < TN; ++n) b[n] = B[k + (size_t)cols[n] * ldb];
+#pragma unroll
+      for (int m = 0; m < TM; ++m)
+#pragma unroll
+        for (int n = 0; n < TN; ++n) madd(acc[m][n], a[m], b[n]);
+    }
+#pragma unroll
+    for (int m = 0; m < TM; ++m) {
+      const int i = r0 + RS * m;
+      if (i >= M) continue;
+#pragma unroll
+      for (int n = 0; n < TN; ++n) {
+        const int j = c0 + CS * n;
+        if (j >= N) continue;
+        TC v = acc[m][n];
+        if (rs) v = rs[i] * v;
+        if (cs) v = v * cs[j];
+        C[i + (size_t)j * ldc] = v;
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // ------------------------------------------------ Householder QR (thin Q)
 // Overwrites Q (N x n, column-major, ld N) with an orthonormal basis of the
 // column space of Y (N x n, ld N), destroying Y.  Reflectors

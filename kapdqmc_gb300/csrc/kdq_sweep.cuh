@@ -30,6 +30,28 @@ __device__ inline uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 
+// Register tiles of the block GEMMs per lattice-size class (MAXRM = row
+// groups of 32: N <= 32, <= 96, <= 192) and arithmetic: square N x N
+// products and thin N x ns / ns x N products.  Chosen so that the tile grid
+// fills whole warps at the configured lattice sizes (72 real: 24 x 8 tiles
+// of 3 x 9; 64 complex: 32 x 8 tiles of 2 x 8).
+template <int MAXRM, class T> struct Tiles;
+template <class T> struct Tiles<1, T> { static constexpr int SM = 1, SN = 4, TM = 1, TN = 4; };
+template <> struct Tiles<3, double> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 4; };
+template <> struct Tiles<3, cd> { static constexpr int SM = 2, SN = 8, TM = 2, TN = 4; };
+template <class T> struct Tiles<6, T> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 6; };
+
+template <int MAXRM, class T, class TA, class TB, class TC, class TS = double>
+__device__ inline void gemm_sq(int M, int N, int K, const TA* A, int lda, const TB* B, int ldb, TC* C,
+                               int ldc, const TS* rs = nullptr, const TS* cs = nullptr) {
+  bgemm_t<Tiles<MAXRM, T>::SM, Tiles<MAXRM, T>::SN>(M, N, K, A, lda, B, ldb, C, ldc, rs, cs);
+}
+template <int MAXRM, class T, class TA, class TB, class TC, class TS = double>
+__device__ inline void gemm_thin(int M, int N, int K, const TA* A, int lda, const TB* B, int ldb, TC* C,
+                                 int ldc, const TS* rs = nullptr, const TS* cs = nullptr) {
+  bgemm_t<Tiles<MAXRM, T>::TM, Tiles<MAXRM, T>::TN>(M, N, K, A, lda, B, ldb, C, ldc, rs, cs);
+}
+
 // Per-CTA shared scratch (static part; the tape slice is dynamic).
 template <class T>
 struct Smem {
@@ -124,8 +146,8 @@ template <int MAXRM, int KIND, class T, class KT>
 __device__ void wrap_fwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
   const int N = c.P.Ns;
   slice_diag(c, lt, +1);
-  bgemm<MAXRM>(N, N, N, c.eK, N, G, N, W, N);                       // eK G
-  bgemm<MAXRM>(N, N, N, W, N, c.eKinv, N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
+  gemm_sq<MAXRM, T>(N, N, N, c.eK, N, G, N, W, N);                       // eK G
+  gemm_sq<MAXRM, T>(N, N, N, W, N, c.eKinv, N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
 }
 
 // G <- B_lt^{-1} G B_lt: WrapKV!("Backward","B"), src/tU/GreenMatrix.jl:78-83.
@@ -138,49 +160,61 @@ __device__ void wrap_bwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
     G[e] = (c.sm.dvec[i] * G[e]) * c.sm.dinv[j];
   }
   __syncthreads();
-  bgemm<MAXRM>(N, N, N, c.eKinv, N, G, N, W, N);
-  bgemm<MAXRM>(N, N, N, W, N, c.eK, N, G, N);
+  gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, G, N, W, N);
+  gemm_sq<MAXRM, T>(N, N, N, W, N, c.eK, N, G, N);
 }
 
 // tV bond rotation of direction j on both sides of G:
-// G <- UV D UV G UV D^-1 UV with UV a direct sum of 2x2 blocks
-// u = [-c -c; -c c]: WrapV!(..,"B"), src/tV/GreenMatrix.jl:110-118.  Every
-// 2x2 block of G (bond i rows, bond i' columns) transforms independently.
+// G <- (UV D UV) G (UV D^-1 UV) (WrapV!(..,"B"), src/tV/GreenMatrix.jl:110-118).
+// UV is a direct sum of 2x2 blocks u = [-c -c; -c c] (c = 2^-1/2) over the
+// bonds of direction j, a perfect matching, so UV D UV is the direct sum of
+// L_b = u diag(d_x, d_y) u = 1/2 [d_x+d_y, d_x-d_y; d_x-d_y, d_x+d_y] and every
+// 2x2 block of G (bond b rows, bond b' columns) becomes L_b B R_b'.
+// The per-bond coefficients are staged in sm.dvec / sm.dinv as (plus, minus)
+// pairs for rows (L) and columns (R).
+template <int KIND, class T, class KT>
+__device__ void tv_coeffs(Ctx<KIND, T, KT>& c, int lt, int j, int sign) {
+  const SweepParams& P = c.P;
+  const int nb = P.Ns / 2;
+  const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * nb;
+  // vtab per slice: [D_x | D_y | 1/D_x | 1/D_y] forward, then the same backward
+  const double* tab = P.vtab + (size_t)(lt - 1) * 32 + (sign > 0 ? 0 : 16);
+  double* L = reinterpret_cast<double*>(c.sm.dvec);
+  double* R = reinterpret_cast<double*>(c.sm.dinv);
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    const int v = sl[i] - 1;
+    const double dx = tab[v], dy = tab[4 + v], ix = tab[8 + v], iy = tab[12 + v];
+    L[2 * i] = 0.5 * (dx + dy);
+    L[2 * i + 1] = 0.5 * (dx - dy);
+    R[2 * i] = 0.5 * (ix + iy);
+    R[2 * i + 1] = 0.5 * (ix - iy);
+  }
+  __syncthreads();
+}
+
 template <int KIND, class T, class KT>
 __device__ void tv_rotate(Ctx<KIND, T, KT>& c, T* G, int lt, int j, int sign) {
   const SweepParams& P = c.P;
   const int N = P.Ns, nb = N / 2;
-  const double h = 0.70710678118654752440;  // 2^0.5/2
-  const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * nb;
-  // vtab per slice: [D_x | D_y | 1/D_x | 1/D_y] forward, then the same backward
-  const double* tab = P.vtab + (size_t)(lt - 1) * 32 + (sign > 0 ? 0 : 16);
+  tv_coeffs(c, lt, j, sign);
+  const double* L = reinterpret_cast<const double*>(c.sm.dvec);
+  const double* R = reinterpret_cast<const double*>(c.sm.dinv);
   const int* bx = P.bx + (size_t)j * nb;
   const int* by = P.by + (size_t)j * nb;
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int i = e % nb, ip = e / nb;
     const int x = bx[i], y = by[i], xp = bx[ip], yp = by[ip];
-    const double dx = tab[sl[i] - 1], dy = tab[4 + sl[i] - 1];          // D on rows x, y
-    const double cxp = tab[8 + sl[ip] - 1], cyp = tab[12 + sl[ip] - 1]; // 1 ./ D on columns x', y'
-    double g00 = re(G[x + (size_t)xp * N]), g01 = re(G[x + (size_t)yp * N]);
-    double g10 = re(G[y + (size_t)xp * N]), g11 = re(G[y + (size_t)yp * N]);
-    // UV * G
-    double a00 = -h * g00 - h * g10, a01 = -h * g01 - h * g11;
-    double a10 = -h * g00 + h * g10, a11 = -h * g01 + h * g11;
-    // * UV
-    g00 = -h * a00 - h * a01; g01 = -h * a00 + h * a01;
-    g10 = -h * a10 - h * a11; g11 = -h * a10 + h * a11;
-    // D * G * D^-1
-    g00 = (dx * g00) * cxp; g01 = (dx * g01) * cyp;
-    g10 = (dy * g10) * cxp; g11 = (dy * g11) * cyp;
-    // UV * G * UV
-    a00 = -h * g00 - h * g10; a01 = -h * g01 - h * g11;
-    a10 = -h * g00 + h * g10; a11 = -h * g01 + h * g11;
-    g00 = -h * a00 - h * a01; g01 = -h * a00 + h * a01;
-    g10 = -h * a10 - h * a11; g11 = -h * a10 + h * a11;
-    G[x + (size_t)xp * N] = from_real<T>(g00);
-    G[x + (size_t)yp * N] = from_real<T>(g01);
-    G[y + (size_t)xp * N] = from_real<T>(g10);
-    G[y + (size_t)yp * N] = from_real<T>(g11);
+    const double lp = L[2 * i], lm = L[2 * i + 1], rp = R[2 * ip], rm = R[2 * ip + 1];
+    const double g00 = re(G[x + (size_t)xp * N]), g01 = re(G[x + (size_t)yp * N]);
+    const double g10 = re(G[y + (size_t)xp * N]), g11 = re(G[y + (size_t)yp * N]);
+    // L B
+    const double a00 = fma(lp, g00, lm * g10), a01 = fma(lp, g01, lm * g11);
+    const double a10 = fma(lm, g00, lp * g10), a11 = fma(lm, g01, lp * g11);
+    // (L B) R
+    G[x + (size_t)xp * N] = from_real<T>(fma(a00, rp, a01 * rm));
+    G[x + (size_t)yp * N] = from_real<T>(fma(a00, rm, a01 * rp));
+    G[y + (size_t)xp * N] = from_real<T>(fma(a10, rp, a11 * rm));
+    G[y + (size_t)yp * N] = from_real<T>(fma(a10, rm, a11 * rp));
   }
   __syncthreads();
 }
@@ -278,9 +312,10 @@ __device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t
       c.ctl->n_acc += acc;
     }
   } else {
+    // w = E_S - G[S,:]
     for (int b = tid - 32; b < N; b += blockDim.x - 32) {
-      sm.wrow[0][b] = G[x + (size_t)b * N];
-      if constexpr (RK == 2) sm.wrow[1][b] = G[y + (size_t)b * N];
+      sm.wrow[0][b] = (b == x ? one<T>() : zero<T>()) - G[x + (size_t)b * N];
+      if constexpr (RK == 2) sm.wrow[1][b] = (b == y ? one<T>() : zero<T>()) - G[y + (size_t)b * N];
     }
   }
   __syncthreads();
@@ -288,12 +323,8 @@ __device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t
     for (int e = tid; e < N * N; e += blockDim.x) {
       const int a = e % N, b = e / N;
       T v = G[e];
-      const T w0 = (b == x ? one<T>() : zero<T>()) - sm.wrow[0][b];
-      v = v - sm.ucol[0][a] * w0;
-      if constexpr (RK == 2) {
-        const T w1 = (b == y ? one<T>() : zero<T>()) - sm.wrow[1][b];
-        v = v - sm.ucol[1][a] * w1;
-      }
+      madd(v, -sm.ucol[0][a], sm.wrow[0][b]);
+      if constexpr (RK == 2) madd(v, -sm.ucol[1][a], sm.wrow[1][b]);
       G[e] = v;
     }
     if (tid == 0) *sfield = (uint8_t)sm.newv;
@@ -377,27 +408,23 @@ __device__ T* apply_slice_left(Ctx<KIND, T, KT>& c, T* Y, T* Y2, int lt) {
   const SweepParams& P = c.P;
   const int N = P.Ns, ns = N / 2;
   if constexpr (KIND == KDQ_TV) {
-    bgemm<MAXRM>(N, ns, N, c.eK, N, Y, N, Y2, N);
-    const double h = 0.70710678118654752440;
+    gemm_thin<MAXRM, T>(N, ns, N, c.eK, N, Y, N, Y2, N);
     for (int j = P.z - 1; j >= 0; --j) {
-      const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * (N / 2);
-      const double* tab = P.vtab + (size_t)(lt - 1) * 32;
+      tv_coeffs(c, lt, j, +1);
+      const double* L = reinterpret_cast<const double*>(c.sm.dvec);
       for (int e = threadIdx.x; e < (N / 2) * ns; e += blockDim.x) {
         const int i = e % (N / 2), col = e / (N / 2);
         const int x = P.bx[j * (N / 2) + i], y = P.by[j * (N / 2) + i];
-        const double dx = tab[sl[i] - 1], dy = tab[4 + sl[i] - 1];
-        double vx = re(Y2[x + (size_t)col * N]), vy = re(Y2[y + (size_t)col * N]);
-        double ax = -h * vx - h * vy, ay = -h * vx + h * vy;   // UV *
-        ax *= dx; ay *= dy;                                     // D *
-        vx = -h * ax - h * ay; vy = -h * ax + h * ay;           // UV *
-        Y2[x + (size_t)col * N] = from_real<T>(vx);
-        Y2[y + (size_t)col * N] = from_real<T>(vy);
+        const double lp = L[2 * i], lm = L[2 * i + 1];
+        const double vx = re(Y2[x + (size_t)col * N]), vy = re(Y2[y + (size_t)col * N]);
+        Y2[x + (size_t)col * N] = from_real<T>(fma(lp, vx, lm * vy));
+        Y2[y + (size_t)col * N] = from_real<T>(fma(lm, vx, lp * vy));
       }
       __syncthreads();
     }
   } else {
     slice_diag(c, lt, +1);
-    bgemm<MAXRM>(N, ns, N, c.eK, N, Y, N, Y2, N, c.sm.dvec, (const T*)nullptr);
+    gemm_thin<MAXRM, T>(N, ns, N, c.eK, N, Y, N, Y2, N, c.sm.dvec, (const T*)nullptr);
   }
   return Y2;
 }
@@ -408,24 +435,20 @@ __device__ T* apply_slice_right(Ctx<KIND, T, KT>& c, T* Z, T* Z2, int lt) {
   const SweepParams& P = c.P;
   const int N = P.Ns, ns = N / 2;
   if constexpr (KIND == KDQ_TV) {
-    const double h = 0.70710678118654752440;
-    const double* tab = P.vtab + (size_t)(lt - 1) * 32;
-    for (int j = 0; j < P.z; ++j) {        // Z V_1 V_2 ... V_z
-      const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * (N / 2);
+    for (int j = 0; j < P.z; ++j) {        // Z V_1 V_2 ... V_z, V_j = L (symmetric)
+      tv_coeffs(c, lt, j, +1);
+      const double* L = reinterpret_cast<const double*>(c.sm.dvec);
       for (int e = threadIdx.x; e < ns * (N / 2); e += blockDim.x) {
         const int row = e % ns, i = e / ns;
         const int x = P.bx[j * (N / 2) + i], y = P.by[j * (N / 2) + i];
-        const double dx = tab[sl[i] - 1], dy = tab[4 + sl[i] - 1];
-        double vx = re(Z[row + (size_t)x * ns]), vy = re(Z[row + (size_t)y * ns]);
-        double ax = -h * vx - h * vy, ay = -h * vx + h * vy;   // * UV
-        ax *= dx; ay *= dy;                                     // * D
-        vx = -h * ax - h * ay; vy = -h * ax + h * ay;           // * UV
-        Z[row + (size_t)x * ns] = from_real<T>(vx);
-        Z[row + (size_t)y * ns] = from_real<T>(vy);
+        const double lp = L[2 * i], lm = L[2 * i + 1];
+        const double vx = re(Z[row + (size_t)x * ns]), vy = re(Z[row + (size_t)y * ns]);
+        Z[row + (size_t)x * ns] = from_real<T>(fma(vx, lp, vy * lm));
+        Z[row + (size_t)y * ns] = from_real<T>(fma(vx, lm, vy * lp));
       }
       __syncthreads();
     }
-    bgemm<MAXRM>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
+    gemm_thin<MAXRM, T>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
   } else {
     slice_diag(c, lt, +1);
     for (int e = threadIdx.x; e < ns * N; e += blockDim.x) {
@@ -433,7 +456,7 @@ __device__ T* apply_slice_right(Ctx<KIND, T, KT>& c, T* Z, T* Z2, int lt) {
       Z[e] = Z[e] * c.sm.dvec[col];
     }
     __syncthreads();
-    bgemm<MAXRM>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
+    gemm_thin<MAXRM, T>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
   }
   return Z2;
 }
@@ -443,7 +466,7 @@ __device__ T* apply_slice_right(Ctx<KIND, T, KT>& c, T* Z, T* Z2, int lt) {
 template <int MAXRM, int KIND, class T, class KT>
 __device__ void get_G(Ctx<KIND, T, KT>& c, const T* BL, const T* BR, bool drift) {
   const int N = c.P.Ns, ns = N / 2;
-  bgemm<MAXRM>(ns, ns, N, BL, ns, BR, N, c.Mss, ns);
+  gemm_thin<MAXRM, T>(ns, ns, N, BL, ns, BR, N, c.Mss, ns);
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
@@ -451,7 +474,7 @@ __device__ void get_G(Ctx<KIND, T, KT>& c, const T* BL, const T* BR, bool drift)
   for (int e = threadIdx.x; e < ns * N; e += blockDim.x) c.X[e] = BL[e];
   __syncthreads();
   lu_solve(ns, N, c.Mss, c.piv, c.X);
-  bgemm<MAXRM>(N, N, ns, BR, N, c.X, ns, c.W1, N);
+  gemm_sq<MAXRM, T>(N, N, ns, BR, N, c.X, ns, c.W1, N);
   double d2 = 0.0, n2 = 0.0;
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
     const int i = e % N, j = e / N;
@@ -559,8 +582,8 @@ __device__ void measure(Ctx<KIND, T, KT>& c, int t0) {
     for (int t = t0; t > half; --t) {
       if constexpr (KIND == KDQ_TV) {
         for (int j = 0; j < P.z; ++j) tv_rotate(c, G0, t, j, -1);
-        bgemm<MAXRM>(N, N, N, c.eKinv, N, G0, N, W, N);
-        bgemm<MAXRM>(N, N, N, W, N, c.eK, N, G0, N);
+        gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, G0, N, W, N);
+        gemm_sq<MAXRM, T>(N, N, N, W, N, c.eK, N, G0, N);
       } else {
         wrap_bwd_kv<MAXRM>(c, G0, W, t);
       }
@@ -568,16 +591,16 @@ __device__ void measure(Ctx<KIND, T, KT>& c, int t0) {
   } else {
     for (int t = t0 + 1; t <= half; ++t) {
       if constexpr (KIND == KDQ_TV) {
-        bgemm<MAXRM>(N, N, N, G0, N, c.eKinv, N, W, N);
-        bgemm<MAXRM>(N, N, N, c.eK, N, W, N, G0, N);
+        gemm_sq<MAXRM, T>(N, N, N, G0, N, c.eKinv, N, W, N);
+        gemm_sq<MAXRM, T>(N, N, N, c.eK, N, W, N, G0, N);
         for (int j = P.z - 1; j >= 0; --j) tv_rotate(c, G0, t, j, +1);
       } else {
         wrap_fwd_kv<MAXRM>(c, G0, W, t);
       }
     }
   }
-  bgemm<MAXRM>(N, N, N, c.HalfeK, N, G0, N, W, N);
-  bgemm<MAXRM>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
+  gemm_sq<MAXRM, T>(N, N, N, c.HalfeK, N, G0, N, W, N);
+  gemm_sq<MAXRM, T>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
 
   double acc[KDQ_MAX_OBS];
 #pragma unroll
@@ -739,8 +762,8 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
     const bool rec = P.record && (KIND == KDQ_TU ? (Θidx - k >= 0 && Θidx - k <= 1) : abs(k - Θidx) <= 1);
     for (int lt = lo + 1; lt <= hi; ++lt) {
       if constexpr (KIND == KDQ_TV) {
-        bgemm<MAXRM>(N, N, N, c.G, N, c.eKinv, N, c.W1, N);
-        bgemm<MAXRM>(N, N, N, c.eK, N, c.W1, N, c.G, N);
+        gemm_sq<MAXRM, T>(N, N, N, c.G, N, c.eKinv, N, c.W1, N);
+        gemm_sq<MAXRM, T>(N, N, N, c.eK, N, c.W1, N, c.G, N);
         for (int j = P.z - 1; j >= 0; --j) {
           tv_rotate(c, c.G, lt, j, +1);
           update_layer(c, lt, j, true);
@@ -762,8 +785,8 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
           update_layer(c, lt, j, false);
           tv_rotate(c, c.G, lt, j, -1);
         }
-        bgemm<MAXRM>(N, N, N, c.eKinv, N, c.G, N, c.W1, N);
-        bgemm<MAXRM>(N, N, N, c.W1, N, c.eK, N, c.G, N);
+        gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, c.G, N, c.W1, N);
+        gemm_sq<MAXRM, T>(N, N, N, c.W1, N, c.eK, N, c.G, N);
         if (rec) measure<MAXRM>(c, lt - 1);
       } else {
         update_layer(c, lt, 0, false);
