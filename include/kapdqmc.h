@@ -157,6 +157,20 @@ int kdq_get_accept_log(kdq_handle* h, uint8_t* flags, size_t nbytes);
  * "Batchsize Wrap Error" check, src/tU/phy_update.jl:89-97). */
 int kdq_get_drift(kdq_handle* h, double* drift, size_t len);
 
+/* Swap-replica Rényi-2 Grover determinant det(2 G1_A G2_A - G1_A - G2_A + I)
+ * (GroverMatrix!, src/public/GF.jl:101-109, and the det of get_ABGM!,
+ * src/tU/SCEE.jl:264-276) for npairs replica pairs.  G holds 2*npairs
+ * Ns x Ns matrices (pair p = matrices 2p and 2p+1; host memory, column-major,
+ * interleaved complex iff g_complex); index holds the nA 1-based sites of
+ * region A; det receives (re, im) per pair.  e^{-S2} is estimated by
+ * <|det|^2> for the spinful models and <det> for t-V. */
+int kdq_grover_det(const double* G, int32_t Ns, int32_t g_complex, int32_t npairs, const int32_t* index,
+                   int32_t nA, double* det, int32_t device);
+
+/* The same for the chains of a handle, paired (0,1), (2,3), ..., at their
+ * current time slice. */
+int kdq_grover_det_chains(kdq_handle* h, const int32_t* index, int32_t nA, double* det);
+
 /* CUDA stream (cudaStream_t) of the handle, for event timing by callers. */
 void* kdq_stream(kdq_handle* h);
 

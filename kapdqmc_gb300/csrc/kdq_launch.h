@@ -13,4 +13,9 @@ cudaError_t launch_tv(const SweepParams& P, int mode, int k, int maxrm, int ncha
                       cudaStream_t st);
 cudaError_t launch_tuv(const SweepParams& P, int mode, int k, int maxrm, bool g_complex,
                        int nchains, size_t dyn, cudaStream_t st);
+// Grover determinants of npairs replica pairs (matrices 2p, 2p+1 of G).
+// scratch: npairs * 3 * nA^2 elements of the G type; pivs: npairs * nA.
+cudaError_t launch_grover(const void* G, int Ns, bool g_complex, const int* index, int nA, int npairs,
+                          void* scratch, int* pivs, double* det, cudaStream_t st);
+size_t grover_scratch_bytes(int nA, int npairs, bool g_complex);
 }  // namespace kdq

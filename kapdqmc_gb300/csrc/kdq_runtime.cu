@@ -58,6 +58,8 @@ struct kdq_handle {
   DevBuf G, W1, W2, Y, Y2, Mss, X, piv, BLs, BRs, s, ctl;
   // outputs
   DevBuf obs, acc_log, drift, tape_k, tape_u;
+  // Grover-determinant workspace
+  DevBuf gr_scratch, gr_piv, gr_index, gr_det;
   int obs_rows = 0;      // rows recorded since kdq_init
   int obs_capacity = 0;  // rows allocated
   long long acc_log_cap = 0;
@@ -688,4 +690,74 @@ int kdq_get_stats(kdq_handle* h, kdq_stats* st) {
   return KDQ_OK;
 }
 
+// ------------------------------------------------------------ Grover det
+namespace {
+int check_region(const int32_t* index, int32_t nA, int32_t Ns, std::string& why) {
+  if (!index || nA < 1 || nA > Ns) { why = "region size must be in [1, Ns]"; return 1; }
+  for (int i = 0; i < nA; ++i)
+    if (index[i] < 1 || index[i] > Ns) { why = "region index out of range (1-based)"; return 1; }
+  return 0;
+}
+}  // namespace
+
+int kdq_grover_det(const double* G, int32_t Ns, int32_t g_complex, int32_t npairs, const int32_t* index,
+                   int32_t nA, double* det, int32_t device) {
+  auto set_err = [](int code, const std::string& msg) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = msg;
+    return code;
+  };
+  std::string why;
+  if (!G || !det) return set_err(KDQ_ERR_ARG, "NULL argument");
+  if (Ns < 2 || npairs < 0) return set_err(KDQ_ERR_ARG, "bad sizes");
+  if (check_region(index, nA, Ns, why)) return set_err(KDQ_ERR_ARG, why);
+  if (npairs == 0) return KDQ_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return set_err(KDQ_ERR_NOGPU, "cannot select device");
+  const size_t esz = g_complex ? 16 : 8;
+  const size_t gbytes = (size_t)2 * npairs * Ns * Ns * esz;
+  std::vector<int> idx0(nA);
+  for (int i = 0; i < nA; ++i) idx0[i] = index[i] - 1;
+  DevBuf dG, dScr, dPiv, dIdx, dDet;
+  cudaError_t e;
+  if ((e = dG.alloc(gbytes)) || (e = dScr.alloc(kdq::grover_scratch_bytes(nA, npairs, g_complex))) ||
+      (e = dPiv.alloc((size_t)npairs * nA * sizeof(int))) || (e = dIdx.alloc((size_t)nA * sizeof(int))) ||
+      (e = dDet.alloc((size_t)2 * npairs * sizeof(double))))
+    return set_err(KDQ_ERR_CUDA, cudaGetErrorString(e));
+  if ((e = cudaMemcpy(dG.p, G, gbytes, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(dIdx.p, idx0.data(), (size_t)nA * sizeof(int), cudaMemcpyHostToDevice)) ||
+      (e = kdq::launch_grover(dG.p, Ns, g_complex != 0, dIdx.as<int>(), nA, npairs, dScr.p, dPiv.as<int>(),
+                              dDet.as<double>(), nullptr)) ||
+      (e = cudaMemcpy(det, dDet.p, (size_t)2 * npairs * sizeof(double), cudaMemcpyDeviceToHost)))
+    return set_err(KDQ_ERR_CUDA, cudaGetErrorString(e));
+  return KDQ_OK;
+}
+
+int kdq_grover_det_chains(kdq_handle* h, const int32_t* index, int32_t nA, double* det) {
+  if (!h || !det) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  std::string why;
+  if (check_region(index, nA, h->Ns, why)) return fail(h, KDQ_ERR_ARG, why);
+  const int npairs = h->nchains / 2;
+  if (npairs == 0) return fail(h, KDQ_ERR_ARG, "need at least two chains");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  const size_t sb = kdq::grover_scratch_bytes(nA, npairs, h->gc);
+  if (h->gr_scratch.bytes < sb) KDQ_CUDA(h, h->gr_scratch.alloc(sb));
+  if (h->gr_piv.bytes < (size_t)npairs * nA * sizeof(int)) KDQ_CUDA(h, h->gr_piv.alloc((size_t)npairs * nA * sizeof(int)));
+  if (h->gr_index.bytes < (size_t)nA * sizeof(int)) KDQ_CUDA(h, h->gr_index.alloc((size_t)nA * sizeof(int)));
+  if (h->gr_det.bytes < (size_t)2 * npairs * sizeof(double)) KDQ_CUDA(h, h->gr_det.alloc((size_t)2 * npairs * sizeof(double)));
+  std::vector<int> idx0(nA);
+  for (int i = 0; i < nA; ++i) idx0[i] = index[i] - 1;
+  KDQ_CUDA(h, cudaMemcpyAsync(h->gr_index.p, idx0.data(), (size_t)nA * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  KDQ_CUDA(h, kdq::launch_grover(h->G.p, h->Ns, h->gc, h->gr_index.as<int>(), nA, npairs, h->gr_scratch.p,
+                                 h->gr_piv.as<int>(), h->gr_det.as<double>(), h->stream));
+  KDQ_CUDA(h, cudaMemcpyAsync(det, h->gr_det.p, (size_t)2 * npairs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  return KDQ_OK;
+}
+
 }  // extern "C"
+
+namespace kdq {
+size_t grover_scratch_bytes(int nA, int npairs, bool g_complex) {
+  return (size_t)npairs * 3 * nA * nA * (g_complex ? 16 : 8);
+}
+}  // namespace kdq

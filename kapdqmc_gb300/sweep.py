@@ -191,11 +191,43 @@ class Sweeper:
         self._ck(self.lib.kdq_get_accept_log(self.h, out.ctypes.data, out.size))
         return out.reshape(self.nchains, self._acc_cap)
 
+    def grover_det(self, index):
+        """Grover determinants of the chain pairs (0,1), (2,3), ... at their current slice."""
+        idx = np.ascontiguousarray(np.asarray(index, dtype=np.int32))
+        out = np.empty(2 * (self.nchains // 2))
+        self._ck(self.lib.kdq_grover_det_chains(self.h, idx.ctypes.data, idx.size, out.ctypes.data))
+        return out.view(np.complex128)
+
     def drift(self, sweeps: int):
         n = sweeps * 2 * (len(self.model.nodes) - 1)
         out = np.empty(self.nchains * n)
         self._ck(self.lib.kdq_get_drift(self.h, out.ctypes.data, out.size))
         return out.reshape(self.nchains, n)
+
+
+def grover_det(G1, G2, index, device: int = 0):
+    """det(2 G1_A G2_A - G1_A - G2_A + I) for stacks of replica pairs.
+
+    G1, G2: (npairs, Ns, Ns) or (Ns, Ns) arrays; index: 1-based sites of A.
+    GroverMatrix! (src/public/GF.jl:101-109) and the det of get_ABGM!
+    (src/tU/SCEE.jl:264-276).  Returns complex determinants (npairs,).
+    """
+    lib = _lib.load()
+    G1 = np.asarray(G1)
+    G2 = np.asarray(G2)
+    if G1.ndim == 2:
+        G1, G2 = G1[None], G2[None]
+    gc = np.iscomplexobj(G1) or np.iscomplexobj(G2)
+    npairs, Ns = G1.shape[0], G1.shape[1]
+    mats = []
+    for a, b in zip(G1, G2):
+        mats += [_mat(a, gc), _mat(b, gc)]
+    buf = np.ascontiguousarray(np.concatenate(mats))
+    idx = np.ascontiguousarray(np.asarray(index, dtype=np.int32))
+    out = np.empty(2 * npairs)
+    _lib.check(lib.kdq_grover_det(buf.ctypes.data, Ns, int(gc), npairs, idx.ctypes.data, idx.size,
+                                  out.ctypes.data, device), None)
+    return out.view(np.complex128)
 
 
 # ------------------------------------------------------------------------

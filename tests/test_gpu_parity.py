@@ -139,3 +139,34 @@ def test_split_api_continues_state():
         g11 = sw.get_fields()
     np.testing.assert_array_equal(g2, g11)
     np.testing.assert_allclose(o2, o11, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("cplx", [True, False])
+def test_grover_det_matches_oracle(cplx):
+    from kapdqmc_gb300.sweep import grover_det
+    rng = np.random.default_rng(3)
+    Ns, npairs = 64, 5
+    index = list(range(1, 33))                     # region A = 32 sites
+    Gs = []
+    for _ in range(2 * npairs):
+        A = rng.normal(size=(Ns, Ns // 2)) + (1j * rng.normal(size=(Ns, Ns // 2)) if cplx else 0)
+        Q = np.linalg.qr(A)[0]
+        Gs.append(np.eye(Ns) - Q @ Q.conj().T)    # a pure-state Green's function
+    G1, G2 = np.array(Gs[0::2]), np.array(Gs[1::2])
+    got = grover_det(G1, G2, index)
+    want = np.array([O.grover_det(a, b, index) for a, b in zip(G1, G2)])
+    np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-14)
+
+
+def test_grover_det_of_sweep_chains():
+    model = cases.tuv_square()
+    fields = np.stack([Initial_s(model, 40 + c) for c in range(4)])
+    index = list(range(1, 9))
+    with Sweeper(model, 4) as sw:
+        sw.set_fields(fields)
+        sw.set_rng(11)
+        sw.phy_update(1)
+        dets = sw.grover_det(index)
+        G = [sw.green(c) for c in range(4)]
+    want = [O.grover_det(G[0], G[1], index), O.grover_det(G[2], G[3], index)]
+    np.testing.assert_allclose(dets, want, rtol=1e-10, atol=1e-14)
