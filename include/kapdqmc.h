@@ -171,6 +171,23 @@ int kdq_grover_det(const double* G, int32_t Ns, int32_t g_complex, int32_t npair
  * current time slice. */
 int kdq_grover_det_chains(kdq_handle* h, const int32_t* index, int32_t nA, double* det);
 
+/* Allocation-free form of kdq_grover_det, for callers that must not call
+ * cudaMalloc (work recorded into a CUDA graph or run where a device
+ * synchronisation is unaffordable, and processes whose free device memory is
+ * held by another allocator).  No counterpart in the reference.  G (2*npairs
+ * Ns x Ns matrices), index (nA 1-based sites) and det (2*npairs doubles) are
+ * DEVICE pointers supplied by the caller; the work is queued on `stream`
+ * (a cudaStream_t; NULL = default stream) and det is valid once that stream
+ * has been synchronised.  Scratch comes from one fixed 8 MiB device array per
+ * GPU, shared by all calls: requests needing more (npairs * (3 nA^2 elements
+ * + nA ints) plus nA ints, with 256-byte padding) fail with KDQ_ERR_ARG, and
+ * calls that overlap on the GPU race on the array.  Region indices outside
+ * 1..Ns give NaN determinants.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Errors are reported through kdq_last_error(NULL). */
+int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32_t npairs,
+                           const int32_t* index, int32_t nA, double* det, void* stream);
+
 /* CUDA stream (cudaStream_t) of the handle, for event timing by callers. */
 void* kdq_stream(kdq_handle* h);
 

@@ -757,6 +757,12 @@ int kdq_grover_det_chains(kdq_handle* h, const int32_t* index, int32_t nA, doubl
 }  // extern "C"
 
 namespace kdq {
+// Message returned by kdq_last_error(NULL) for the handle-free entry points.
+void set_global_error(const std::string& msg) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_create_err = msg;
+}
+
 size_t grover_scratch_bytes(int nA, int npairs, bool g_complex) {
   return (size_t)npairs * 3 * nA * nA * (g_complex ? 16 : 8);
 }
