@@ -135,6 +135,15 @@ def fp64_peak_tflops(torch, dev):
     return best
 
 
+def traffic_per_launch():
+    """DRAM bytes (read + write) per sweep-kernel launch from the committed ncu capture."""
+    try:
+        return float(json.loads((ROOT / "profiles" / "k_block_tv6x6_traffic.json").read_text())
+                     ["dram_bytes_per_launch"])
+    except Exception:
+        return None
+
+
 def hbm_peak_gbs():
     try:
         return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
@@ -144,9 +153,10 @@ def hbm_peak_gbs():
 
 # ---------------------------------------------------------------- CPU arm
 def _cpu_worker(args):
+    """One chain of the workload through the C restatement of the reference sweep."""
     seed, chain, sweeps = args
-    os.environ["OMP_NUM_THREADS"] = "1"
     sys.path.insert(0, str(ROOT / "oracle"))
+    import cport_tv
     import dqmc_oracle as O
     import philox
     from kapdqmc_gb300 import Initial_s
@@ -154,25 +164,71 @@ def _cpu_worker(args):
     s = Initial_s(model, 1000 + chain)
     n = O.proposals_per_sweep(model)
     ks, us = zip(*(philox.tape(seed, chain, w, n) for w in range(sweeps)))
+    cport_tv.load()
     t0 = time.perf_counter()
-    O.phy_update(model, s, sweeps, O.Tape(np.concatenate(ks), np.concatenate(us)), record=True)
+    cport_tv.tv_phy_update(model, s, sweeps, np.concatenate(ks), np.concatenate(us), record=True)
     return time.perf_counter() - t0
 
 
-def _cpu_init():
-    for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
-        os.environ[v] = "1"
+CPU_KIND = "port"
+CPU_SAMPLE = ("C restatement of the reference t-V sweep (dense bond-rotation GEMMs as the reference; "
+              "OpenBLAS/LAPACK from numpy, 1 thread each), one chain per host core")
 
 
 def cpu_chain_sweeps_per_s(cores: int, sweeps_per_chain: int = 1):
-    """Oracle (CPU restatement) throughput: one chain per core, all cores busy."""
+    """CPU throughput of the reference algorithm: one chain per core, all cores busy."""
     import multiprocessing as mp
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores, initializer=_cpu_init) as pool:
-        t0 = time.perf_counter()
-        pool.map(_cpu_worker, [(7, c, sweeps_per_chain) for c in range(cores)])
-        wall = time.perf_counter() - t0
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cport_tv
+    cport_tv.build()
+    saved = {v: os.environ.get(v) for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+    for v in saved:                         # inherited by the workers before numpy loads
+        os.environ[v] = "1"
+    try:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            pool.map(_cpu_worker, [(7, c, 0) for c in range(cores)])        # warm the workers
+            t0 = time.perf_counter()
+            pool.map(_cpu_worker, [(7, c, sweeps_per_chain) for c in range(cores)])
+            wall = time.perf_counter() - t0
+    finally:
+        for v, x in saved.items():
+            if x is None:
+                os.environ.pop(v, None)
+            else:
+                os.environ[v] = x
     return cores * sweeps_per_chain / wall, wall
+
+
+def run_tau(args):
+    """Long run of the plain sweep: τ_int(E_kin) with a binning cross-check.
+
+    Prints the JSON that is committed as the workload's τ_int (both bench arms
+    run the same Markov chain algorithm, so they share it)."""
+    from kapdqmc_gb300 import Initial_s
+    from kapdqmc_gb300.sweep import Sweeper
+    model = make_model()
+    sw = Sweeper(model, NCHAINS)
+    sw.set_fields(np.stack([Initial_s(model, 5000 + c) for c in range(NCHAINS)]))
+    sw.set_rng(424242)
+    sw.init()
+    burn = 20
+    sw.sweep(burn + args.tau_run, record=True)
+    sw.synchronize()
+    ek = sw.get_obs(burn + args.tau_run)[:, burn:, 0]
+    tau = tau_int(ek)
+    # binning: τ_int ≈ var(bin means) * B / (2 var)
+    var = ek.var()
+    bins = {}
+    for B in (1, 2, 4, 8, 16):
+        T = ek.shape[1] // B
+        m = ek[:, :T * B].reshape(ek.shape[0], T, B).mean(axis=2)
+        bins[B] = float(m.var() * B / (2 * var))
+    out = {"workload": CONFIG["workload"], "chains": NCHAINS, "sweeps": args.tau_run, "burn_in": burn,
+           "observable": "kinetic energy (first measurement column)", "estimator": "Sokal window c=5",
+           "tau_int": tau, "tau_int_binning": bins, "energy_mean": float(ek.mean()),
+           "energy_err": float(ek.mean(axis=1).std() / math.sqrt(NCHAINS))}
+    print(json.dumps(out))
 
 
 def run_reference(args):
@@ -191,14 +247,14 @@ def run_reference(args):
     cs = float(np.median(vals))
     tau = args.tau_int or reference_tau_int() or 1.0
     value = cs / tau
-    sample = (f"{cores} chains (one per core) x 1 sweep each per step, numpy/scipy restatement, "
-              f"BLAS threads 1; tau_int={tau:.3g} taken from the GPU arm's estimate")
+    sample = (f"{CPU_SAMPLE}; {cores} chains x 1 sweep per step; tau_int={tau:.3g} "
+              f"(the workload's committed long-run value)")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": float(np.median(walls)) * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded HS fields and Philox proposal stream)", "config": CONFIG,
            "impl": "reference",
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": CPU_KIND, "sample": sample,
                             "chain_sweeps_per_s": cs},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -275,7 +331,10 @@ def run_gpu(args):
     roof = {"bound": "fp64", "pipe": "FP64 DFMA (CUDA cores)", "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
-            "traffic": None, "flops_per_launch": flops_per_launch,
+            "traffic": traffic_per_launch(),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean over every k_block "
+                              "launch of the same workload (profiles/k_block_tv6x6_launches.md)",
+            "flops_per_launch": flops_per_launch,
             "flops_per_chain_sweep": fl}
 
     # ---- end to end through kdq_phy_update with host buffers
@@ -319,11 +378,10 @@ def run_gpu(args):
         if not args.no_cpu and world == 1:
             cores = os.cpu_count() or 1
             cs_cpu, wall_cpu = cpu_chain_sweeps_per_s(cores)
-            out["cpu_baseline"] = {"value": cs_cpu / tau, "unit": UNIT, "cores": cores, "kind": "port",
+            out["cpu_baseline"] = {"value": cs_cpu / tau, "unit": UNIT, "cores": cores, "kind": CPU_KIND,
                                    "chain_sweeps_per_s": cs_cpu,
-                                   "sample": f"{cores} chains x 1 sweep (one chain per core) of the same "
-                                             f"workload, numpy/scipy restatement, {wall_cpu:.1f} s; "
-                                             f"tau_int from this run"}
+                                   "sample": f"{CPU_SAMPLE}; {cores} chains x 1 sweep of the same workload, "
+                                             f"{wall_cpu:.1f} s"}
         print(json.dumps(out))
     sw.close()
     if dist:
@@ -343,12 +401,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--tau-int", type=float, default=None,
                     help="τ_int used to convert chain-sweeps/s (default: the committed long-run value)")
+    ap.add_argument("--tau-run", type=int, default=0,
+                    help="long run of this many sweeps; prints the workload's τ_int JSON and exits")
     ap.add_argument("--chains", type=int, default=NCHAINS,
                     help="chains per GPU (profiling of small cases only; bench lines use 256)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    if args.impl == "reference":
+    if args.tau_run:
+        run_tau(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -103,3 +103,18 @@ def test_golden_fixture(path):
     assert sum(sw.accepts) == spec["n_accept"]
     np.testing.assert_allclose(np.array(sw.obs_rows), np.array(spec["obs"]), rtol=1e-9, atol=1e-12)
     importlib.invalidate_caches()
+
+
+def test_c_restatement_matches_numpy_oracle():
+    """The timed CPU baseline (C, dense bond GEMMs) makes the oracle's decisions."""
+    import cport_tv
+    model = cases.tv_honeycomb()
+    s = Initial_s(model, 3)
+    n = O.proposals_per_sweep(model)
+    ks, us = zip(*(philox.tape(5, 0, w, n) for w in range(2)))
+    k, u = np.concatenate(ks), np.concatenate(us)
+    ref = O.phy_update(model, s, 2, O.Tape(k, u), True)
+    s2, obs, acc = cport_tv.tv_phy_update(model, s, 2, k, u, True, log=True)
+    np.testing.assert_array_equal(acc.astype(bool), np.array(ref.accepts))
+    np.testing.assert_array_equal(s2, ref.s)
+    np.testing.assert_allclose(obs, np.array(ref.obs_rows), rtol=1e-9, atol=1e-10)
