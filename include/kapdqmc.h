@@ -120,7 +120,11 @@ int kdq_set_tape(kdq_handle* h, const uint8_t* k, const double* u, size_t n_per_
  * forward+backward sweeps with local updates and QR stabilisation, and
  * return the per-sweep measurement rows when record != 0 (tU: Ek Eu CDW0
  * CDW1 SDW0 SDW1; tV: Ek Ev R0[4] R1[4]; tUV: Ek Eu Ev CDW0 CDW1 SDW0 SDW1).
- * obs may be NULL when record == 0; otherwise obs_len must be at least
+ * record = 1 measures exactly as the reference (a copy of G wrapped slice by
+ * slice to Nt/2 for every measured slice); record = 2 gives the same
+ * estimator with the wraps folded into two products L, R kept between
+ * measurements (G0 = L G R; same observables up to rounding, far fewer
+ * GEMMs).  obs may be NULL when record == 0; otherwise obs_len must be at least
  * n_chains * sweeps * kdq_n_obs(h), filled chain-major.
  * Replaces src/tU/phy_update.jl:3-152, src/tV/phy_update.jl:1-188,
  * src/tUV/phy_update.jl:1-186 (the CSV append is left to the caller). */

@@ -27,7 +27,7 @@ struct ChainCtl {
   int drift_pos;        // drift-log cursor
   int obs_slot;         // next measurement row of this call
   int obs_cnt;          // measurements accumulated in the current sweep
-  int pad;
+  int meas_n;           // slice factors held in the fast-measurement products
   double max_drift;
   double obs_acc[KDQ_MAX_OBS];
 };
@@ -69,6 +69,12 @@ struct SweepParams {
   uint8_t* s;
   ChainCtl* ctl;
   size_t sz_NN, sz_Nn, sz_nn, sz_chainB;   // element strides per chain
+  // fast measurement (record == 2): L, R products and their factor stack
+  void* Lm;
+  void* Rm;
+  uint8_t* mstack;              // per chain: mstack_max ints (signed slices) + mstack_max field snapshots
+  size_t mstack_stride;
+  int mstack_max;
   // random stream
   uint64_t seed;
   const uint8_t* tape_k;

@@ -56,6 +56,7 @@ struct kdq_handle {
   DevBuf eK, eKinv, HalfeK, HalfeKinv, K, Pt, PtH;
   // chain buffers
   DevBuf G, W1, W2, Y, Y2, Mss, X, piv, BLs, BRs, s, ctl;
+  DevBuf Lm, Rm, mstack;   // fast-measurement products, allocated on first use
   // outputs
   DevBuf obs, acc_log, drift, tape_k, tape_u;
   // Grover-determinant workspace
@@ -146,6 +147,7 @@ __global__ void k_reset_ctl(ChainCtl* ctl, int n, int full) {
     x.idx = 1;
     x.obs_slot = 0;
     x.obs_cnt = 0;
+    x.meas_n = 0;
     for (int q = 0; q < KDQ_MAX_OBS; ++q) x.obs_acc[q] = 0.0;
   }
   x.err = 0;
@@ -550,6 +552,7 @@ int kdq_init(kdq_handle* h) {
 int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
   if (!h) return KDQ_ERR_ARG;
   if (sweeps < 0) return fail(h, KDQ_ERR_ARG, "sweeps must be >= 0");
+  if (record < 0 || record > 2) return fail(h, KDQ_ERR_ARG, "record must be 0, 1 or 2");
   if (!h->initialised) return fail(h, KDQ_ERR_STATE, "kdq_init must precede kdq_sweep");
   KDQ_CUDA(h, cudaSetDevice(h->device));
   if (h->use_tape) {
@@ -593,7 +596,21 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
     h->P.obs = h->obs.as<double>();
     h->P.obs_cap = h->obs_capacity;
   }
-  h->P.record = record ? 1 : 0;
+  if (record == 2 && !h->Lm.p) {
+    const size_t NNe = (size_t)h->Ns * h->Ns, C = h->nchains;
+    const int fmax = h->Nt / 2 + 1;
+    const size_t stride = (((size_t)fmax * (sizeof(int) + h->n_field)) + 255) & ~(size_t)255;
+    KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    KDQ_CUDA(h, h->Lm.alloc(C * NNe * h->esz));
+    KDQ_CUDA(h, h->Rm.alloc(C * NNe * h->esz));
+    KDQ_CUDA(h, h->mstack.alloc(C * stride));
+    h->P.Lm = h->Lm.p;
+    h->P.Rm = h->Rm.p;
+    h->P.mstack = h->mstack.as<uint8_t>();
+    h->P.mstack_stride = stride;
+    h->P.mstack_max = fmax;
+  }
+  h->P.record = record;
   auto t0 = std::chrono::steady_clock::now();
   for (int w = 0; w < sweeps; ++w) {
     for (int k = 1; k <= h->NN - 1; ++k) KDQ_CUDA(h, launch(h, KDQ_MODE_FWD, k));

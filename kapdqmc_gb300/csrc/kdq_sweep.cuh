@@ -97,9 +97,9 @@ struct Ctx {
 // Forward (sign=+1) / backward (sign=-1) diagonal factor of slice lt
 // (1-based) into sm.dvec, and its elementwise inverse into sm.dinv.
 template <int KIND, class T, class KT>
-__device__ void slice_diag(Ctx<KIND, T, KT>& c, int lt, int sign) {
+__device__ void slice_diag(Ctx<KIND, T, KT>& c, int lt, int sign, const uint8_t* fields = nullptr) {
   const SweepParams& P = c.P;
-  const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field;
+  const uint8_t* sl = fields ? fields : c.s + (size_t)(lt - 1) * P.n_field;
   if constexpr (KIND == KDQ_TU) {
     // D = cis(±α η_s), 1 ./ D  (src/tU/phy_update.jl:61-63,123-125)
     const cd* tab = reinterpret_cast<const cd*>(P.dtab) + (size_t)(lt - 1) * 16 + (sign > 0 ? 0 : 8);
@@ -173,10 +173,10 @@ __device__ void wrap_bwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
 // The per-bond coefficients are staged in sm.dvec / sm.dinv as (plus, minus)
 // pairs for rows (L) and columns (R).
 template <int KIND, class T, class KT>
-__device__ void tv_coeffs(Ctx<KIND, T, KT>& c, int lt, int j, int sign) {
+__device__ void tv_coeffs(Ctx<KIND, T, KT>& c, int lt, int j, int sign, const uint8_t* fields = nullptr) {
   const SweepParams& P = c.P;
   const int nb = P.Ns / 2;
-  const uint8_t* sl = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * nb;
+  const uint8_t* sl = (fields ? fields : c.s + (size_t)(lt - 1) * P.n_field) + (size_t)j * nb;
   // vtab per slice: [D_x | D_y | 1/D_x | 1/D_y] forward, then the same backward
   const double* tab = P.vtab + (size_t)(lt - 1) * 32 + (sign > 0 ? 0 : 16);
   double* L = reinterpret_cast<double*>(c.sm.dvec);
@@ -563,6 +563,9 @@ __device__ inline double re_prod(double k, double g) { return k * g; }
 __device__ inline double re_prod(double k, cd g) { return k * g.x; }
 __device__ inline double re_prod(cd k, cd g) { return k.x * g.x - k.y * g.y; }
 
+template <int KIND, class T, class KT>
+__device__ void observables(Ctx<KIND, T, KT>& c, const T* G0);
+
 // Equal-time observables at tau = Nt/2 from G at slice t0 (phy_measure):
 // wrap a copy to Nt/2, symmetrise with HalfeK, accumulate one row.
 // tU: src/tU/phy_update.jl:154-254; tV: src/tV/phy_update.jl:207-314;
@@ -601,7 +604,15 @@ __device__ void measure(Ctx<KIND, T, KT>& c, int t0) {
   }
   gemm_sq<MAXRM, T>(N, N, N, c.HalfeK, N, G0, N, W, N);
   gemm_sq<MAXRM, T>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
+  observables(c, G0);
+}
 
+// Observables of the symmetrised Green's function G0 at tau = Nt/2,
+// accumulated into the chain's current measurement row.
+template <int KIND, class T, class KT>
+__device__ void observables(Ctx<KIND, T, KT>& c, const T* G0) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns;
   double acc[KDQ_MAX_OBS];
 #pragma unroll
   for (int q = 0; q < KDQ_MAX_OBS; ++q) acc[q] = 0.0;
@@ -718,6 +729,138 @@ __device__ void measure(Ctx<KIND, T, KT>& c, int t0) {
   __syncthreads();
 }
 
+// ------------------------------------------------- measurement, fast form
+// record == 2: the same estimator as `measure`, with the wrap of the G copy
+// to Nt/2 and the HalfeK symmetrisation folded into two N x N factors,
+//   G0 = L G R,  L = HalfeK W,  R = W^-1 HalfeKinv,
+// W = B_half ... B_{t0+1} (t0 <= Nt/2) or B_{half+1}^-1 ... B_{t0}^-1 (t0 > Nt/2)
+// with the current fields.  L and R are kept between measurements as a
+// stack of slice factors, each with the fields it was built from; a new
+// measurement pops the factors whose slice or fields no longer match and
+// pushes the missing ones (one or two of each between consecutive measured
+// slices), instead of re-wrapping |t0 - Nt/2| slices.
+
+// X <- X B_lt (right = true) or B_lt X, with B the slice matrix of `fields`
+// (inv: B^-1).  W is N x N scratch.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void mul_slice(Ctx<KIND, T, KT>& c, T* X, T* W, int lt, const uint8_t* fields, bool right, bool inv) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns;
+  if constexpr (KIND == KDQ_TV) {
+    // B = V_1 ... V_z eK, V_j = UV D_j UV (2x2 blocks (lp, lm)); V_j^-1 blocks (rp, rm)
+    auto rot = [&](int j) {
+      tv_coeffs(c, lt, j, +1, fields);
+      const double* Q = reinterpret_cast<const double*>(inv ? c.sm.dinv : c.sm.dvec);
+      const int nb = N / 2;
+      for (int e = threadIdx.x; e < nb * N; e += blockDim.x) {
+        const int i = e % nb, o = e / nb;
+        const int x = P.bx[j * nb + i], y = P.by[j * nb + i];
+        const double qp = Q[2 * i], qm = Q[2 * i + 1];
+        T* px = right ? X + (size_t)x * N + o : X + x + (size_t)o * N;
+        T* py = right ? X + (size_t)y * N + o : X + y + (size_t)o * N;
+        const T vx = *px, vy = *py;
+        *px = vx * qp + vy * qm;
+        *py = vx * qm + vy * qp;
+      }
+      __syncthreads();
+    };
+    const bool k_first = right == inv;   // X eKinv ... / eK X ... come first
+    if (k_first) {
+      if (right) gemm_sq<MAXRM, T>(N, N, N, X, N, c.eKinv, N, W, N);
+      else gemm_sq<MAXRM, T>(N, N, N, c.eK, N, X, N, W, N);
+      for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = W[e];
+      __syncthreads();
+    }
+    // right: X V_1 V_2 ... (B) or X ... V_2^-1 V_1^-1 (B^-1, after eKinv)
+    // left:  V_1 V_2 ... V_z (eK X) applied innermost-first, or V_1^-1 first for B^-1
+    const bool ascending = right ? !inv : inv;
+    for (int q = 0; q < P.z; ++q) rot(ascending ? q : P.z - 1 - q);
+    if (!k_first) {
+      if (right) gemm_sq<MAXRM, T>(N, N, N, X, N, c.eK, N, W, N);
+      else gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, X, N, W, N);
+      for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = W[e];
+      __syncthreads();
+    }
+  } else {
+    slice_diag(c, lt, +1, fields);   // dvec = D, dinv = 1 ./ D
+    const T* d = inv ? c.sm.dinv : c.sm.dvec;
+    if (right && !inv) {          // X D eK
+      for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = X[e] * d[e / N];
+      __syncthreads();
+      gemm_sq<MAXRM, T>(N, N, N, X, N, c.eK, N, W, N);
+    } else if (right) {           // X eKinv D^-1
+      gemm_sq<MAXRM, T>(N, N, N, X, N, c.eKinv, N, W, N, (const T*)nullptr, d);
+    } else if (!inv) {            // D eK X
+      gemm_sq<MAXRM, T>(N, N, N, c.eK, N, X, N, W, N, d, (const T*)nullptr);
+    } else {                      // eKinv D^-1 X
+      for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = d[e % N] * X[e];
+      __syncthreads();
+      gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, X, N, W, N);
+    }
+    for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = W[e];
+    __syncthreads();
+  }
+}
+
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void measure_fast(Ctx<KIND, T, KT>& c, int t0) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, half = P.Nt / 2, nf = P.n_field;
+  T* L = static_cast<T*>(P.Lm) + (size_t)c.chain * P.sz_NN;
+  T* R = static_cast<T*>(P.Rm) + (size_t)c.chain * P.sz_NN;
+  T* W = c.W1;
+  int* fslice = reinterpret_cast<int*>(P.mstack + (size_t)c.chain * P.mstack_stride);
+  uint8_t* fsnap = P.mstack + (size_t)c.chain * P.mstack_stride + (size_t)P.mstack_max * sizeof(int);
+  const bool below = 2 * t0 <= P.Nt;     // t0 <= Nt/2: factors B_half ... B_{t0+1}
+  const int m = below ? half - t0 : t0 - half;
+  auto target = [&](int q) { return below ? half - q : half + 1 + q; };   // slice of factor q
+  auto orient = [&](int q) { return below ? +1 : -1; };
+  const int n = c.ctl->meas_n;
+  // slices carry their orientation in the sign of fslice
+  __shared__ int match;
+  int k = 0;
+  for (; k < n && k < m; ++k) {
+    if (threadIdx.x == 0) match = fslice[k] == orient(k) * target(k);
+    __syncthreads();
+    const uint8_t* cur = c.s + (size_t)(target(k) - 1) * nf;
+    const uint8_t* snap = fsnap + (size_t)k * nf;
+    int diff = 0;
+    for (int i = threadIdx.x; i < nf; i += blockDim.x) diff |= cur[i] != snap[i];
+    diff = __syncthreads_or(diff);
+    if (!match || diff) break;
+  }
+  if (k == 0) {
+    for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+      L[e] = conv<T>::from(c.HalfeK[e]);
+      R[e] = conv<T>::from(c.HalfeKinv[e]);
+    }
+    __syncthreads();
+  } else {
+    for (int q = n - 1; q >= k; --q) {   // pop: undo factor q
+      const int sl = fslice[q] > 0 ? fslice[q] : -fslice[q];
+      const bool is_B = fslice[q] > 0;
+      const uint8_t* snap = fsnap + (size_t)q * nf;
+      mul_slice<MAXRM>(c, L, W, sl, snap, true, is_B);    // L <- L F^-1
+      mul_slice<MAXRM>(c, R, W, sl, snap, false, !is_B);  // R <- F R
+    }
+  }
+  for (int q = k; q < m; ++q) {          // push factor q with the current fields
+    const int sl = target(q);
+    const bool is_B = orient(q) > 0;
+    const uint8_t* cur = c.s + (size_t)(sl - 1) * nf;
+    mul_slice<MAXRM>(c, L, W, sl, cur, true, !is_B);     // L <- L F
+    mul_slice<MAXRM>(c, R, W, sl, cur, false, is_B);     // R <- F^-1 R
+    uint8_t* snap = fsnap + (size_t)q * nf;
+    for (int i = threadIdx.x; i < nf; i += blockDim.x) snap[i] = cur[i];
+    if (threadIdx.x == 0) fslice[q] = orient(q) * sl;
+  }
+  if (threadIdx.x == 0) c.ctl->meas_n = m;
+  __syncthreads();
+  gemm_sq<MAXRM, T>(N, N, N, L, N, c.G, N, W, N);
+  gemm_sq<MAXRM, T>(N, N, N, W, N, R, N, c.W2, N);
+  observables(c, c.W2);
+}
+
 // ------------------------------------------------------------------ kernel
 // mode KDQ_MODE_INIT: block k of the initial left chain (and G at k == 1);
 // KDQ_MODE_FWD: forward slices node(k)+1 .. node(k+1), then the node;
@@ -772,7 +915,10 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
         wrap_fwd_kv<MAXRM>(c, c.G, c.W1, lt);
         update_layer(c, lt, 0, true);
       }
-      if (rec) measure<MAXRM>(c, lt);
+      if (rec) {
+        if (P.record == 2) measure_fast<MAXRM>(c, lt);
+        else measure<MAXRM>(c, lt);
+      }
     }
     node_forward<MAXRM>(c, k);
   } else {
@@ -787,10 +933,16 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
         }
         gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, c.G, N, c.W1, N);
         gemm_sq<MAXRM, T>(N, N, N, c.W1, N, c.eK, N, c.G, N);
-        if (rec) measure<MAXRM>(c, lt - 1);
+        if (rec) {
+          if (P.record == 2) measure_fast<MAXRM>(c, lt - 1);
+          else measure<MAXRM>(c, lt - 1);
+        }
       } else {
         update_layer(c, lt, 0, false);
-        if (rec) measure<MAXRM>(c, lt);
+        if (rec) {
+          if (P.record == 2) measure_fast<MAXRM>(c, lt);
+          else measure<MAXRM>(c, lt);
+        }
         wrap_bwd_kv<MAXRM>(c, c.G, c.W1, lt);
       }
     }

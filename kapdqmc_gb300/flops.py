@@ -21,7 +21,7 @@ def _mac(model, left_complex: bool, right_complex: bool) -> int:
     return 2
 
 
-def sweep_flops(model, accepted: float, record: bool, k_complex: bool = False) -> dict:
+def sweep_flops(model, accepted: float, record, k_complex: bool = False) -> dict:
     """FLOPs of one forward+backward sweep of one chain.
 
     ``accepted``: accepted proposals per chain-sweep (measured).
@@ -48,7 +48,11 @@ def sweep_flops(model, accepted: float, record: bool, k_complex: bool = False) -
     hh = 2 * (2 * N * ns * ns - 2 * ns ** 3 // 3) * (mgg // 2)   # geqrf + orgqr (mgg/2 per op pair)
     getg = (ns * ns * N + ns ** 3 // 3 + ns * ns * N + N * N * ns) * mgg
     out["stabilise"] = thin + n_cross * (hh + getg)
-    if record:
+    if record == 2:
+        # fast form: two products per measurement plus the factor pushes/pops
+        # (each a slice matrix applied to L and to R)
+        out["measure"] = (fast_factor_ops(model) * (wrap + rot) + measured_slices(model) * 2 * N ** 3 * mgg)
+    elif record:
         out["measure"] = measure_wraps(model) * (wrap + rot) + measured_slices(model) * 2 * N ** 3 * mgk
     else:
         out["measure"] = 0
@@ -87,3 +91,54 @@ def measure_wraps(model) -> int:
     for t0 in _window(model):
         n += (t0 - half) if 2 * t0 > model.Nt else (half - t0)
     return n
+
+
+def fast_factor_ops(model) -> int:
+    """Factor pushes + pops of the record == 2 measurement in one steady-state sweep.
+
+    Replays the sweep order (every slice's fields change when it is updated)
+    against the factor stack of the kernel's measure_fast."""
+    Nt, half = model.Nt, model.Nt // 2
+    NN = len(model.nodes)
+    Θidx = NN // 2 + 1
+    nodes = list(model.nodes)
+    version = [0] * (Nt + 2)
+    stack: list = []
+    ops = 0
+
+    def measure(t0):
+        nonlocal stack, ops
+        below = 2 * t0 <= Nt
+        m = half - t0 if below else t0 - half
+        target = [((half - q) if below else (half + 1 + q), 1 if below else -1) for q in range(m)]
+        k = 0
+        while k < min(len(stack), m) and stack[k] == (target[k][0], target[k][1], version[target[k][0]]):
+            k += 1
+        ops += (len(stack) - k if k else 0) + (m - k)
+        stack = [(sl, o, version[sl]) for sl, o in target]
+
+    def in_window(idx):
+        if model.kind == KIND_TU:
+            return None
+        return abs(idx - Θidx) <= 1
+
+    count_from = None
+    for sweep in range(2):
+        if sweep == 1:
+            count_from = ops
+        idx = 1
+        for lt in range(1, Nt + 1):
+            version[lt] += 1
+            on = (0 <= Θidx - idx <= 1) if model.kind == KIND_TU else abs(idx - Θidx) <= 1
+            if on:
+                measure(lt)
+            if lt in nodes:
+                idx += 1
+        for lt in range(Nt, 0, -1):
+            version[lt] += 1
+            on = (0 <= idx - Θidx <= 1) if model.kind == KIND_TU else abs(idx - Θidx) <= 1
+            if on:
+                measure(lt - 1 if model.kind == KIND_TV else lt)
+            if lt - 1 in nodes:
+                idx -= 1
+    return ops - count_from

@@ -140,11 +140,14 @@ class Sweeper:
         self._ck(self.lib.kdq_set_tape(self.h, k.ctypes.data, u.ctypes.data, k.shape[1]))
 
     # -- sweeps ------------------------------------------------------------
-    def phy_update(self, sweeps: int, record: bool = False):
-        """Init from the fields + sweeps; returns obs (nchains, sweeps, n_obs) or None."""
+    def phy_update(self, sweeps: int, record=False):
+        """Init from the fields + sweeps; returns obs (nchains, sweeps, n_obs) or None.
+
+        record: 0/False none, 1/True as the reference, 2 the fast form of the
+        same estimator (see kdq_phy_update)."""
         if record:
             obs = np.empty(self.nchains * sweeps * self.n_obs)
-            self._ck(self.lib.kdq_phy_update(self.h, sweeps, 1, obs.ctypes.data, obs.size))
+            self._ck(self.lib.kdq_phy_update(self.h, sweeps, int(record), obs.ctypes.data, obs.size))
             return obs.reshape(self.nchains, sweeps, self.n_obs)
         self._ck(self.lib.kdq_phy_update(self.h, sweeps, 0, None, 0))
         return None
@@ -152,8 +155,8 @@ class Sweeper:
     def init(self):
         self._ck(self.lib.kdq_init(self.h))
 
-    def sweep(self, sweeps: int, record: bool = False):
-        self._ck(self.lib.kdq_sweep(self.h, sweeps, int(bool(record))))
+    def sweep(self, sweeps: int, record=False):
+        self._ck(self.lib.kdq_sweep(self.h, sweeps, int(record)))
 
     def synchronize(self):
         self._ck(self.lib.kdq_synchronize(self.h))

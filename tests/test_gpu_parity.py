@@ -25,7 +25,7 @@ def _oracle(model, s, seed, chain, sweeps, record):
     return O.phy_update(model, s, sweeps, O.Tape(np.concatenate(ks), np.concatenate(us)), record)
 
 
-def _compare(model, nchains=2, sweeps=2, record=True, seed=1234):
+def _compare(model, nchains=2, sweeps=2, record=True, seed=1234, obs_tol=OBS_TOL):
     fields = np.stack([Initial_s(model, 100 + c) for c in range(nchains)])
     n = O.proposals_per_sweep(model) * sweeps
     with Sweeper(model, nchains) as sw:
@@ -47,7 +47,7 @@ def _compare(model, nchains=2, sweeps=2, record=True, seed=1234):
         if record:
             ro = np.array(ref.obs_rows)
             err = np.abs(obs[c] - ro).max() / max(1.0, np.abs(ro).max())
-            assert err < OBS_TOL, f"chain {c}: obs diff {err:.3e}\n{obs[c]}\n{ro}"
+            assert err < obs_tol, f"chain {c}: obs diff {err:.3e}\n{obs[c]}\n{ro}"
         np.testing.assert_allclose(drift[c], ref.drift, rtol=0, atol=1e-9)
     assert st["proposals"] == nchains * n
     assert st["max_drift"] < 1e-6
@@ -170,3 +170,18 @@ def test_grover_det_of_sweep_chains():
         G = [sw.green(c) for c in range(4)]
     want = [O.grover_det(G[0], G[1], index), O.grover_det(G[2], G[3], index)]
     np.testing.assert_allclose(dets, want, rtol=1e-10, atol=1e-14)
+
+
+# record = 2: the measurement wraps folded into the products L, R (reassociated
+# arithmetic, same estimator): rows agree with the reference's to 1e-8.
+FAST_TOL = 1e-8
+
+
+@pytest.mark.parametrize("make", [cases.tu_square, cases.tu_honeycomb, cases.tu_quench, cases.tv_honeycomb,
+                                  cases.tuv_honeycomb, cases.tuv_square])
+def test_fast_measurement_matches_reference_window(make):
+    _compare(make(), sweeps=3, record=2, obs_tol=FAST_TOL)
+
+
+def test_fast_measurement_c1():
+    _compare(cases.c1(), nchains=1, sweeps=2, record=2, obs_tol=FAST_TOL)
