@@ -333,13 +333,7 @@ def run_gpu(args):
     ek = obs[:, args.warmup:, 0]
     tau_live = tau_int(ek)
     tau = args.tau_int or reference_tau_int() or tau_live
-    t_max = ms
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    chain_sweeps = NCHAINS * args.steps * world
-    cs_per_s = chain_sweeps / (t_max * 1e-3)
+    cs_per_s, t_max = replica_throughput(dist, ms, NCHAINS * args.steps, dev)
     value = cs_per_s / tau
 
     # ---- roofline of the sweep kernel (the only kernel of the timed region)
@@ -375,11 +369,9 @@ def run_gpu(args):
         cur = sw.get_fields()
         e2e_rows.append(o[:, 0, 0])
     wall = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([wall], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall = float(t.item())
-    e2e_value = NCHAINS * world * e2e_steps / wall / tau
+    e2e_cs, _ = replica_throughput(dist, wall * 1e3, NCHAINS * e2e_steps, dev)
+    wall = dist_max(dist, wall, dev)
+    e2e_value = e2e_cs / tau
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -409,6 +401,23 @@ def run_gpu(args):
     sw.close()
     if dist:
         dist.destroy_process_group()
+
+
+def dist_max(dist, value: float, device=None) -> float:
+    """Max of a per-rank value over all ranks (identity without a process group)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(dist, ms_local: float, units_local: int, device=None):
+    """Whole-job units/s of independent replicas: units of all ranks over the slowest rank's time."""
+    world = dist.get_world_size() if dist is not None else 1
+    ms = dist_max(dist, ms_local, device)
+    return units_local * world / (ms * 1e-3), ms
 
 
 def model_nobs(sw):

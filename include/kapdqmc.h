@@ -192,6 +192,12 @@ int kdq_grover_det_chains(kdq_handle* h, const int32_t* index, int32_t nA, doubl
 int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32_t npairs,
                            const int32_t* index, int32_t nA, double* det, void* stream);
 
+/* Replay each sweep's 2 (n_nodes-1) block launches from a captured CUDA
+ * graph (default on) or launch them one by one (enable = 0).  The graph is
+ * re-captured whenever the launch parameters change.  No counterpart in the
+ * reference (a launch-sequencing choice of this implementation). */
+int kdq_set_graphs(kdq_handle* h, int32_t enable);
+
 /* CUDA stream (cudaStream_t) of the handle, for event timing by callers. */
 void* kdq_stream(kdq_handle* h);
 

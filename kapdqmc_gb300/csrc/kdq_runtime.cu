@@ -70,6 +70,15 @@ struct kdq_handle {
   size_t tape_len = 0;
   double last_seconds = 0.0;
   bool initialised = false;
+  int drift_rows = 0;           // drift entries per chain written by the last call
+  // one sweep (2 (NN-1) block launches) captured as a CUDA graph, replayed
+  // while the launch parameters stay the same
+  bool use_graphs = true;
+  cudaGraphExec_t graph = nullptr;
+  SweepParams graph_P{};
+  ~kdq_handle() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
 };
 
 namespace {
@@ -567,14 +576,15 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
   k_reset_ctl<<<(h->nchains + 127) / 128, 128, 0, h->stream>>>(h->ctl.as<ChainCtl>(), h->nchains, 0);
   KDQ_CUDA(h, cudaGetLastError());
   // drift log for this call
-  const int dcap = sweeps * 2 * (h->NN - 1);
-  if ((size_t)dcap * h->nchains * sizeof(double) > h->drift.bytes) {
+  const int dneed = sweeps * 2 * (h->NN - 1);
+  if (dneed > h->drift_cap) {   // capacity per chain only grows, so graphs stay valid
     KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
-    KDQ_CUDA(h, h->drift.alloc((size_t)dcap * h->nchains * sizeof(double)));
+    KDQ_CUDA(h, h->drift.alloc((size_t)dneed * h->nchains * sizeof(double)));
+    h->drift_cap = dneed;
   }
-  h->drift_cap = dcap;
+  h->drift_rows = dneed;
   h->P.drift = h->drift.as<double>();
-  h->P.drift_cap = dcap;
+  h->P.drift_cap = h->drift_cap;
   // observables: rows for every sweep recorded since kdq_init (chain-major,
   // obs_cap rows per chain); grown by copying the old rows over
   if (record) {
@@ -612,9 +622,34 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
   }
   h->P.record = record;
   auto t0 = std::chrono::steady_clock::now();
-  for (int w = 0; w < sweeps; ++w) {
-    for (int k = 1; k <= h->NN - 1; ++k) KDQ_CUDA(h, launch(h, KDQ_MODE_FWD, k));
-    for (int k = h->NN - 1; k >= 1; --k) KDQ_CUDA(h, launch(h, KDQ_MODE_BWD, k));
+  if (h->use_graphs && sweeps > 0) {
+    if (!h->graph || std::memcmp(&h->graph_P, &h->P, sizeof(SweepParams)) != 0) {
+      if (h->graph) {
+        KDQ_CUDA(h, cudaGraphExecDestroy(h->graph));
+        h->graph = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      KDQ_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t ce = cudaSuccess;
+      for (int k = 1; k <= h->NN - 1 && ce == cudaSuccess; ++k) ce = launch(h, KDQ_MODE_FWD, k);
+      for (int k = h->NN - 1; k >= 1 && ce == cudaSuccess; --k) ce = launch(h, KDQ_MODE_BWD, k);
+      cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+      if (ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(h, ce, "sweep capture");
+      }
+      KDQ_CUDA(h, ee);
+      cudaError_t ie = cudaGraphInstantiate(&h->graph, g, 0);
+      cudaGraphDestroy(g);
+      KDQ_CUDA(h, ie);
+      h->graph_P = h->P;
+    }
+    for (int w = 0; w < sweeps; ++w) KDQ_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+  } else {
+    for (int w = 0; w < sweeps; ++w) {
+      for (int k = 1; k <= h->NN - 1; ++k) KDQ_CUDA(h, launch(h, KDQ_MODE_FWD, k));
+      for (int k = h->NN - 1; k >= 1; --k) KDQ_CUDA(h, launch(h, KDQ_MODE_BWD, k));
+    }
   }
   if (record) h->obs_rows += sweeps;
   h->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -682,11 +717,20 @@ int kdq_get_green(kdq_handle* h, int32_t chain, double* G, size_t len) {
 
 int kdq_get_drift(kdq_handle* h, double* drift, size_t len) {
   if (!h || !drift) return fail(h, KDQ_ERR_ARG, "NULL argument");
-  const size_t n = (size_t)h->drift_cap * h->nchains;
+  const size_t n = (size_t)h->drift_rows * h->nchains;
   if (len != n) return fail(h, KDQ_ERR_ARG, "drift buffer must hold " + std::to_string(n) + " doubles");
   KDQ_CUDA(h, cudaSetDevice(h->device));
   KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
-  if (n) KDQ_CUDA(h, cudaMemcpy(drift, h->drift.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (n)
+    KDQ_CUDA(h, cudaMemcpy2D(drift, (size_t)h->drift_rows * sizeof(double), h->drift.p,
+                             (size_t)h->drift_cap * sizeof(double), (size_t)h->drift_rows * sizeof(double),
+                             h->nchains, cudaMemcpyDeviceToHost));
+  return KDQ_OK;
+}
+
+int kdq_set_graphs(kdq_handle* h, int32_t enable) {
+  if (!h) return KDQ_ERR_ARG;
+  h->use_graphs = enable != 0;
   return KDQ_OK;
 }
 

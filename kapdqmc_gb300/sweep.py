@@ -166,6 +166,10 @@ class Sweeper:
         self._ck(self.lib.kdq_get_obs(self.h, obs.ctypes.data, obs.size))
         return obs.reshape(self.nchains, rows, self.n_obs)
 
+    def set_graphs(self, enable: bool):
+        """Replay sweeps from a captured CUDA graph (default) or launch block by block."""
+        self._ck(self.lib.kdq_set_graphs(self.h, int(bool(enable))))
+
     @property
     def stream(self) -> int:
         return self.lib.kdq_stream(self.h) or 0

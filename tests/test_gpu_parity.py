@@ -198,3 +198,20 @@ def test_fast_measurement_c1():
 @pytest.mark.parametrize("name", ["c2", "c3", "c4", "c5"])
 def test_config_sizes_one_sweep(name):
     _compare(getattr(cases, name)(), nchains=1, sweeps=1, record=2, obs_tol=FAST_TOL)
+
+
+def test_graph_replay_equals_direct_launches():
+    model = cases.tv_honeycomb()
+    s0 = np.stack([Initial_s(model, 70 + c) for c in range(3)])
+    out = []
+    for graphs in (True, False):
+        with Sweeper(model, 3) as sw:
+            sw.set_graphs(graphs)
+            sw.set_fields(s0)
+            sw.set_rng(9)
+            o = sw.phy_update(3, 2)
+            out.append((o, sw.get_fields(), sw.green(1), sw.drift(3)))
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][2], out[1][2])
+    np.testing.assert_array_equal(out[0][3], out[1][3])
