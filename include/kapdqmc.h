@@ -35,6 +35,8 @@ enum {
 
 enum { KDQ_TU = 0, KDQ_TV = 1, KDQ_TUV = 2 };
 
+enum { KDQ_PREC_FP64 = 0, KDQ_PREC_MIXED = 1 };
+
 enum { KDQ_SQUARE45 = 0, KDQ_SQUARE90 = 1, KDQ_HONEYCOMB120 = 2, KDQ_HONEYCOMB60 = 3 };
 
 /* Model description: the fields of tU_Hubbard_Para_ / tV_Hubbard_Para_ /
@@ -191,6 +193,19 @@ int kdq_grover_det_chains(kdq_handle* h, const int32_t* index, int32_t nA, doubl
  * Errors are reported through kdq_last_error(NULL). */
 int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32_t npairs,
                            const int32_t* index, int32_t nA, double* det, void* stream);
+
+/* Arithmetic of the sweep.  KDQ_PREC_FP64 (default): everything in FP64, the
+ * reference's arithmetic.  KDQ_PREC_MIXED: the slice wraps, the block
+ * products of the stabilisation chain, the measurement products and the
+ * rank-k updates of G run in FP32 on the FP32 pipe (G is held in FP32),
+ * while the acceptance ratios, the Householder QR, the LU and the recompute
+ * of G at every node stay FP64; kdq_get_drift then reports
+ * ||G_FP32-wrap - G_FP64-recompute||_F / ||G||_F.  Only the complex sweeps
+ * (t-U, t-UV with U > 0) accept it: their HS factors cis(alpha eta) are
+ * unitary, while the real factors exp(+-alpha eta) of t-V and real t-UV
+ * amplify FP32 rounding in the wraps (KDQ_ERR_ARG).  No counterpart in the
+ * reference (which is FP64 only).  Call before kdq_init / kdq_phy_update. */
+int kdq_set_precision(kdq_handle* h, int32_t mode);
 
 /* Replay each sweep's 2 (n_nodes-1) block launches from a captured CUDA
  * graph (default on) or launch them one by one (enable = 0).  The graph is

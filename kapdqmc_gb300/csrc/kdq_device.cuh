@@ -42,15 +42,68 @@ __device__ inline double abs2(double a) { return a * a; }
 __device__ inline bool finite(cd a) { return isfinite(a.x) && isfinite(a.y); }
 __device__ inline bool finite(double a) { return isfinite(a); }
 
+// complex float (working precision of the mixed-precision sweep)
+struct cf {
+  float x, y;
+};
+__device__ inline cf operator+(cf a, cf b) { return {a.x + b.x, a.y + b.y}; }
+__device__ inline cf operator-(cf a, cf b) { return {a.x - b.x, a.y - b.y}; }
+__device__ inline cf operator-(cf a) { return {-a.x, -a.y}; }
+__device__ inline cf operator*(cf a, cf b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ inline cf operator*(cf a, float b) { return {a.x * b, a.y * b}; }
+__device__ inline cf operator*(float a, cf b) { return {a * b.x, a * b.y}; }
+__device__ inline cf operator*(cf a, double b) { return {a.x * (float)b, a.y * (float)b}; }
+__device__ inline cf conjg(cf a) { return {a.x, -a.y}; }
+__device__ inline float conjg(float a) { return a; }
+__device__ inline float re(cf a) { return a.x; }
+__device__ inline float re(float a) { return a; }
+__device__ inline double abs2(cf a) { return (double)a.x * a.x + (double)a.y * a.y; }
+__device__ inline double abs2(float a) { return (double)a * a; }
+
+// conversions between the FP64 and the working types
+template <class To> struct cvt_t;
+template <> struct cvt_t<double> {
+  __device__ static double f(double v) { return v; }
+  __device__ static double f(float v) { return v; }
+};
+template <> struct cvt_t<float> {
+  __device__ static float f(double v) { return (float)v; }
+  __device__ static float f(float v) { return v; }
+};
+template <> struct cvt_t<cd> {
+  __device__ static cd f(cd v) { return v; }
+  __device__ static cd f(cf v) { return {v.x, v.y}; }
+  __device__ static cd f(double v) { return {v, 0.0}; }
+  __device__ static cd f(float v) { return {v, 0.0}; }
+};
+template <> struct cvt_t<cf> {
+  __device__ static cf f(cf v) { return v; }
+  __device__ static cf f(cd v) { return {(float)v.x, (float)v.y}; }
+  __device__ static cf f(double v) { return {(float)v, 0.0f}; }
+  __device__ static cf f(float v) { return {v, 0.0f}; }
+};
+template <class To, class From> __device__ inline To cvt(From v) { return cvt_t<To>::f(v); }
+
+// the reduced-precision type of an FP64 type
+template <class T> struct low_t;
+template <> struct low_t<double> { using type = float; };
+template <> struct low_t<cd> { using type = cf; };
+
 template <class T> __device__ inline T zero();
 template <> __device__ inline double zero<double>() { return 0.0; }
 template <> __device__ inline cd zero<cd>() { return {0.0, 0.0}; }
+template <> __device__ inline float zero<float>() { return 0.0f; }
+template <> __device__ inline cf zero<cf>() { return {0.0f, 0.0f}; }
 template <class T> __device__ inline T one();
 template <> __device__ inline double one<double>() { return 1.0; }
 template <> __device__ inline cd one<cd>() { return {1.0, 0.0}; }
+template <> __device__ inline float one<float>() { return 1.0f; }
+template <> __device__ inline cf one<cf>() { return {1.0f, 0.0f}; }
 template <class T> __device__ inline T from_real(double v);
 template <> __device__ inline double from_real<double>(double v) { return v; }
 template <> __device__ inline cd from_real<cd>(double v) { return {v, 0.0}; }
+template <> __device__ inline float from_real<float>(double v) { return (float)v; }
+template <> __device__ inline cf from_real<cf>(double v) { return {(float)v, 0.0f}; }
 
 // acc += a * b for every mix of real and complex operands
 __device__ inline void madd(double& acc, double a, double b) { acc = fma(a, b, acc); }
@@ -61,6 +114,16 @@ __device__ inline void madd(cd& acc, cd a, cd b) {
   acc.x = fma(-a.y, b.y, acc.x);
   acc.y = fma(a.x, b.y, acc.y);
   acc.y = fma(a.y, b.x, acc.y);
+}
+
+__device__ inline void madd(float& acc, float a, float b) { acc = fmaf(a, b, acc); }
+__device__ inline void madd(cf& acc, cf a, float b) { acc.x = fmaf(a.x, b, acc.x); acc.y = fmaf(a.y, b, acc.y); }
+__device__ inline void madd(cf& acc, float a, cf b) { acc.x = fmaf(a, b.x, acc.x); acc.y = fmaf(a, b.y, acc.y); }
+__device__ inline void madd(cf& acc, cf a, cf b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.x, b.y, acc.y);
+  acc.y = fmaf(a.y, b.x, acc.y);
 }
 
 template <class T> struct conv;
@@ -79,6 +142,12 @@ __device__ inline double warp_sum(double v) {
   return v;
 }
 __device__ inline cd warp_sum(cd v) { return {warp_sum(v.x), warp_sum(v.y)}; }
+__device__ inline float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ inline cf warp_sum(cf v) { return {warp_sum(v.x), warp_sum(v.y)}; }
 
 // Block-wide sum; `red` is shared scratch of >= 32 doubles.  All threads
 // receive the result.
@@ -210,7 +279,7 @@ __device__ void bgemm_t(int M, int N, int K, const TA* __restrict__ A, int lda,
 // 1958; the LAPACK ?geqrf + ?orgqr pair restated with Hermitian reflectors).
 // Scratch: wn (n doubles: 2/(w^H w)), red (>= 32 doubles) in shared memory.
 template <class T>
-__device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red, T* w0) {
+__device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   for (int j = 0; j < n; ++j) {
@@ -227,7 +296,6 @@ __device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red,
       double ww = 2.0 * nrm * (nrm + aa);     // w^H w
       wn[j] = ww > 0.0 ? 2.0 / ww : 0.0;
       x[j] = wj;
-      *w0 = wj;
     }
     __syncthreads();
     // trailing columns c > j: A[:,c] -= (2/ww) w (w^H A[:,c])

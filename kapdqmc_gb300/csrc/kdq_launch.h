@@ -13,6 +13,13 @@ cudaError_t launch_tv(const SweepParams& P, int mode, int k, int maxrm, int ncha
                       cudaStream_t st);
 cudaError_t launch_tuv(const SweepParams& P, int mode, int k, int maxrm, bool g_complex,
                        int nchains, size_t dyn, cudaStream_t st);
+// the same with FP32 working precision (mixed-precision sweep)
+cudaError_t launch_tu_mixed(const SweepParams& P, int mode, int k, int maxrm, bool k_complex,
+                            int nchains, size_t dyn, cudaStream_t st);
+cudaError_t launch_tv_mixed(const SweepParams& P, int mode, int k, int maxrm, int nchains, size_t dyn,
+                            cudaStream_t st);
+cudaError_t launch_tuv_mixed(const SweepParams& P, int mode, int k, int maxrm, bool g_complex,
+                             int nchains, size_t dyn, cudaStream_t st);
 // Grover determinants of npairs replica pairs (matrices 2p, 2p+1 of G).
 // scratch: npairs * 3 * nA^2 elements of the G type; pivs: npairs * nA.
 cudaError_t launch_grover(const void* G, int Ns, bool g_complex, const int* index, int nA, int npairs,

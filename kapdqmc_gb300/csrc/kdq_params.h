@@ -49,18 +49,22 @@ struct SweepParams {
   const int* bx;                // 0-based bond ends
   const int* by;
   const int* site_bonds;        // tUV: per site, bond*2 + role (0 first, 1 second), -1 padded
-  const void* eK;
+  const void* eK;               // eK, eKinv, HalfeK, HalfeKinv in the working precision
   const void* eKinv;
   const void* HalfeK;
   const void* HalfeKinv;
-  const void* K;
+  const void* K;                // FP64
   const void* Pt;
-  // chain state (chain-major)
+  // chain state (chain-major); G, W1, W2, Yw, Y2w, Lm, Rm are in the working
+  // precision, the rest FP64 (in plain mode Yw, Y2w alias Y, Y2 and Gd aliases W1)
   void* G;
   void* W1;
   void* W2;
   void* Y;
   void* Y2;
+  void* Yw;
+  void* Y2w;
+  void* Gd;
   void* Mss;
   void* X;
   void* BLs_;

@@ -57,6 +57,10 @@ struct kdq_handle {
   // chain buffers
   DevBuf G, W1, W2, Y, Y2, Mss, X, piv, BLs, BRs, s, ctl;
   DevBuf Lm, Rm, mstack;   // fast-measurement products, allocated on first use
+  // mixed precision: FP32 working buffers and kinetic matrices, FP64 recompute product
+  int precision = KDQ_PREC_FP64;
+  size_t esz_w = 16;       // bytes per working-precision G element
+  DevBuf Yw, Y2w, Gd, eKw, eKinvw, HalfeKw, HalfeKinvw;
   // outputs
   DevBuf obs, acc_log, drift, tape_k, tape_u;
   // Grover-determinant workspace
@@ -124,6 +128,16 @@ cudaError_t upload_mat(DevBuf& b, const double* src, size_t n, bool cplx_in, boo
 
 // Launch one stabilisation block for all chains.
 cudaError_t launch(kdq_handle* h, int mode, int k) {
+  if (h->precision == KDQ_PREC_MIXED) {
+    switch (h->kind) {
+      case KDQ_TU:
+        return kdq::launch_tu_mixed(h->P, mode, k, h->maxrm, h->kc, h->nchains, h->dyn, h->stream);
+      case KDQ_TV:
+        return kdq::launch_tv_mixed(h->P, mode, k, h->maxrm, h->nchains, h->dyn, h->stream);
+      default:
+        return kdq::launch_tuv_mixed(h->P, mode, k, h->maxrm, h->gc, h->nchains, h->dyn, h->stream);
+    }
+  }
   switch (h->kind) {
     case KDQ_TU:
       return kdq::launch_tu(h->P, mode, k, h->maxrm, h->kc, h->nchains, h->dyn, h->stream);
@@ -146,6 +160,11 @@ __global__ void k_seed_chains(void* BRs, void* BLs, const void* Pt, const void* 
     br[i] = pt[i];
     bl[i] = ph[i];
   }
+}
+
+__global__ void k_to_float(const double* src, float* dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
 }
 
 __global__ void k_reset_ctl(ChainCtl* ctl, int n, int full) {
@@ -265,6 +284,7 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
   h->gc = m->g_complex != 0;
   h->kc = m->k_complex != 0;
   h->esz = h->gc ? 16 : 8;
+  h->esz_w = h->esz;
   h->n_field = m->kind == KDQ_TU ? m->Ns : (m->kind == KDQ_TV ? (m->Ns / 2) * h->z : m->Ns * h->z);
   h->n_obs = m->kind == KDQ_TU ? 6 : (m->kind == KDQ_TV ? 10 : 7);
   h->maxrm = m->Ns <= 32 ? 1 : (m->Ns <= 96 ? 3 : 6);
@@ -448,6 +468,7 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
   P.eK = h->eK.p; P.eKinv = h->eKinv.p; P.HalfeK = h->HalfeK.p; P.HalfeKinv = h->HalfeKinv.p;
   P.K = h->K.p; P.Pt = h->Pt.p;
   P.G = h->G.p; P.W1 = h->W1.p; P.W2 = h->W2.p; P.Y = h->Y.p; P.Y2 = h->Y2.p; P.Mss = h->Mss.p;
+  P.Yw = h->Y.p; P.Y2w = h->Y2.p; P.Gd = h->W1.p;
   P.X = h->X.p; P.BLs_ = h->BLs.p; P.BRs_ = h->BRs.p; P.piv = h->piv.as<int>();
   P.s = h->s.as<uint8_t>(); P.ctl = h->ctl.as<ChainCtl>();
   P.sz_NN = NNe; P.sz_Nn = (size_t)N * ns; P.sz_nn = (size_t)ns * ns; P.sz_chainB = chainB;
@@ -611,8 +632,8 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
     const int fmax = h->Nt / 2 + 1;
     const size_t stride = (((size_t)fmax * (sizeof(int) + h->n_field)) + 255) & ~(size_t)255;
     KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
-    KDQ_CUDA(h, h->Lm.alloc(C * NNe * h->esz));
-    KDQ_CUDA(h, h->Rm.alloc(C * NNe * h->esz));
+    KDQ_CUDA(h, h->Lm.alloc(C * NNe * h->esz_w));
+    KDQ_CUDA(h, h->Rm.alloc(C * NNe * h->esz_w));
     KDQ_CUDA(h, h->mstack.alloc(C * stride));
     h->P.Lm = h->Lm.p;
     h->P.Rm = h->Rm.p;
@@ -710,8 +731,14 @@ int kdq_get_green(kdq_handle* h, int32_t chain, double* G, size_t len) {
   if (len != n) return fail(h, KDQ_ERR_ARG, "G buffer must hold " + std::to_string(n) + " doubles");
   KDQ_CUDA(h, cudaSetDevice(h->device));
   KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
-  KDQ_CUDA(h, cudaMemcpy(G, static_cast<uint8_t*>(h->G.p) + (size_t)chain * h->Ns * h->Ns * h->esz,
-                         n * sizeof(double), cudaMemcpyDeviceToHost));
+  const uint8_t* src = static_cast<uint8_t*>(h->G.p) + (size_t)chain * h->Ns * h->Ns * h->esz_w;
+  if (h->esz_w == h->esz) {
+    KDQ_CUDA(h, cudaMemcpy(G, src, n * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {   // working precision is FP32
+    std::vector<float> f(n);
+    KDQ_CUDA(h, cudaMemcpy(f.data(), src, n * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) G[i] = f[i];
+  }
   return KDQ_OK;
 }
 
@@ -725,6 +752,69 @@ int kdq_get_drift(kdq_handle* h, double* drift, size_t len) {
     KDQ_CUDA(h, cudaMemcpy2D(drift, (size_t)h->drift_rows * sizeof(double), h->drift.p,
                              (size_t)h->drift_cap * sizeof(double), (size_t)h->drift_rows * sizeof(double),
                              h->nchains, cudaMemcpyDeviceToHost));
+  return KDQ_OK;
+}
+
+int kdq_set_precision(kdq_handle* h, int32_t mode) {
+  if (!h) return KDQ_ERR_ARG;
+  if (mode != KDQ_PREC_FP64 && mode != KDQ_PREC_MIXED) return fail(h, KDQ_ERR_ARG, "unknown precision mode");
+  if (mode == KDQ_PREC_MIXED && !h->gc)
+    return fail(h, KDQ_ERR_ARG,
+                "mixed precision needs the unitary HS factors of the complex sweeps (t-U, t-UV with U > 0); "
+                "the real HS factors exp(+-alpha eta) of t-V and real t-UV amplify FP32 rounding in the "
+                "wraps by the block's condition number (FP64 drift at n_wrap = 10 is already ~1e-6)");
+  if (mode == h->precision) return KDQ_OK;
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  const size_t C = h->nchains, NNe = (size_t)h->Ns * h->Ns, Nn = (size_t)h->Ns * h->ns;
+  h->esz_w = mode == KDQ_PREC_MIXED ? h->esz / 2 : h->esz;
+  KDQ_CUDA(h, h->G.alloc(C * NNe * h->esz_w));
+  KDQ_CUDA(h, cudaMemset(h->G.p, 0, C * NNe * h->esz_w));
+  KDQ_CUDA(h, h->W1.alloc(C * NNe * h->esz_w));
+  KDQ_CUDA(h, h->W2.alloc(C * NNe * h->esz_w));
+  h->Lm.alloc(0);
+  h->Rm.alloc(0);
+  h->mstack.alloc(0);
+  h->P.Lm = h->P.Rm = nullptr;
+  h->P.mstack = nullptr;
+  SweepParams& P = h->P;
+  P.G = h->G.p;
+  P.W1 = h->W1.p;
+  P.W2 = h->W2.p;
+  if (mode == KDQ_PREC_MIXED) {
+    KDQ_CUDA(h, h->Yw.alloc(C * Nn * h->esz_w));
+    KDQ_CUDA(h, h->Y2w.alloc(C * Nn * h->esz_w));
+    KDQ_CUDA(h, h->Gd.alloc(C * NNe * h->esz));
+    const size_t kn = NNe * (h->kc ? 2 : 1);   // doubles per kinetic matrix
+    DevBuf* dst[4] = {&h->eKw, &h->eKinvw, &h->HalfeKw, &h->HalfeKinvw};
+    DevBuf* src[4] = {&h->eK, &h->eKinv, &h->HalfeK, &h->HalfeKinv};
+    for (int q = 0; q < 4; ++q) {
+      KDQ_CUDA(h, dst[q]->alloc(kn * sizeof(float)));
+      k_to_float<<<64, 256, 0, h->stream>>>(src[q]->as<double>(), dst[q]->as<float>(), kn);
+      KDQ_CUDA(h, cudaGetLastError());
+    }
+    P.Yw = h->Yw.p;
+    P.Y2w = h->Y2w.p;
+    P.Gd = h->Gd.p;
+    P.eK = h->eKw.p;
+    P.eKinv = h->eKinvw.p;
+    P.HalfeK = h->HalfeKw.p;
+    P.HalfeKinv = h->HalfeKinvw.p;
+  } else {
+    h->Yw.alloc(0);
+    h->Y2w.alloc(0);
+    h->Gd.alloc(0);
+    P.Yw = h->Y.p;
+    P.Y2w = h->Y2.p;
+    P.Gd = h->W1.p;
+    P.eK = h->eK.p;
+    P.eKinv = h->eKinv.p;
+    P.HalfeK = h->HalfeK.p;
+    P.HalfeKinv = h->HalfeKinv.p;
+  }
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->precision = mode;
+  h->initialised = false;
   return KDQ_OK;
 }
 

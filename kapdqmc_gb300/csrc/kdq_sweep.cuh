@@ -2,13 +2,22 @@
 // block.  A launch runs the block's time slices (wrap, local updates,
 // optional measurement) and then the QR-stabilised recompute of G at the
 // block's closing node, so a full sweep is 2*(NN-1) launches of the same
-// kernel (NN = number of nodes).  All arithmetic is FP64 (complex128 or
-// float64, as the model's sweep requires).
+// kernel (NN = number of nodes).
+//
+// Two precisions.  T / KT are the FP64 types of the sweep (complex128 or
+// float64 for G, float64 or complex128 for the kinetic matrices); TW / KW are
+// the working types of the bulk products (slice wraps, thin B-products,
+// measurement products) and of the rank-k updates.  Plain mode: TW = T.
+// Mixed mode: TW = FP32 (float / complex float) on the CUDA cores' FP32
+// pipe, while the acceptance ratios, the Householder QR, the LU and the G
+// recompute at every node stay FP64 (T).
 //
 // Reference (KAPDQMC): src/tU/phy_update.jl:3-267, src/tU/GreenMatrix.jl,
 // src/tV/phy_update.jl:1-314, src/tV/GreenMatrix.jl,
 // src/tUV/phy_update.jl:1-355, src/tUV/GreenMatrix.jl, src/public/Gupdate.jl.
 #pragma once
+#include <type_traits>
+
 #include "kdq_device.cuh"
 #include "kdq_params.h"
 
@@ -40,6 +49,8 @@ template <class T> struct Tiles<1, T> { static constexpr int SM = 1, SN = 4, TM 
 template <> struct Tiles<3, double> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 4; };
 template <> struct Tiles<3, cd> { static constexpr int SM = 2, SN = 8, TM = 2, TN = 4; };
 template <class T> struct Tiles<6, T> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 6; };
+template <> struct Tiles<3, float> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 4; };
+template <> struct Tiles<3, cf> { static constexpr int SM = 2, SN = 8, TM = 2, TN = 4; };
 
 template <int MAXRM, class T, class TA, class TB, class TC, class TS = double>
 __device__ inline void gemm_sq(int M, int N, int K, const TA* A, int lda, const TB* B, int ldb, TC* C,
@@ -52,12 +63,12 @@ __device__ inline void gemm_thin(int M, int N, int K, const TA* A, int lda, cons
   bgemm_t<Tiles<MAXRM, T>::TM, Tiles<MAXRM, T>::TN>(M, N, K, A, lda, B, ldb, C, ldc, rs, cs);
 }
 
-// Per-CTA shared scratch (static part; the tape slice is dynamic).
+// Per-CTA shared scratch (static part; the tape slice is dynamic); T is the
+// working type.
 template <class T>
 struct Smem {
   double red[32];
   double wn[KDQ_MAX_NS / 2];
-  T w0;
   T dvec[KDQ_MAX_NS];   // row scaling of the current slice
   T dinv[KDQ_MAX_NS];   // column scaling
   T ucol[2][KDQ_MAX_NS];
@@ -68,36 +79,38 @@ struct Smem {
   int bad;
 };
 
-template <int KIND, class T, class KT>
+template <int KIND, class T, class KT, class TW, class KW>
 struct Ctx {
   const SweepParams& P;
-  Smem<T>& sm;
+  Smem<TW>& sm;
   uint8_t* tk;     // tape slice: choice index
   double* tu;      // tape slice: uniform
   int chain;
   ChainCtl* ctl;
-  T* G;
-  T* W1;
-  T* W2;
-  T* Y;
+  TW* G;           // equal-time Green's function, working precision
+  TW* W1;          // N x N work
+  TW* W2;          // N x N work (measurement)
+  TW* Yw;          // thin factors in working precision (N x ns)
+  TW* Y2w;
+  T* Y;            // thin factors in FP64 (alias Yw, Y2w in plain mode)
   T* Y2;
+  T* Gd;           // N x N FP64 recompute product (alias W1 in plain mode)
   T* Mss;
   T* X;
   int* piv;
   uint8_t* s;      // this chain's field, Nt x n_field
-  const KT* eK;
-  const KT* eKinv;
-  const KT* HalfeK;
-  const KT* HalfeKinv;
-  const KT* Kmat;
-  const T* Pt;
+  const KW* eK;    // kinetic matrices in working precision
+  const KW* eKinv;
+  const KW* HalfeK;
+  const KW* HalfeKinv;
+  const KT* Kmat;  // hopping matrix (observables, FP64)
 };
 
 // ---------------------------------------------------------------- tables
 // Forward (sign=+1) / backward (sign=-1) diagonal factor of slice lt
 // (1-based) into sm.dvec, and its elementwise inverse into sm.dinv.
-template <int KIND, class T, class KT>
-__device__ void slice_diag(Ctx<KIND, T, KT>& c, int lt, int sign, const uint8_t* fields = nullptr) {
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void slice_diag(Ctx<KIND, T, KT, TW, KW>& c, int lt, int sign, const uint8_t* fields = nullptr) {
   const SweepParams& P = c.P;
   const uint8_t* sl = fields ? fields : c.s + (size_t)(lt - 1) * P.n_field;
   if constexpr (KIND == KDQ_TU) {
@@ -105,8 +118,8 @@ __device__ void slice_diag(Ctx<KIND, T, KT>& c, int lt, int sign, const uint8_t*
     const cd* tab = reinterpret_cast<const cd*>(P.dtab) + (size_t)(lt - 1) * 16 + (sign > 0 ? 0 : 8);
     for (int i = threadIdx.x; i < P.Ns; i += blockDim.x) {
       const int v = sl[i] - 1;
-      c.sm.dvec[i] = tab[v];
-      c.sm.dinv[i] = tab[4 + v];
+      c.sm.dvec[i] = cvt<TW>(tab[v]);
+      c.sm.dinv[i] = cvt<TW>(tab[4 + v]);
     }
   } else if constexpr (KIND == KDQ_TUV) {
     // phase per site: Σ η over bonds starting at x + a Σ η over bonds ending
@@ -132,8 +145,8 @@ __device__ void slice_diag(Ctx<KIND, T, KT>& c, int lt, int sign, const uint8_t*
         d = dd;
         di = 1.0 / dd;
       }
-      c.sm.dvec[x] = d;
-      c.sm.dinv[x] = di;
+      c.sm.dvec[x] = cvt<TW>(d);
+      c.sm.dinv[x] = cvt<TW>(di);
     }
   }
   __syncthreads();
@@ -142,17 +155,17 @@ __device__ void slice_diag(Ctx<KIND, T, KT>& c, int lt, int sign, const uint8_t*
 // ------------------------------------------------------------------ wraps
 // G <- B_lt G B_lt^{-1}, B = D eK (tU, tUV): WrapKV!("Forward","B"),
 // src/tU/GreenMatrix.jl:64-69.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ void wrap_fwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void wrap_fwd_kv(Ctx<KIND, T, KT, TW, KW>& c, TW* G, TW* W, int lt) {
   const int N = c.P.Ns;
   slice_diag(c, lt, +1);
-  gemm_sq<MAXRM, T>(N, N, N, c.eK, N, G, N, W, N);                       // eK G
-  gemm_sq<MAXRM, T>(N, N, N, W, N, c.eKinv, N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
+  gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, G, N, W, N);                       // eK G
+  gemm_sq<MAXRM, TW>(N, N, N, W, N, c.eKinv, N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
 }
 
 // G <- B_lt^{-1} G B_lt: WrapKV!("Backward","B"), src/tU/GreenMatrix.jl:78-83.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ void wrap_bwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void wrap_bwd_kv(Ctx<KIND, T, KT, TW, KW>& c, TW* G, TW* W, int lt) {
   const int N = c.P.Ns;
   slice_diag(c, lt, -1);
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
@@ -160,8 +173,8 @@ __device__ void wrap_bwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
     G[e] = (c.sm.dvec[i] * G[e]) * c.sm.dinv[j];
   }
   __syncthreads();
-  gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, G, N, W, N);
-  gemm_sq<MAXRM, T>(N, N, N, W, N, c.eK, N, G, N);
+  gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, G, N, W, N);
+  gemm_sq<MAXRM, TW>(N, N, N, W, N, c.eK, N, G, N);
 }
 
 // tV bond rotation of direction j on both sides of G:
@@ -172,49 +185,49 @@ __device__ void wrap_bwd_kv(Ctx<KIND, T, KT>& c, T* G, T* W, int lt) {
 // 2x2 block of G (bond b rows, bond b' columns) becomes L_b B R_b'.
 // The per-bond coefficients are staged in sm.dvec / sm.dinv as (plus, minus)
 // pairs for rows (L) and columns (R).
-template <int KIND, class T, class KT>
-__device__ void tv_coeffs(Ctx<KIND, T, KT>& c, int lt, int j, int sign, const uint8_t* fields = nullptr) {
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void tv_coeffs(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, int sign, const uint8_t* fields = nullptr) {
   const SweepParams& P = c.P;
   const int nb = P.Ns / 2;
   const uint8_t* sl = (fields ? fields : c.s + (size_t)(lt - 1) * P.n_field) + (size_t)j * nb;
   // vtab per slice: [D_x | D_y | 1/D_x | 1/D_y] forward, then the same backward
   const double* tab = P.vtab + (size_t)(lt - 1) * 32 + (sign > 0 ? 0 : 16);
-  double* L = reinterpret_cast<double*>(c.sm.dvec);
-  double* R = reinterpret_cast<double*>(c.sm.dinv);
+  TW* L = c.sm.dvec;
+  TW* R = c.sm.dinv;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) {
     const int v = sl[i] - 1;
     const double dx = tab[v], dy = tab[4 + v], ix = tab[8 + v], iy = tab[12 + v];
-    L[2 * i] = 0.5 * (dx + dy);
-    L[2 * i + 1] = 0.5 * (dx - dy);
-    R[2 * i] = 0.5 * (ix + iy);
-    R[2 * i + 1] = 0.5 * (ix - iy);
+    L[2 * i] = cvt<TW>(0.5 * (dx + dy));
+    L[2 * i + 1] = cvt<TW>(0.5 * (dx - dy));
+    R[2 * i] = cvt<TW>(0.5 * (ix + iy));
+    R[2 * i + 1] = cvt<TW>(0.5 * (ix - iy));
   }
   __syncthreads();
 }
 
-template <int KIND, class T, class KT>
-__device__ void tv_rotate(Ctx<KIND, T, KT>& c, T* G, int lt, int j, int sign) {
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void tv_rotate(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int j, int sign) {
   const SweepParams& P = c.P;
   const int N = P.Ns, nb = N / 2;
   tv_coeffs(c, lt, j, sign);
-  const double* L = reinterpret_cast<const double*>(c.sm.dvec);
-  const double* R = reinterpret_cast<const double*>(c.sm.dinv);
+  const TW* L = c.sm.dvec;
+  const TW* R = c.sm.dinv;
   const int* bx = P.bx + (size_t)j * nb;
   const int* by = P.by + (size_t)j * nb;
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int i = e % nb, ip = e / nb;
     const int x = bx[i], y = by[i], xp = bx[ip], yp = by[ip];
-    const double lp = L[2 * i], lm = L[2 * i + 1], rp = R[2 * ip], rm = R[2 * ip + 1];
-    const double g00 = re(G[x + (size_t)xp * N]), g01 = re(G[x + (size_t)yp * N]);
-    const double g10 = re(G[y + (size_t)xp * N]), g11 = re(G[y + (size_t)yp * N]);
+    const TW lp = L[2 * i], lm = L[2 * i + 1], rp = R[2 * ip], rm = R[2 * ip + 1];
+    const TW g00 = G[x + (size_t)xp * N], g01 = G[x + (size_t)yp * N];
+    const TW g10 = G[y + (size_t)xp * N], g11 = G[y + (size_t)yp * N];
     // L B
-    const double a00 = fma(lp, g00, lm * g10), a01 = fma(lp, g01, lm * g11);
-    const double a10 = fma(lm, g00, lp * g10), a11 = fma(lm, g01, lp * g11);
+    const TW a00 = lp * g00 + lm * g10, a01 = lp * g01 + lm * g11;
+    const TW a10 = lm * g00 + lp * g10, a11 = lm * g01 + lp * g11;
     // (L B) R
-    G[x + (size_t)xp * N] = from_real<T>(fma(a00, rp, a01 * rm));
-    G[x + (size_t)yp * N] = from_real<T>(fma(a00, rm, a01 * rp));
-    G[y + (size_t)xp * N] = from_real<T>(fma(a10, rp, a11 * rm));
-    G[y + (size_t)yp * N] = from_real<T>(fma(a10, rm, a11 * rp));
+    G[x + (size_t)xp * N] = a00 * rp + a01 * rm;
+    G[x + (size_t)yp * N] = a00 * rm + a01 * rp;
+    G[y + (size_t)xp * N] = a10 * rp + a11 * rm;
+    G[y + (size_t)yp * N] = a10 * rm + a11 * rp;
   }
   __syncthreads();
 }
@@ -225,14 +238,14 @@ __device__ void tv_rotate(Ctx<KIND, T, KT>& c, T* G, int lt, int j, int sign) {
 // u' = G[:,S] r into shared memory while the other warps stage the rows
 // G[S,:]; then every thread applies G -= u' (E_S - G[S,:]) (Gupdate!,
 // src/public/Gupdate.jl:5-11).
-template <int KIND, class T, class KT>
-__device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t* sfield,
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y, uint8_t* sfield,
                         uint8_t tk, double tu, int logpos, int par) {
   const SweepParams& P = c.P;
   const int N = P.Ns;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr int RK = (KIND == KDQ_TU) ? 1 : 2;
-  Smem<T>& sm = c.sm;
+  Smem<TW>& sm = c.sm;
   if (warp == 0) {
     const int sold = *sfield;
     const int sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
@@ -242,7 +255,7 @@ __device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t
     if constexpr (KIND == KDQ_TU) {
       // get_r!, src/tU/GreenMatrix.jl:49-54; γ ratio src/tU/phy_update.jl:261
       const cd Δ = reinterpret_cast<const cd*>(P.rtab)[(size_t)(lt - 1) * 16 + o * 4 + nv];
-      const cd g = G[x + (size_t)x * N];
+      const cd g = cvt<cd>(G[x + (size_t)x * N]);
       const cd pc = cd{1.0, 0.0} + Δ * (cd{1.0, 0.0} - g);
       r00 = Δ / pc;
       p = abs2(pc) * P.gratio[o * 4 + nv];
@@ -270,8 +283,8 @@ __device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t
     } else {
       // get_r!, src/tUV/GreenMatrix.jl:73-89; weight src/tUV/phy_update.jl:193-197
       const T* t2 = reinterpret_cast<const T*>(P.rtab) + (size_t)(o * 4 + nv) * 2;
-      const T gxx = G[x + (size_t)x * N], gxy = G[x + (size_t)y * N];
-      const T gyx = G[y + (size_t)x * N], gyy = G[y + (size_t)y * N];
+      const T gxx = cvt<T>(G[x + (size_t)x * N]), gxy = cvt<T>(G[x + (size_t)y * N]);
+      const T gyx = cvt<T>(G[y + (size_t)x * N]), gyy = cvt<T>(G[y + (size_t)y * N]);
       T a00 = t2[0] - t2[0] * gxx, a01 = zero<T>() - t2[0] * gxy;
       T a10 = zero<T>() - t2[1] * gyx, a11 = t2[1] - t2[1] * gyy;
       a00 = a00 + one<T>();
@@ -291,15 +304,16 @@ __device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t
       if (lane == 0) atomicOr(&c.ctl->err, KDQ_FLAG_NAN);
     }
     if (acc) {
-      // u' = G[:,S] r
+      // u' = G[:,S] r (working precision)
+      const TW w00 = cvt<TW>(r00), w01 = cvt<TW>(r01), w10 = cvt<TW>(r10), w11 = cvt<TW>(r11);
       for (int a = lane; a < N; a += 32) {
-        const T gx = G[a + (size_t)x * N];
+        const TW gx = G[a + (size_t)x * N];
         if constexpr (RK == 1) {
-          sm.ucol[0][a] = gx * r00;
+          sm.ucol[0][a] = gx * w00;
         } else {
-          const T gy = G[a + (size_t)y * N];
-          sm.ucol[0][a] = gx * r00 + gy * r10;
-          sm.ucol[1][a] = gx * r01 + gy * r11;
+          const TW gy = G[a + (size_t)y * N];
+          sm.ucol[0][a] = gx * w00 + gy * w10;
+          sm.ucol[1][a] = gx * w01 + gy * w11;
         }
       }
     }
@@ -314,15 +328,15 @@ __device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t
   } else {
     // w = E_S - G[S,:]
     for (int b = tid - 32; b < N; b += blockDim.x - 32) {
-      sm.wrow[0][b] = (b == x ? one<T>() : zero<T>()) - G[x + (size_t)b * N];
-      if constexpr (RK == 2) sm.wrow[1][b] = (b == y ? one<T>() : zero<T>()) - G[y + (size_t)b * N];
+      sm.wrow[0][b] = (b == x ? one<TW>() : zero<TW>()) - G[x + (size_t)b * N];
+      if constexpr (RK == 2) sm.wrow[1][b] = (b == y ? one<TW>() : zero<TW>()) - G[y + (size_t)b * N];
     }
   }
   __syncthreads();
   if (sm.accept[par]) {
     for (int e = tid; e < N * N; e += blockDim.x) {
       const int a = e % N, b = e / N;
-      T v = G[e];
+      TW v = G[e];
       madd(v, -sm.ucol[0][a], sm.wrow[0][b]);
       if constexpr (RK == 2) madd(v, -sm.ucol[1][a], sm.wrow[1][b]);
       G[e] = v;
@@ -334,8 +348,8 @@ __device__ void propose(Ctx<KIND, T, KT>& c, T* G, int lt, int x, int y, uint8_t
 
 // Fill the shared tape slice with n proposals starting at sweep-relative
 // index q0 (Philox) or at the chain's explicit-tape cursor.
-template <int KIND, class T, class KT>
-__device__ void load_tape(Ctx<KIND, T, KT>& c, uint32_t q0, int n) {
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void load_tape(Ctx<KIND, T, KT, TW, KW>& c, uint32_t q0, int n) {
   const SweepParams& P = c.P;
   if (P.tape_k) {
     const size_t base = (size_t)c.chain * P.tape_len + c.ctl->tape_pos;
@@ -357,14 +371,14 @@ __device__ void load_tape(Ctx<KIND, T, KT>& c, uint32_t q0, int n) {
   __syncthreads();
 }
 
-template <int KIND, class T, class KT>
-__device__ void finish_tape(Ctx<KIND, T, KT>& c, int n) {
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void finish_tape(Ctx<KIND, T, KT, TW, KW>& c, int n) {
   if (threadIdx.x == 0 && c.P.tape_k) c.ctl->tape_pos += n;
 }
 
 // All proposals of slice lt (tU, tUV) or of direction j of slice lt (tV).
-template <int KIND, class T, class KT>
-__device__ void update_layer(Ctx<KIND, T, KT>& c, int lt, int j, bool fwd) {
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fwd) {
   const SweepParams& P = c.P;
   const int Nt = P.Nt, pf = P.n_field;
   uint8_t* sl = c.s + (size_t)(lt - 1) * pf;
@@ -403,52 +417,52 @@ __device__ void update_layer(Ctx<KIND, T, KT>& c, int lt, int j, bool fwd) {
 // same product, half the multiply-adds.
 
 // Y (N x ns) <- B_lt Y, ping-ponging with Y2; returns the buffer holding it.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ T* apply_slice_left(Ctx<KIND, T, KT>& c, T* Y, T* Y2, int lt) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ TW* apply_slice_left(Ctx<KIND, T, KT, TW, KW>& c, TW* Y, TW* Y2, int lt) {
   const SweepParams& P = c.P;
   const int N = P.Ns, ns = N / 2;
   if constexpr (KIND == KDQ_TV) {
-    gemm_thin<MAXRM, T>(N, ns, N, c.eK, N, Y, N, Y2, N);
+    gemm_thin<MAXRM, TW>(N, ns, N, c.eK, N, Y, N, Y2, N);
     for (int j = P.z - 1; j >= 0; --j) {
       tv_coeffs(c, lt, j, +1);
-      const double* L = reinterpret_cast<const double*>(c.sm.dvec);
+      const TW* L = c.sm.dvec;
       for (int e = threadIdx.x; e < (N / 2) * ns; e += blockDim.x) {
         const int i = e % (N / 2), col = e / (N / 2);
         const int x = P.bx[j * (N / 2) + i], y = P.by[j * (N / 2) + i];
-        const double lp = L[2 * i], lm = L[2 * i + 1];
-        const double vx = re(Y2[x + (size_t)col * N]), vy = re(Y2[y + (size_t)col * N]);
-        Y2[x + (size_t)col * N] = from_real<T>(fma(lp, vx, lm * vy));
-        Y2[y + (size_t)col * N] = from_real<T>(fma(lm, vx, lp * vy));
+        const TW lp = L[2 * i], lm = L[2 * i + 1];
+        const TW vx = Y2[x + (size_t)col * N], vy = Y2[y + (size_t)col * N];
+        Y2[x + (size_t)col * N] = lp * vx + lm * vy;
+        Y2[y + (size_t)col * N] = lm * vx + lp * vy;
       }
       __syncthreads();
     }
   } else {
     slice_diag(c, lt, +1);
-    gemm_thin<MAXRM, T>(N, ns, N, c.eK, N, Y, N, Y2, N, c.sm.dvec, (const T*)nullptr);
+    gemm_thin<MAXRM, TW>(N, ns, N, c.eK, N, Y, N, Y2, N, c.sm.dvec, (const TW*)nullptr);
   }
   return Y2;
 }
 
 // Z (ns x N) <- Z B_lt, ping-ponging with Z2; returns the buffer holding it.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ T* apply_slice_right(Ctx<KIND, T, KT>& c, T* Z, T* Z2, int lt) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ TW* apply_slice_right(Ctx<KIND, T, KT, TW, KW>& c, TW* Z, TW* Z2, int lt) {
   const SweepParams& P = c.P;
   const int N = P.Ns, ns = N / 2;
   if constexpr (KIND == KDQ_TV) {
     for (int j = 0; j < P.z; ++j) {        // Z V_1 V_2 ... V_z, V_j = L (symmetric)
       tv_coeffs(c, lt, j, +1);
-      const double* L = reinterpret_cast<const double*>(c.sm.dvec);
+      const TW* L = c.sm.dvec;
       for (int e = threadIdx.x; e < ns * (N / 2); e += blockDim.x) {
         const int row = e % ns, i = e / ns;
         const int x = P.bx[j * (N / 2) + i], y = P.by[j * (N / 2) + i];
-        const double lp = L[2 * i], lm = L[2 * i + 1];
-        const double vx = re(Z[row + (size_t)x * ns]), vy = re(Z[row + (size_t)y * ns]);
-        Z[row + (size_t)x * ns] = from_real<T>(fma(vx, lp, vy * lm));
-        Z[row + (size_t)y * ns] = from_real<T>(fma(vx, lm, vy * lp));
+        const TW lp = L[2 * i], lm = L[2 * i + 1];
+        const TW vx = Z[row + (size_t)x * ns], vy = Z[row + (size_t)y * ns];
+        Z[row + (size_t)x * ns] = vx * lp + vy * lm;
+        Z[row + (size_t)y * ns] = vx * lm + vy * lp;
       }
       __syncthreads();
     }
-    gemm_thin<MAXRM, T>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
+    gemm_thin<MAXRM, TW>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
   } else {
     slice_diag(c, lt, +1);
     for (int e = threadIdx.x; e < ns * N; e += blockDim.x) {
@@ -456,15 +470,15 @@ __device__ T* apply_slice_right(Ctx<KIND, T, KT>& c, T* Z, T* Z2, int lt) {
       Z[e] = Z[e] * c.sm.dvec[col];
     }
     __syncthreads();
-    gemm_thin<MAXRM, T>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
+    gemm_thin<MAXRM, TW>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
   }
   return Z2;
 }
 
 // G = I - BR (BL BR)^-1 BL (get_G!, src/public/Gupdate.jl:139-157); records
 // the drift against the wrapped G when `drift` is set.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ void get_G(Ctx<KIND, T, KT>& c, const T* BL, const T* BR, bool drift) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, bool drift) {
   const int N = c.P.Ns, ns = N / 2;
   gemm_thin<MAXRM, T>(ns, ns, N, BL, ns, BR, N, c.Mss, ns);
   __shared__ int bad;
@@ -474,17 +488,17 @@ __device__ void get_G(Ctx<KIND, T, KT>& c, const T* BL, const T* BR, bool drift)
   for (int e = threadIdx.x; e < ns * N; e += blockDim.x) c.X[e] = BL[e];
   __syncthreads();
   lu_solve(ns, N, c.Mss, c.piv, c.X);
-  gemm_sq<MAXRM, T>(N, N, ns, BR, N, c.X, ns, c.W1, N);
+  gemm_sq<MAXRM, T>(N, N, ns, BR, N, c.X, ns, c.Gd, N);
   double d2 = 0.0, n2 = 0.0;
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
     const int i = e % N, j = e / N;
-    T g = zero<T>() - c.W1[e];
+    T g = zero<T>() - c.Gd[e];
     if (i == j) g = g + one<T>();
     if (drift) {
-      d2 += abs2(c.G[e] - g);
+      d2 += abs2(cvt<T>(c.G[e]) - g);
       n2 += abs2(g);
     }
-    c.G[e] = g;
+    c.G[e] = cvt<TW>(g);
   }
   if (drift) {
     d2 = block_sum(d2, c.sm.red);
@@ -503,55 +517,72 @@ __device__ void get_G(Ctx<KIND, T, KT>& c, const T* BL, const T* BR, bool drift)
 }
 
 // BRs[k+1] = orth_cols(BM(k) BRs[k]) then G recompute at node k+1.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ void node_forward(Ctx<KIND, T, KT>& c, int k) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
   const SweepParams& P = c.P;
   const int N = P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
   T* BRk = P.BRs<T>(c.chain) + (size_t)(k - 1) * fs;
   T* BRn = BRk + fs;
-  for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Y[e] = BRk[e];
+  for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Yw[e] = cvt<TW>(BRk[e]);
   __syncthreads();
-  T* cur = c.Y;
-  T* oth = c.Y2;
+  TW* cur = c.Yw;
+  TW* oth = c.Y2w;
   for (int lt = (int)P.nodes[k - 1] + 1; lt <= (int)P.nodes[k]; ++lt) {
-    T* res = apply_slice_left<MAXRM>(c, cur, oth, lt);
+    TW* res = apply_slice_left<MAXRM>(c, cur, oth, lt);
     oth = cur;
     cur = res;
   }
-  householder_q(N, ns, cur, BRn, c.sm.wn, c.sm.red, &c.sm.w0);
+  T* src;
+  if constexpr (std::is_same_v<T, TW>) {
+    src = cur;
+  } else {   // the block product in working precision, its QR in FP64
+    for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Y[e] = cvt<T>(cur[e]);
+    __syncthreads();
+    src = c.Y;
+  }
+  householder_q(N, ns, src, BRn, c.sm.wn, c.sm.red);
   const T* BLn = P.BLs<T>(c.chain) + (size_t)k * fs;
   get_G<MAXRM>(c, BLn, BRn, true);
   if (threadIdx.x == 0) c.ctl->idx = k + 1;
 }
 
 // BLs[k] = orth_rows(BLs[k+1] BM(k)) then (optionally) G recompute.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ void node_backward(Ctx<KIND, T, KT>& c, int k, bool recompute, bool drift) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute, bool drift) {
   const SweepParams& P = c.P;
   const int N = P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
   T* BLk = P.BLs<T>(c.chain) + (size_t)(k - 1) * fs;
   const T* BLn = BLk + fs;
-  for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Y[e] = BLn[e];
+  for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Yw[e] = cvt<TW>(BLn[e]);
   __syncthreads();
-  T* cur = c.Y;
-  T* oth = c.Y2;
+  TW* cur = c.Yw;
+  TW* oth = c.Y2w;
   for (int lt = (int)P.nodes[k]; lt > (int)P.nodes[k - 1]; --lt) {
-    T* res = apply_slice_right<MAXRM>(c, cur, oth, lt);
+    TW* res = apply_slice_right<MAXRM>(c, cur, oth, lt);
     oth = cur;
     cur = res;
   }
-  // orth_rows: QR of Z^H (N x ns), BL = Q^H
+  // orth_rows: QR of Z^H (N x ns) in FP64, BL = Q^H
+  T* A;
+  T* Q;
+  if constexpr (std::is_same_v<T, TW>) {
+    A = oth;
+    Q = cur;
+  } else {
+    A = c.Y;
+    Q = c.Y2;
+  }
   for (size_t e = threadIdx.x; e < fs; e += blockDim.x) {
     const int r = e % ns, col = e / ns;
-    oth[col + (size_t)r * N] = conjg(cur[e]);
+    A[col + (size_t)r * N] = conjg(cvt<T>(cur[e]));
   }
   __syncthreads();
-  householder_q(N, ns, oth, cur, c.sm.wn, c.sm.red, &c.sm.w0);
+  householder_q(N, ns, A, Q, c.sm.wn, c.sm.red);
   for (size_t e = threadIdx.x; e < fs; e += blockDim.x) {
     const int r = e % ns, col = e / ns;
-    BLk[e] = conjg(cur[col + (size_t)r * N]);
+    BLk[e] = conjg(Q[col + (size_t)r * N]);
   }
   __syncthreads();
   if (recompute) get_G<MAXRM>(c, BLk, P.BRs<T>(c.chain) + (size_t)(k - 1) * fs, drift);
@@ -563,8 +594,8 @@ __device__ inline double re_prod(double k, double g) { return k * g; }
 __device__ inline double re_prod(double k, cd g) { return k * g.x; }
 __device__ inline double re_prod(cd k, cd g) { return k.x * g.x - k.y * g.y; }
 
-template <int KIND, class T, class KT>
-__device__ void observables(Ctx<KIND, T, KT>& c, const T* G0);
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void observables(Ctx<KIND, T, KT, TW, KW>& c, const TW* G0);
 
 // Equal-time observables at tau = Nt/2 from G at slice t0 (phy_measure):
 // wrap a copy to Nt/2, symmetrise with HalfeK, accumulate one row.
@@ -573,20 +604,20 @@ __device__ void observables(Ctx<KIND, T, KT>& c, const T* G0);
 // the reference's accumulation (only the first term of each correlator in
 // the complex branch, where the `+adjoint(...)` lines are discarded
 // statements); `xy_i` is called with its real three-argument signature.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ void measure(Ctx<KIND, T, KT>& c, int t0) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void measure(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
   const SweepParams& P = c.P;
   const int N = P.Ns, Nt = P.Nt, half = Nt / 2;
-  T* G0 = c.W2;
-  T* W = c.W1;
+  TW* G0 = c.W2;
+  TW* W = c.W1;
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) G0[e] = c.G[e];
   __syncthreads();
   if (2 * t0 > Nt) {
     for (int t = t0; t > half; --t) {
       if constexpr (KIND == KDQ_TV) {
         for (int j = 0; j < P.z; ++j) tv_rotate(c, G0, t, j, -1);
-        gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, G0, N, W, N);
-        gemm_sq<MAXRM, T>(N, N, N, W, N, c.eK, N, G0, N);
+        gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, G0, N, W, N);
+        gemm_sq<MAXRM, TW>(N, N, N, W, N, c.eK, N, G0, N);
       } else {
         wrap_bwd_kv<MAXRM>(c, G0, W, t);
       }
@@ -594,23 +625,23 @@ __device__ void measure(Ctx<KIND, T, KT>& c, int t0) {
   } else {
     for (int t = t0 + 1; t <= half; ++t) {
       if constexpr (KIND == KDQ_TV) {
-        gemm_sq<MAXRM, T>(N, N, N, G0, N, c.eKinv, N, W, N);
-        gemm_sq<MAXRM, T>(N, N, N, c.eK, N, W, N, G0, N);
+        gemm_sq<MAXRM, TW>(N, N, N, G0, N, c.eKinv, N, W, N);
+        gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, W, N, G0, N);
         for (int j = P.z - 1; j >= 0; --j) tv_rotate(c, G0, t, j, +1);
       } else {
         wrap_fwd_kv<MAXRM>(c, G0, W, t);
       }
     }
   }
-  gemm_sq<MAXRM, T>(N, N, N, c.HalfeK, N, G0, N, W, N);
-  gemm_sq<MAXRM, T>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
+  gemm_sq<MAXRM, TW>(N, N, N, c.HalfeK, N, G0, N, W, N);
+  gemm_sq<MAXRM, TW>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
   observables(c, G0);
 }
 
 // Observables of the symmetrised Green's function G0 at tau = Nt/2,
 // accumulated into the chain's current measurement row.
-template <int KIND, class T, class KT>
-__device__ void observables(Ctx<KIND, T, KT>& c, const T* G0) {
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void observables(Ctx<KIND, T, KT, TW, KW>& c, const TW* G0) {
   const SweepParams& P = c.P;
   const int N = P.Ns;
   double acc[KDQ_MAX_OBS];
@@ -618,11 +649,11 @@ __device__ void observables(Ctx<KIND, T, KT>& c, const T* G0) {
   for (int q = 0; q < KDQ_MAX_OBS; ++q) acc[q] = 0.0;
   // kinetic energy: Σ K .* G0
   double ek = 0.0;
-  for (int e = threadIdx.x; e < N * N; e += blockDim.x) ek += re_prod(c.Kmat[e], G0[e]);
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) ek += re_prod(c.Kmat[e], cvt<T>(G0[e]));
   // on-site term
   double eu = 0.0;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    const T d = G0[i + (size_t)i * N];
+    const T d = cvt<T>(G0[i + (size_t)i * N]);
     if constexpr (KIND == KDQ_TUV && sizeof(T) == sizeof(double)) {
       eu += re((one<T>() - d) * (one<T>() - d));
     } else {
@@ -635,8 +666,8 @@ __device__ void observables(Ctx<KIND, T, KT>& c, const T* G0) {
     const int nbond = KIND == KDQ_TV ? (N / 2) * P.z : N * P.z;
     for (int b = threadIdx.x; b < nbond; b += blockDim.x) {
       const int x = P.bx[b], y = P.by[b];
-      const T gxx = G0[x + (size_t)x * N], gyy = G0[y + (size_t)y * N];
-      const T gxy = G0[x + (size_t)y * N], gyx = G0[y + (size_t)x * N];
+      const T gxx = cvt<T>(G0[x + (size_t)x * N]), gyy = cvt<T>(G0[y + (size_t)y * N]);
+      const T gxy = cvt<T>(G0[x + (size_t)y * N]), gyx = cvt<T>(G0[y + (size_t)x * N]);
       const T ox = one<T>() - gxx, oy = one<T>() - gyy;
       if constexpr (KIND == KDQ_TV || sizeof(T) == sizeof(double)) {
         const double v = re(ox * oy - gxy * gyx);
@@ -662,7 +693,7 @@ __device__ void observables(Ctx<KIND, T, KT>& c, const T* G0) {
       const int a1 = 2 * (ix + (iy - 1) * L1) - 2, a2 = 2 * (jx + (jy - 1) * L1) - 2;
       const int b1 = a1 + 1, b2 = a2 + 1;
       const double ph = P.cosr[r];
-      auto g = [&](int i, int j) { return G0[i + (size_t)j * N]; };
+      auto g = [&](int i, int j) { return cvt<T>(G0[i + (size_t)j * N]); };
       const T o = one<T>();
       if constexpr (KIND == KDQ_TV) {
         double t[4];
@@ -742,23 +773,23 @@ __device__ void observables(Ctx<KIND, T, KT>& c, const T* G0) {
 
 // X <- X B_lt (right = true) or B_lt X, with B the slice matrix of `fields`
 // (inv: B^-1).  W is N x N scratch.
-template <int MAXRM, int KIND, class T, class KT>
-__device__ void mul_slice(Ctx<KIND, T, KT>& c, T* X, T* W, int lt, const uint8_t* fields, bool right, bool inv) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void mul_slice(Ctx<KIND, T, KT, TW, KW>& c, TW* X, TW* W, int lt, const uint8_t* fields, bool right, bool inv) {
   const SweepParams& P = c.P;
   const int N = P.Ns;
   if constexpr (KIND == KDQ_TV) {
     // B = V_1 ... V_z eK, V_j = UV D_j UV (2x2 blocks (lp, lm)); V_j^-1 blocks (rp, rm)
     auto rot = [&](int j) {
       tv_coeffs(c, lt, j, +1, fields);
-      const double* Q = reinterpret_cast<const double*>(inv ? c.sm.dinv : c.sm.dvec);
+      const TW* Q = inv ? c.sm.dinv : c.sm.dvec;
       const int nb = N / 2;
       for (int e = threadIdx.x; e < nb * N; e += blockDim.x) {
         const int i = e % nb, o = e / nb;
         const int x = P.bx[j * nb + i], y = P.by[j * nb + i];
-        const double qp = Q[2 * i], qm = Q[2 * i + 1];
-        T* px = right ? X + (size_t)x * N + o : X + x + (size_t)o * N;
-        T* py = right ? X + (size_t)y * N + o : X + y + (size_t)o * N;
-        const T vx = *px, vy = *py;
+        const TW qp = Q[2 * i], qm = Q[2 * i + 1];
+        TW* px = right ? X + (size_t)x * N + o : X + x + (size_t)o * N;
+        TW* py = right ? X + (size_t)y * N + o : X + y + (size_t)o * N;
+        const TW vx = *px, vy = *py;
         *px = vx * qp + vy * qm;
         *py = vx * qm + vy * qp;
       }
@@ -766,8 +797,8 @@ __device__ void mul_slice(Ctx<KIND, T, KT>& c, T* X, T* W, int lt, const uint8_t
     };
     const bool k_first = right == inv;   // X eKinv ... / eK X ... come first
     if (k_first) {
-      if (right) gemm_sq<MAXRM, T>(N, N, N, X, N, c.eKinv, N, W, N);
-      else gemm_sq<MAXRM, T>(N, N, N, c.eK, N, X, N, W, N);
+      if (right) gemm_sq<MAXRM, TW>(N, N, N, X, N, c.eKinv, N, W, N);
+      else gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, X, N, W, N);
       for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = W[e];
       __syncthreads();
     }
@@ -776,39 +807,39 @@ __device__ void mul_slice(Ctx<KIND, T, KT>& c, T* X, T* W, int lt, const uint8_t
     const bool ascending = right ? !inv : inv;
     for (int q = 0; q < P.z; ++q) rot(ascending ? q : P.z - 1 - q);
     if (!k_first) {
-      if (right) gemm_sq<MAXRM, T>(N, N, N, X, N, c.eK, N, W, N);
-      else gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, X, N, W, N);
+      if (right) gemm_sq<MAXRM, TW>(N, N, N, X, N, c.eK, N, W, N);
+      else gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, X, N, W, N);
       for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = W[e];
       __syncthreads();
     }
   } else {
     slice_diag(c, lt, +1, fields);   // dvec = D, dinv = 1 ./ D
-    const T* d = inv ? c.sm.dinv : c.sm.dvec;
+    const TW* d = inv ? c.sm.dinv : c.sm.dvec;
     if (right && !inv) {          // X D eK
       for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = X[e] * d[e / N];
       __syncthreads();
-      gemm_sq<MAXRM, T>(N, N, N, X, N, c.eK, N, W, N);
+      gemm_sq<MAXRM, TW>(N, N, N, X, N, c.eK, N, W, N);
     } else if (right) {           // X eKinv D^-1
-      gemm_sq<MAXRM, T>(N, N, N, X, N, c.eKinv, N, W, N, (const T*)nullptr, d);
+      gemm_sq<MAXRM, TW>(N, N, N, X, N, c.eKinv, N, W, N, (const TW*)nullptr, d);
     } else if (!inv) {            // D eK X
-      gemm_sq<MAXRM, T>(N, N, N, c.eK, N, X, N, W, N, d, (const T*)nullptr);
+      gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, X, N, W, N, d, (const TW*)nullptr);
     } else {                      // eKinv D^-1 X
       for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = d[e % N] * X[e];
       __syncthreads();
-      gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, X, N, W, N);
+      gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, X, N, W, N);
     }
     for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = W[e];
     __syncthreads();
   }
 }
 
-template <int MAXRM, int KIND, class T, class KT>
-__device__ void measure_fast(Ctx<KIND, T, KT>& c, int t0) {
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void measure_fast(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
   const SweepParams& P = c.P;
   const int N = P.Ns, half = P.Nt / 2, nf = P.n_field;
-  T* L = static_cast<T*>(P.Lm) + (size_t)c.chain * P.sz_NN;
-  T* R = static_cast<T*>(P.Rm) + (size_t)c.chain * P.sz_NN;
-  T* W = c.W1;
+  TW* L = static_cast<TW*>(P.Lm) + (size_t)c.chain * P.sz_NN;
+  TW* R = static_cast<TW*>(P.Rm) + (size_t)c.chain * P.sz_NN;
+  TW* W = c.W1;
   int* fslice = reinterpret_cast<int*>(P.mstack + (size_t)c.chain * P.mstack_stride);
   uint8_t* fsnap = P.mstack + (size_t)c.chain * P.mstack_stride + (size_t)P.mstack_max * sizeof(int);
   const bool below = 2 * t0 <= P.Nt;     // t0 <= Nt/2: factors B_half ... B_{t0+1}
@@ -831,8 +862,8 @@ __device__ void measure_fast(Ctx<KIND, T, KT>& c, int t0) {
   }
   if (k == 0) {
     for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
-      L[e] = conv<T>::from(c.HalfeK[e]);
-      R[e] = conv<T>::from(c.HalfeKinv[e]);
+      L[e] = cvt<TW>(c.HalfeK[e]);
+      R[e] = cvt<TW>(c.HalfeKinv[e]);
     }
     __syncthreads();
   } else {
@@ -856,8 +887,8 @@ __device__ void measure_fast(Ctx<KIND, T, KT>& c, int t0) {
   }
   if (threadIdx.x == 0) c.ctl->meas_n = m;
   __syncthreads();
-  gemm_sq<MAXRM, T>(N, N, N, L, N, c.G, N, W, N);
-  gemm_sq<MAXRM, T>(N, N, N, W, N, R, N, c.W2, N);
+  gemm_sq<MAXRM, TW>(N, N, N, L, N, c.G, N, W, N);
+  gemm_sq<MAXRM, TW>(N, N, N, W, N, R, N, c.W2, N);
   observables(c, c.W2);
 }
 
@@ -865,35 +896,40 @@ __device__ void measure_fast(Ctx<KIND, T, KT>& c, int t0) {
 // mode KDQ_MODE_INIT: block k of the initial left chain (and G at k == 1);
 // KDQ_MODE_FWD: forward slices node(k)+1 .. node(k+1), then the node;
 // KDQ_MODE_BWD: backward slices node(k+1) .. node(k)+1, then the node.
-template <int KIND, class T, class KT, int MAXRM>
+// MIXED selects the FP32 working precision (see the header of this file).
+template <int KIND, class T, class KT, int MAXRM, bool MIXED>
 __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int mode, int k) {
+  using TW = std::conditional_t<MIXED, typename low_t<T>::type, T>;
+  using KW = std::conditional_t<MIXED, typename low_t<KT>::type, KT>;
   extern __shared__ double dyn_d[];
-  __shared__ Smem<T> sm;
+  __shared__ Smem<TW> sm;
   const int chain = blockIdx.x;
   const int N = P.Ns;
   const size_t cNN = (size_t)chain * P.sz_NN;
   const size_t cNn = (size_t)chain * P.sz_Nn;
-  Ctx<KIND, T, KT> c{P,
-                     sm,
-                     reinterpret_cast<uint8_t*>(dyn_d + P.n_field),
-                     dyn_d,
-                     chain,
-                     P.ctl + chain,
-                     static_cast<T*>(P.G) + cNN,
-                     static_cast<T*>(P.W1) + cNN,
-                     static_cast<T*>(P.W2) + cNN,
-                     static_cast<T*>(P.Y) + cNn,
-                     static_cast<T*>(P.Y2) + cNn,
-                     static_cast<T*>(P.Mss) + (size_t)chain * P.sz_nn,
-                     static_cast<T*>(P.X) + cNn,
-                     P.piv + (size_t)chain * (N / 2),
-                     P.s + (size_t)chain * P.Nt * P.n_field,
-                     static_cast<const KT*>(P.eK),
-                     static_cast<const KT*>(P.eKinv),
-                     static_cast<const KT*>(P.HalfeK),
-                     static_cast<const KT*>(P.HalfeKinv),
-                     static_cast<const KT*>(P.K),
-                     static_cast<const T*>(P.Pt)};
+  Ctx<KIND, T, KT, TW, KW> c{P,
+                             sm,
+                             reinterpret_cast<uint8_t*>(dyn_d + P.n_field),
+                             dyn_d,
+                             chain,
+                             P.ctl + chain,
+                             static_cast<TW*>(P.G) + cNN,
+                             static_cast<TW*>(P.W1) + cNN,
+                             static_cast<TW*>(P.W2) + cNN,
+                             static_cast<TW*>(P.Yw) + cNn,
+                             static_cast<TW*>(P.Y2w) + cNn,
+                             static_cast<T*>(P.Y) + cNn,
+                             static_cast<T*>(P.Y2) + cNn,
+                             static_cast<T*>(P.Gd) + cNN,
+                             static_cast<T*>(P.Mss) + (size_t)chain * P.sz_nn,
+                             static_cast<T*>(P.X) + cNn,
+                             P.piv + (size_t)chain * (N / 2),
+                             P.s + (size_t)chain * P.Nt * P.n_field,
+                             static_cast<const KW*>(P.eK),
+                             static_cast<const KW*>(P.eKinv),
+                             static_cast<const KW*>(P.HalfeK),
+                             static_cast<const KW*>(P.HalfeKinv),
+                             static_cast<const KT*>(P.K)};
   if (mode == KDQ_MODE_INIT) {
     node_backward<MAXRM>(c, k, k == 1, false);
     return;
@@ -905,8 +941,8 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
     const bool rec = P.record && (KIND == KDQ_TU ? (Θidx - k >= 0 && Θidx - k <= 1) : abs(k - Θidx) <= 1);
     for (int lt = lo + 1; lt <= hi; ++lt) {
       if constexpr (KIND == KDQ_TV) {
-        gemm_sq<MAXRM, T>(N, N, N, c.G, N, c.eKinv, N, c.W1, N);
-        gemm_sq<MAXRM, T>(N, N, N, c.eK, N, c.W1, N, c.G, N);
+        gemm_sq<MAXRM, TW>(N, N, N, c.G, N, c.eKinv, N, c.W1, N);
+        gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, c.W1, N, c.G, N);
         for (int j = P.z - 1; j >= 0; --j) {
           tv_rotate(c, c.G, lt, j, +1);
           update_layer(c, lt, j, true);
@@ -931,8 +967,8 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
           update_layer(c, lt, j, false);
           tv_rotate(c, c.G, lt, j, -1);
         }
-        gemm_sq<MAXRM, T>(N, N, N, c.eKinv, N, c.G, N, c.W1, N);
-        gemm_sq<MAXRM, T>(N, N, N, c.W1, N, c.eK, N, c.G, N);
+        gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, c.G, N, c.W1, N);
+        gemm_sq<MAXRM, TW>(N, N, N, c.W1, N, c.eK, N, c.G, N);
         if (rec) {
           if (P.record == 2) measure_fast<MAXRM>(c, lt - 1);
           else measure<MAXRM>(c, lt - 1);

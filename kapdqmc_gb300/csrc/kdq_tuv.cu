@@ -1,22 +1,8 @@
-// t-U-V model kernels: complex sweep for U > 0, real otherwise.
-#include "kdq_launch.h"
-#include "kdq_sweep.cuh"
+// tuv model sweep kernels, FP64.
+#include "kdq_launch_impl.cuh"
 
 namespace kdq {
-template <class T, int R>
-static cudaError_t go(const SweepParams& P, int mode, int k, int nch, size_t dyn, cudaStream_t st) {
-  k_block<KDQ_TUV, T, double, R><<<nch, KDQ_THREADS, dyn, st>>>(P, mode, k);
-  return cudaGetLastError();
-}
-cudaError_t launch_tuv(const SweepParams& P, int mode, int k, int maxrm, bool gc, int nch, size_t dyn,
-                       cudaStream_t st) {
-  if (gc) {
-    if (maxrm == 1) return go<cd, 1>(P, mode, k, nch, dyn, st);
-    if (maxrm == 3) return go<cd, 3>(P, mode, k, nch, dyn, st);
-    return go<cd, 6>(P, mode, k, nch, dyn, st);
-  }
-  if (maxrm == 1) return go<double, 1>(P, mode, k, nch, dyn, st);
-  if (maxrm == 3) return go<double, 3>(P, mode, k, nch, dyn, st);
-  return go<double, 6>(P, mode, k, nch, dyn, st);
+cudaError_t launch_tuv(const SweepParams& P, int mode, int k, int maxrm, bool gc, int nch, size_t dyn, cudaStream_t st) {
+  return launch_tuv_impl<false>(P, mode, k, maxrm, gc, nch, dyn, st);
 }
 }  // namespace kdq

@@ -166,6 +166,13 @@ class Sweeper:
         self._ck(self.lib.kdq_get_obs(self.h, obs.ctypes.data, obs.size))
         return obs.reshape(self.nchains, rows, self.n_obs)
 
+    def set_precision(self, mode: str):
+        """"fp64" (default, the reference's arithmetic) or "mixed" (FP32 bulk
+        products and updates, FP64 ratios and stabilisation)."""
+        code = {"fp64": 0, "mixed": 1}[mode]
+        self._ck(self.lib.kdq_set_precision(self.h, code))
+        self.precision = mode
+
     def set_graphs(self, enable: bool):
         """Replay sweeps from a captured CUDA graph (default) or launch block by block."""
         self._ck(self.lib.kdq_set_graphs(self.h, int(bool(enable))))
