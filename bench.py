@@ -50,17 +50,62 @@ def reference_tau_int():
         return None
 
 
-def make_model():
+def _tv_6x6():
     from kapdqmc_gb300 import tV_Hubbard_Para
     return tV_Hubbard_Para(Ht=1.0, Hv1=1.0, Hv2=1.0, Δt=0.05, Θrelax=10.0, Θquench=0.0,
                            Lattice="HoneyComb120", site=[6, 6], BatchSize=10, Initial="H0")
 
 
-CONFIG = {"workload": "t-V 6x6 honeycomb (N=72), 400 slices, n_wrap=10, V/t=1, dt=0.05, "
-                      "256 independent chains, FP64, energy + density structure factor per sweep",
-          "model": "tV_Hubbard_Para(HoneyComb120, site=[6,6])", "chains_per_gpu": NCHAINS,
-          "Ns": 72, "Nt": 400, "n_wrap": 10,
-          "l2": "no flush: per-GPU chain state (B chains, fields, G) is ~0.5 GB > 129 MB L2"}
+def _tu_12x12():
+    from kapdqmc_gb300 import tU_Hubbard_Para
+    return tU_Hubbard_Para(Ht=1.0, Hu1=8.0, Hu2=8.0, Δt=0.05, Θrelax=8.0, Θquench=0.0,
+                           Lattice="SQUARE45", site=[6, 12], BatchSize=8, Initial="H0")
+
+
+def _tuv_8x8():
+    from kapdqmc_gb300 import tUV_Hubbard_Para
+    return tUV_Hubbard_Para(Ht=1.0, Hu=4.0, Hv=0.5, Lattice="SQUARE45", site=[4, 8], Δt=0.1, Θ=10.0,
+                            BatchSize=10, Initial="H0", allow_marginal=True)
+
+
+def _tu_hc_9x9():
+    from kapdqmc_gb300 import tU_Hubbard_Para
+    return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Δt=0.1, Θrelax=10.0, Θquench=0.0,
+                           Lattice="HoneyComb120", site=[9, 9], BatchSize=10, Initial="H0")
+
+
+# The bench line is c2 (the metric's configuration: batched plain FP64 sweep);
+# the others are the remaining single-GPU configurations, for `--workload`.
+WORKLOADS = {
+    "c2": dict(make=_tv_6x6, chains=256, Ns=72, Nt=400, n_wrap=10,
+               desc="t-V 6x6 honeycomb (N=72), 400 slices, n_wrap=10, V/t=1, dt=0.05, 256 independent "
+                    "chains, energy + density structure factor per sweep",
+               model="tV_Hubbard_Para(HoneyComb120, site=[6,6])"),
+    "c3": dict(make=_tu_12x12, chains=128, Ns=144, Nt=320, n_wrap=8,
+               desc="t-U 12x12 square (N=144), 320 slices, n_wrap=8, U/t=8, dt=0.05, 128 independent "
+                    "chains, energy + double occupancy per sweep",
+               model="tU_Hubbard_Para(SQUARE45, site=[6,12])"),
+    "c4": dict(make=_tuv_8x8, chains=256, Ns=64, Nt=200, n_wrap=10,
+               desc="t-UV 8x8 square (N=64), 200 slices, n_wrap=10, U/t=4, V/t=0.5, dt=0.1, 256 chains "
+                    "(128 replica pairs), energies per sweep",
+               model="tUV_Hubbard_Para(SQUARE45, site=[4,8], allow_marginal=True)"),
+    "c5": dict(make=_tu_hc_9x9, chains=256, Ns=162, Nt=200, n_wrap=10,
+               desc="t-U 9x9 honeycomb (N=162), 200 slices, n_wrap=10, U/t=4, dt=0.1, 256 chains, "
+                    "energy, double occupancy and structure factors per sweep",
+               model="tU_Hubbard_Para(HoneyComb120, site=[9,9])"),
+}
+WL = WORKLOADS["c2"]
+PRECISION = "fp64"
+
+
+def make_model():
+    return WL["make"]()
+
+
+def config():
+    return {"workload": WL["desc"] + f", {PRECISION}", "model": WL["model"], "chains_per_gpu": NCHAINS,
+            "Ns": WL["Ns"], "Nt": WL["Nt"], "n_wrap": WL["n_wrap"], "precision": PRECISION,
+            "l2": "no flush: per-GPU chain state (B chains, fields, G) is larger than the 129 MB L2"}
 
 
 def tau_int(series: np.ndarray, c: float = 5.0):
@@ -233,6 +278,7 @@ def run_tau(args):
     from kapdqmc_gb300.sweep import Sweeper
     model = make_model()
     sw = Sweeper(model, NCHAINS)
+    sw.set_precision(PRECISION)
     sw.set_fields(np.stack([Initial_s(model, 5000 + c) for c in range(NCHAINS)]))
     sw.set_rng(424242)
     sw.init()
@@ -248,7 +294,7 @@ def run_tau(args):
         T = ek.shape[1] // B
         m = ek[:, :T * B].reshape(ek.shape[0], T, B).mean(axis=2)
         bins[B] = float(m.var() * B / (2 * var))
-    out = {"workload": CONFIG["workload"], "chains": NCHAINS, "sweeps": args.tau_run, "burn_in": burn,
+    out = {"workload": config()["workload"], "chains": NCHAINS, "sweeps": args.tau_run, "burn_in": burn,
            "observable": "kinetic energy (first measurement column)", "estimator": "Sokal window c=5",
            "tau_int": tau, "tau_int_binning": bins, "energy_mean": float(ek.mean()),
            "energy_err": float(ek.mean(axis=1).std() / math.sqrt(NCHAINS))}
@@ -275,7 +321,7 @@ def run_reference(args):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": float(np.mean(walls)) * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic (seeded HS fields and Philox proposal stream)", "config": CONFIG,
+           "data": "synthetic (seeded HS fields and Philox proposal stream)", "config": config(),
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": CPU_KIND, "sample": sample,
                             "chain_sweeps_per_s": cs},
@@ -300,10 +346,9 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    global NCHAINS
-    NCHAINS = args.chains
     model = make_model()
     sw = Sweeper(model, NCHAINS, device=local)
+    sw.set_precision(PRECISION)
     fields = np.stack([Initial_s(model, 1000 + NCHAINS * rank + c) for c in range(NCHAINS)])
     seed = 20261203 + rank
     stream = torch.cuda.ExternalStream(sw.stream, device=dev)
@@ -332,27 +377,37 @@ def run_gpu(args):
     obs = sw.get_obs(args.warmup + args.steps)
     ek = obs[:, args.warmup:, 0]
     tau_live = tau_int(ek)
-    tau = args.tau_int or reference_tau_int() or tau_live
+    tau = args.tau_int or (reference_tau_int() if WL is WORKLOADS["c2"] and PRECISION == "fp64" else None) \
+        or tau_live
     cs_per_s, t_max = replica_throughput(dist, ms, NCHAINS * args.steps, dev)
     value = cs_per_s / tau
 
     # ---- roofline of the sweep kernel (the only kernel of the timed region)
     acc_per_chain_sweep = st["accepted"] / (NCHAINS * args.steps)
-    fl = sweep_flops(model, acc_per_chain_sweep, record=RECORD)
     launches_per_sweep = 2 * (len(model.nodes) - 1) + 1     # block launches + one control reset per call
     block_launches = args.steps * 2 * (len(model.nodes) - 1)
-    flops_per_launch = fl["total"] * NCHAINS / (2 * (len(model.nodes) - 1))
+    per_launch = NCHAINS / (2 * (len(model.nodes) - 1))
     avg_launch_s = ms * 1e-3 / block_launches
-    achieved = flops_per_launch / avg_launch_s / 1e12
     peak = fp64_peak_tflops(torch, dev)
-    roof = {"bound": "fp64", "pipe": "FP64 DFMA (CUDA cores)", "achieved": achieved, "peak": peak,
+    kc = bool(np.any(np.imag(np.asarray(model.eK)) != 0))
+    fl = sweep_flops(model, acc_per_chain_sweep, record=RECORD, k_complex=kc)
+    if PRECISION == "fp64":
+        flops_per_launch = fl["total"] * per_launch
+        pipe = "FP64 DFMA (CUDA cores)"
+    else:   # the FP64 part (QR, LU, G recompute) is what the mixed sweep is bound by
+        flops_per_launch = fl["stabilise_qr_lu"] * per_launch
+        pipe = "FP64 DFMA for QR, LU and the G recompute (the FP32 bulk products are reported apart)"
+    achieved = flops_per_launch / avg_launch_s / 1e12
+    roof = {"bound": "fp64", "pipe": pipe, "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
-            "traffic": traffic_per_launch(),
+            "traffic": traffic_per_launch() if WL is WORKLOADS["c2"] else None,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean over every k_block "
                               "launch of the same workload (profiles/k_block_tv6x6_launches.md)",
             "flops_per_launch": flops_per_launch,
             "flops_per_chain_sweep": fl}
+    if PRECISION == "mixed":
+        roof["fp32_achieved_tflops"] = (fl["total"] - fl["stabilise_qr_lu"]) * per_launch / avg_launch_s / 1e12
 
     # ---- end to end through kdq_phy_update with host buffers
     e2e_steps = max(2, min(args.steps, 5))
@@ -378,7 +433,7 @@ def run_gpu(args):
                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                "data": "synthetic (seeded HS fields and Philox proposal stream)",
-               "config": dict(CONFIG, parallelism=f"replicas x{world}"),
+               "config": dict(config(), parallelism=f"replicas x{world}"),
                "chain_sweeps_per_s": cs_per_s, "tau_int": tau, "tau_int_live": tau_live,
                "tau_int_source": "committed long run" if tau != tau_live else "this run",
                "acceptance": st["accepted"] / max(st["proposals"], 1),
@@ -390,7 +445,7 @@ def run_gpu(args):
                        "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                        "ms_per_step": wall / e2e_steps * 1e3}}
         print(json.dumps(out), file=sys.stderr, flush=True)
-        if not args.no_cpu and world == 1:
+        if not args.no_cpu and world == 1 and WL is WORKLOADS["c2"]:
             cores = os.cpu_count() or 1
             cs_cpu, wall_cpu = cpu_chain_sweeps_per_s(cores, sweeps_per_chain=CPU_SWEEPS)
             out["cpu_baseline"] = {"value": cs_cpu / tau, "unit": UNIT, "cores": cores, "kind": CPU_KIND,
@@ -435,11 +490,22 @@ def main():
                     help="τ_int used to convert chain-sweeps/s (default: the committed long-run value)")
     ap.add_argument("--tau-run", type=int, default=0,
                     help="long run of this many sweeps; prints the workload's τ_int JSON and exits")
-    ap.add_argument("--chains", type=int, default=NCHAINS,
-                    help="chains per GPU (profiling of small cases only; bench lines use 256)")
+    ap.add_argument("--chains", type=int, default=None,
+                    help="chains per GPU (profiling of small cases only; bench lines use the workload's)")
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
+                    help="configuration (default c2, the metric's; the CPU arm exists for c2 only)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="arithmetic of the sweep (mixed: complex sweeps only)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    global WL, NCHAINS, PRECISION
+    WL = WORKLOADS[args.workload]
+    NCHAINS = args.chains or WL["chains"]
+    PRECISION = args.precision
+    if args.impl == "reference" and args.workload != "c2":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement covers the t-V workload only"}))
+        return
     if args.tau_run:
         run_tau(args)
     elif args.impl == "reference":

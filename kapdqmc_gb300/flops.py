@@ -48,6 +48,7 @@ def sweep_flops(model, accepted: float, record, k_complex: bool = False) -> dict
     hh = 2 * (2 * N * ns * ns - 2 * ns ** 3 // 3) * (mgg // 2)   # geqrf + orgqr (mgg/2 per op pair)
     getg = (ns * ns * N + ns ** 3 // 3 + ns * ns * N + N * N * ns) * mgg
     out["stabilise"] = thin + n_cross * (hh + getg)
+    out["stabilise_qr_lu"] = n_cross * (hh + getg)     # FP64 in both precisions
     if record == 2:
         # fast form: two products per measurement plus the factor pushes/pops
         # (each a slice matrix applied to L and to R)
@@ -56,7 +57,7 @@ def sweep_flops(model, accepted: float, record, k_complex: bool = False) -> dict
         out["measure"] = measure_wraps(model) * (wrap + rot) + measured_slices(model) * 2 * N ** 3 * mgk
     else:
         out["measure"] = 0
-    out["total"] = sum(out.values())
+    out["total"] = sum(v for k, v in out.items() if k != "stabilise_qr_lu")
     return out
 
 
