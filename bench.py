@@ -409,6 +409,17 @@ def run_gpu(args):
     if PRECISION == "mixed":
         roof["fp32_achieved_tflops"] = (fl["total"] - fl["stabilise_qr_lu"]) * per_launch / avg_launch_s / 1e12
 
+    if args.phases:
+        sw.enable_phase_timing(True)
+        sw.sweep(1, record=RECORD)
+        sw.synchronize()
+        ph = sw.phase_cycles()
+        tot = sum(ph.values())
+        print(json.dumps({"phase_shares": {k: round(v / tot, 4) for k, v in ph.items()},
+                          "ms_per_chain_sweep_at_sm_clock": {k: v / NCHAINS / 2.07e6 for k, v in ph.items()}}),
+              file=sys.stderr, flush=True)
+        sw.enable_phase_timing(False)
+
     # ---- end to end through kdq_phy_update with host buffers
     e2e_steps = max(2, min(args.steps, 5))
     cur = sw.get_fields()
@@ -488,6 +499,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--tau-int", type=float, default=None,
                     help="τ_int used to convert chain-sweeps/s (default: the committed long-run value)")
+    ap.add_argument("--phases", action="store_true",
+                    help="print the per-stage clock shares of one untimed sweep to stderr")
     ap.add_argument("--tau-run", type=int, default=0,
                     help="long run of this many sweeps; prints the workload's τ_int JSON and exits")
     ap.add_argument("--chains", type=int, default=None,

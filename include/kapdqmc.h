@@ -207,6 +207,14 @@ int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32
  * reference (which is FP64 only).  Call before kdq_init / kdq_phy_update. */
 int kdq_set_precision(kdq_handle* h, int32_t mode);
 
+/* Per-stage clock counts of the sweep (SM clock cycles, summed over chains):
+ * cycles[0] wraps, [1] proposals and updates, [2] measurements, [3] block
+ * products of the stabilisation chain, [4] Householder QR, [5] G recompute
+ * (cycles has 8 entries).  Enabling resets the counters and adds a barrier
+ * per stage.  No counterpart in the reference (which has no tracing). */
+int kdq_enable_phase_timing(kdq_handle* h, int32_t enable);
+int kdq_get_phase_cycles(kdq_handle* h, double* cycles);
+
 /* Replay each sweep's 2 (n_nodes-1) block launches from a captured CUDA
  * graph (default on) or launch them one by one (enable = 0).  The graph is
  * re-captured whenever the launch parameters change.  No counterpart in the

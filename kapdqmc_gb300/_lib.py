@@ -35,6 +35,8 @@ _SIGS = {
     "kdq_stream": (C.c_void_p, [C.c_void_p]),
     "kdq_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
     "kdq_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kdq_enable_phase_timing": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kdq_get_phase_cycles": (C.c_int, [C.c_void_p, C.c_void_p]),
     "kdq_grover_det": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
                                  C.c_void_p, C.c_int32]),
     "kdq_grover_det_chains": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),

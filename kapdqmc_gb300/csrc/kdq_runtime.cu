@@ -61,6 +61,7 @@ struct kdq_handle {
   int precision = KDQ_PREC_FP64;
   size_t esz_w = 16;       // bytes per working-precision G element
   DevBuf Yw, Y2w, Gd, eKw, eKinvw, HalfeKw, HalfeKinvw;
+  DevBuf phase;            // per-chain phase clocks when enabled
   // outputs
   DevBuf obs, acc_log, drift, tape_k, tape_u;
   // Grover-determinant workspace
@@ -815,6 +816,34 @@ int kdq_set_precision(kdq_handle* h, int32_t mode) {
   KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
   h->precision = mode;
   h->initialised = false;
+  return KDQ_OK;
+}
+
+int kdq_enable_phase_timing(kdq_handle* h, int32_t enable) {
+  if (!h) return KDQ_ERR_ARG;
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (enable) {
+    KDQ_CUDA(h, h->phase.alloc((size_t)h->nchains * 8 * sizeof(unsigned long long)));
+    KDQ_CUDA(h, cudaMemset(h->phase.p, 0, h->phase.bytes));
+    h->P.phase = h->phase.as<unsigned long long>();
+  } else {
+    h->phase.alloc(0);
+    h->P.phase = nullptr;
+  }
+  return KDQ_OK;
+}
+
+int kdq_get_phase_cycles(kdq_handle* h, double* cycles) {
+  if (!h || !cycles) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  if (!h->P.phase) return fail(h, KDQ_ERR_STATE, "phase timing is not enabled");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<unsigned long long> v((size_t)h->nchains * 8);
+  KDQ_CUDA(h, cudaMemcpy(v.data(), h->phase.p, v.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  for (int q = 0; q < 8; ++q) cycles[q] = 0.0;
+  for (int c = 0; c < h->nchains; ++c)
+    for (int q = 0; q < 8; ++q) cycles[q] += (double)v[(size_t)c * 8 + q];
   return KDQ_OK;
 }
 

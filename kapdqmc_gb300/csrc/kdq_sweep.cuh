@@ -48,7 +48,8 @@ template <int MAXRM, class T> struct Tiles;
 template <class T> struct Tiles<1, T> { static constexpr int SM = 1, SN = 4, TM = 1, TN = 4; };
 template <> struct Tiles<3, double> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 4; };
 template <> struct Tiles<3, cd> { static constexpr int SM = 2, SN = 8, TM = 2, TN = 4; };
-template <class T> struct Tiles<6, T> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 6; };
+template <class T> struct Tiles<6, T> { static constexpr int SM = 3, SN = 6, TM = 3, TN = 6; };
+template <> struct Tiles<6, cd> { static constexpr int SM = 2, SN = 6, TM = 2, TN = 6; };
 template <> struct Tiles<3, float> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 4; };
 template <> struct Tiles<3, cf> { static constexpr int SM = 2, SN = 8, TM = 2, TN = 4; };
 
@@ -62,6 +63,28 @@ __device__ inline void gemm_thin(int M, int N, int K, const TA* A, int lda, cons
                                  int ldc, const TS* rs = nullptr, const TS* cs = nullptr) {
   bgemm_t<Tiles<MAXRM, T>::TM, Tiles<MAXRM, T>::TN>(M, N, K, A, lda, B, ldb, C, ldc, rs, cs);
 }
+
+// ------------------------------------------------------------ phase timing
+// Optional per-chain clock counts of the sweep's phases (thread 0, between
+// barriers): 0 wraps, 1 proposals and updates, 2 measurements, 3 block
+// products of the stabilisation chain, 4 Householder QR, 5 G recompute.
+struct PhaseClock {
+  unsigned long long* acc;
+  long long t;
+  __device__ void start(unsigned long long* a) {
+    acc = a;
+    t = a ? clock64() : 0;
+  }
+  __device__ void lap(int phase) {
+    if (!acc) return;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const long long now = clock64();
+      acc[phase] += (unsigned long long)(now - t);
+      t = now;
+    }
+  }
+};
 
 // Per-CTA shared scratch (static part; the tape slice is dynamic); T is the
 // working type.
@@ -104,6 +127,30 @@ struct Ctx {
   const KW* HalfeK;
   const KW* HalfeKinv;
   const KT* Kmat;  // hopping matrix (observables, FP64)
+  PhaseClock& clk;
+};
+
+// Walks the elements e = tid, tid + nthreads, ... of a column-major M x N
+// matrix keeping (row, col) up to date without a division per element.
+struct Walk {
+  int e, i, j, di, dj, M, total;
+  __device__ Walk(int M_, int N_) : M(M_), total(M_ * N_) {
+    e = threadIdx.x;
+    i = e % M;
+    j = e / M;
+    di = blockDim.x % M;
+    dj = blockDim.x / M;
+  }
+  __device__ bool ok() const { return e < total; }
+  __device__ void next() {
+    e += blockDim.x;
+    i += di;
+    j += dj;
+    if (i >= M) {
+      i -= M;
+      ++j;
+    }
+  }
 };
 
 // ---------------------------------------------------------------- tables
@@ -168,10 +215,7 @@ template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void wrap_bwd_kv(Ctx<KIND, T, KT, TW, KW>& c, TW* G, TW* W, int lt) {
   const int N = c.P.Ns;
   slice_diag(c, lt, -1);
-  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
-    const int i = e % N, j = e / N;
-    G[e] = (c.sm.dvec[i] * G[e]) * c.sm.dinv[j];
-  }
+  for (Walk w(N, N); w.ok(); w.next()) G[w.e] = (c.sm.dvec[w.i] * G[w.e]) * c.sm.dinv[w.j];
   __syncthreads();
   gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, G, N, W, N);
   gemm_sq<MAXRM, TW>(N, N, N, W, N, c.eK, N, G, N);
@@ -214,8 +258,8 @@ __device__ void tv_rotate(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int j, int
   const TW* R = c.sm.dinv;
   const int* bx = P.bx + (size_t)j * nb;
   const int* by = P.by + (size_t)j * nb;
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int i = e % nb, ip = e / nb;
+  for (Walk w(nb, nb); w.ok(); w.next()) {
+    const int i = w.i, ip = w.j;
     const int x = bx[i], y = by[i], xp = bx[ip], yp = by[ip];
     const TW lp = L[2 * i], lm = L[2 * i + 1], rp = R[2 * ip], rm = R[2 * ip + 1];
     const TW g00 = G[x + (size_t)xp * N], g01 = G[x + (size_t)yp * N];
@@ -238,7 +282,7 @@ __device__ void tv_rotate(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int j, int
 // u' = G[:,S] r into shared memory while the other warps stage the rows
 // G[S,:]; then every thread applies G -= u' (E_S - G[S,:]) (Gupdate!,
 // src/public/Gupdate.jl:5-11).
-template <int KIND, class T, class KT, class TW, class KW>
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y, uint8_t* sfield,
                         uint8_t tk, double tu, int logpos, int par) {
   const SweepParams& P = c.P;
@@ -257,8 +301,14 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
       const cd Δ = reinterpret_cast<const cd*>(P.rtab)[(size_t)(lt - 1) * 16 + o * 4 + nv];
       const cd g = cvt<cd>(G[x + (size_t)x * N]);
       const cd pc = cd{1.0, 0.0} + Δ * (cd{1.0, 0.0} - g);
-      r00 = Δ / pc;
       p = abs2(pc) * P.gratio[o * 4 + nv];
+      if constexpr (std::is_same_v<T, TW>) {
+        r00 = Δ / pc;
+      } else if (tu < p) {   // only the G update uses r, in the working precision
+        const cf q = cf{(float)(Δ.x * pc.x + Δ.y * pc.y), (float)(Δ.y * pc.x - Δ.x * pc.y)};
+        const float inv = 1.0f / (float)abs2(pc);
+        r00 = cd{q.x * inv, q.y * inv};
+      }
     } else if constexpr (KIND == KDQ_TV) {
       // get_r!, src/tV/GreenMatrix.jl:76-89
       const double h = 0.70710678118654752440;
@@ -333,13 +383,45 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
     }
   }
   __syncthreads();
-  if (sm.accept[par]) {
-    for (int e = tid; e < N * N; e += blockDim.x) {
-      const int a = e % N, b = e / N;
-      TW v = G[e];
-      madd(v, -sm.ucol[0][a], sm.wrow[0][b]);
-      if constexpr (RK == 2) madd(v, -sm.ucol[1][a], sm.wrow[1][b]);
-      G[e] = v;
+  if (sm.accept[par] && std::is_same_v<T, TW>) {
+    // FP64: a flat walk over the elements keeps every lane of the FP64 pipe busy
+    for (Walk w(N, N); w.ok(); w.next()) {
+      TW v = G[w.e];
+      madd(v, -sm.ucol[0][w.i], sm.wrow[0][w.j]);
+      if constexpr (RK == 2) madd(v, -sm.ucol[1][w.i], sm.wrow[1][w.j]);
+      G[w.e] = v;
+    }
+    if (tid == 0) *sfield = (uint8_t)sm.newv;
+    __syncthreads();
+  } else if (sm.accept[par]) {
+    // FP32: memory latency, not arithmetic, bounds the update; warps own
+    // columns, lanes own rows (coalesced), -u' stays in registers across the
+    // columns and the row chunks are unrolled so their loads overlap
+    TW u0[MAXRM], u1[MAXRM];
+#pragma unroll
+    for (int r = 0; r < MAXRM; ++r) {
+      const int a = min(lane + 32 * r, N - 1);
+      u0[r] = -sm.ucol[0][a];
+      if constexpr (RK == 2) u1[r] = -sm.ucol[1][a];
+    }
+    const int nw = blockDim.x >> 5;
+    for (int b = warp; b < N; b += nw) {
+      TW* col = G + (size_t)b * N;
+      const TW w0 = sm.wrow[0][b];
+      TW w1;
+      if constexpr (RK == 2) w1 = sm.wrow[1][b];
+      TW v[MAXRM];
+#pragma unroll
+      for (int r = 0; r < MAXRM; ++r)
+        if (lane + 32 * r < N) v[r] = col[lane + 32 * r];
+#pragma unroll
+      for (int r = 0; r < MAXRM; ++r) {
+        if (lane + 32 * r < N) {
+          madd(v[r], u0[r], w0);
+          if constexpr (RK == 2) madd(v[r], u1[r], w1);
+          col[lane + 32 * r] = v[r];
+        }
+      }
     }
     if (tid == 0) *sfield = (uint8_t)sm.newv;
     __syncthreads();
@@ -377,7 +459,7 @@ __device__ void finish_tape(Ctx<KIND, T, KT, TW, KW>& c, int n) {
 }
 
 // All proposals of slice lt (tU, tUV) or of direction j of slice lt (tV).
-template <int KIND, class T, class KT, class TW, class KW>
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fwd) {
   const SweepParams& P = c.P;
   const int Nt = P.Nt, pf = P.n_field;
@@ -403,7 +485,7 @@ __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fw
     } else {
       x = P.bx[m]; y = P.by[m]; f = m;
     }
-    propose(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, m & 1);
+    propose<MAXRM>(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, m & 1);
   }
   if (threadIdx.x == 0) c.ctl->log_pos += n;
   finish_tape(c, n);
@@ -490,15 +572,14 @@ __device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, boo
   lu_solve(ns, N, c.Mss, c.piv, c.X);
   gemm_sq<MAXRM, T>(N, N, ns, BR, N, c.X, ns, c.Gd, N);
   double d2 = 0.0, n2 = 0.0;
-  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
-    const int i = e % N, j = e / N;
-    T g = zero<T>() - c.Gd[e];
-    if (i == j) g = g + one<T>();
+  for (Walk w(N, N); w.ok(); w.next()) {
+    T g = zero<T>() - c.Gd[w.e];
+    if (w.i == w.j) g = g + one<T>();
     if (drift) {
-      d2 += abs2(cvt<T>(c.G[e]) - g);
+      d2 += abs2(cvt<T>(c.G[w.e]) - g);
       n2 += abs2(g);
     }
-    c.G[e] = cvt<TW>(g);
+    c.G[w.e] = cvt<TW>(g);
   }
   if (drift) {
     d2 = block_sum(d2, c.sm.red);
@@ -541,9 +622,12 @@ __device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
     __syncthreads();
     src = c.Y;
   }
+  c.clk.lap(3);
   householder_q(N, ns, src, BRn, c.sm.wn, c.sm.red);
+  c.clk.lap(4);
   const T* BLn = P.BLs<T>(c.chain) + (size_t)k * fs;
   get_G<MAXRM>(c, BLn, BRn, true);
+  c.clk.lap(5);
   if (threadIdx.x == 0) c.ctl->idx = k + 1;
 }
 
@@ -579,13 +663,16 @@ __device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute
     A[col + (size_t)r * N] = conjg(cvt<T>(cur[e]));
   }
   __syncthreads();
+  c.clk.lap(3);
   householder_q(N, ns, A, Q, c.sm.wn, c.sm.red);
   for (size_t e = threadIdx.x; e < fs; e += blockDim.x) {
     const int r = e % ns, col = e / ns;
     BLk[e] = conjg(Q[col + (size_t)r * N]);
   }
   __syncthreads();
+  c.clk.lap(4);
   if (recompute) get_G<MAXRM>(c, BLk, P.BRs<T>(c.chain) + (size_t)(k - 1) * fs, drift);
+  c.clk.lap(5);
   if (threadIdx.x == 0) c.ctl->idx = k;
 }
 
@@ -816,7 +903,7 @@ __device__ void mul_slice(Ctx<KIND, T, KT, TW, KW>& c, TW* X, TW* W, int lt, con
     slice_diag(c, lt, +1, fields);   // dvec = D, dinv = 1 ./ D
     const TW* d = inv ? c.sm.dinv : c.sm.dvec;
     if (right && !inv) {          // X D eK
-      for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = X[e] * d[e / N];
+      for (Walk w(N, N); w.ok(); w.next()) X[w.e] = X[w.e] * d[w.j];
       __syncthreads();
       gemm_sq<MAXRM, TW>(N, N, N, X, N, c.eK, N, W, N);
     } else if (right) {           // X eKinv D^-1
@@ -824,7 +911,7 @@ __device__ void mul_slice(Ctx<KIND, T, KT, TW, KW>& c, TW* X, TW* W, int lt, con
     } else if (!inv) {            // D eK X
       gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, X, N, W, N, d, (const TW*)nullptr);
     } else {                      // eKinv D^-1 X
-      for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = d[e % N] * X[e];
+      for (Walk w(N, N); w.ok(); w.next()) X[w.e] = d[w.i] * X[w.e];
       __syncthreads();
       gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, X, N, W, N);
     }
@@ -898,13 +985,15 @@ __device__ void measure_fast(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
 // KDQ_MODE_BWD: backward slices node(k+1) .. node(k)+1, then the node.
 // MIXED selects the FP32 working precision (see the header of this file).
 template <int KIND, class T, class KT, int MAXRM, bool MIXED>
-__global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int mode, int k) {
+__global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, int mode, int k) {
   using TW = std::conditional_t<MIXED, typename low_t<T>::type, T>;
   using KW = std::conditional_t<MIXED, typename low_t<KT>::type, KT>;
   extern __shared__ double dyn_d[];
   __shared__ Smem<TW> sm;
   const int chain = blockIdx.x;
   const int N = P.Ns;
+  PhaseClock clk;
+  clk.start(P.phase ? P.phase + (size_t)chain * 8 : nullptr);
   const size_t cNN = (size_t)chain * P.sz_NN;
   const size_t cNn = (size_t)chain * P.sz_Nn;
   Ctx<KIND, T, KT, TW, KW> c{P,
@@ -929,7 +1018,8 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
                              static_cast<const KW*>(P.eKinv),
                              static_cast<const KW*>(P.HalfeK),
                              static_cast<const KW*>(P.HalfeKinv),
-                             static_cast<const KT*>(P.K)};
+                             static_cast<const KT*>(P.K),
+                             clk};
   if (mode == KDQ_MODE_INIT) {
     node_backward<MAXRM>(c, k, k == 1, false);
     return;
@@ -945,17 +1035,23 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
         gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, c.W1, N, c.G, N);
         for (int j = P.z - 1; j >= 0; --j) {
           tv_rotate(c, c.G, lt, j, +1);
-          update_layer(c, lt, j, true);
+          clk.lap(0);
+          update_layer<MAXRM>(c, lt, j, true);
+          clk.lap(1);
         }
       } else {
         wrap_fwd_kv<MAXRM>(c, c.G, c.W1, lt);
-        update_layer(c, lt, 0, true);
+        clk.lap(0);
+        update_layer<MAXRM>(c, lt, 0, true);
+        clk.lap(1);
       }
       if (rec) {
         if (P.record == 2) measure_fast<MAXRM>(c, lt);
         else measure<MAXRM>(c, lt);
+        clk.lap(2);
       }
     }
+    clk.lap(0);
     node_forward<MAXRM>(c, k);
   } else {
     // idx == k+1 while these slices run (src/tU/phy_update.jl:101-139)
@@ -964,24 +1060,32 @@ __global__ void __launch_bounds__(KDQ_THREADS) k_block(const SweepParams P, int 
     for (int lt = hi; lt > lo; --lt) {
       if constexpr (KIND == KDQ_TV) {
         for (int j = 0; j < P.z; ++j) {
-          update_layer(c, lt, j, false);
+          update_layer<MAXRM>(c, lt, j, false);
+          clk.lap(1);
           tv_rotate(c, c.G, lt, j, -1);
+          clk.lap(0);
         }
         gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, c.G, N, c.W1, N);
         gemm_sq<MAXRM, TW>(N, N, N, c.W1, N, c.eK, N, c.G, N);
+        clk.lap(0);
         if (rec) {
           if (P.record == 2) measure_fast<MAXRM>(c, lt - 1);
           else measure<MAXRM>(c, lt - 1);
+          clk.lap(2);
         }
       } else {
-        update_layer(c, lt, 0, false);
+        update_layer<MAXRM>(c, lt, 0, false);
+        clk.lap(1);
         if (rec) {
           if (P.record == 2) measure_fast<MAXRM>(c, lt);
           else measure<MAXRM>(c, lt);
+          clk.lap(2);
         }
         wrap_bwd_kv<MAXRM>(c, c.G, c.W1, lt);
+        clk.lap(0);
       }
     }
+    clk.lap(0);
     node_backward<MAXRM>(c, k, true, true);
     if (k == 1 && threadIdx.x == 0) {
       ChainCtl* ctl = c.ctl;
