@@ -378,6 +378,75 @@ __device__ void lu_factor(int n, T* M, int* piv, int* bad) {
   }
 }
 
+// In-place inverse of the n x n matrix M (ld n) by Gauss-Jordan elimination
+// with partial (row) pivoting; every elimination step is one parallel
+// rank-1 update of M, so the inverse costs n^3 multiply-adds at block-GEMM
+// parallelism.  f (n elements of shared memory) stages the pivot column;
+// cols (n ints) records the row swaps.  *bad is set on a zero pivot.
+template <class T>
+__device__ void gj_inverse(int n, T* M, T* f, int* swaps, int* bad) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ int sp;
+  for (int k = 0; k < n; ++k) {
+    if (tid < 32) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + tid; i < n; i += 32) {
+        const double v = abs2(M[i + (size_t)k * n]);
+        if (v > best) { best = v; bi = i; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (tid == 0) {
+        sp = bi;
+        swaps[k] = bi;
+        if (!(best > 0.0)) *bad = 1;
+      }
+    }
+    __syncthreads();
+    const int p = sp;
+    if (p != k)
+      for (int c = tid; c < n; c += nt) {
+        const T tmp = M[k + (size_t)c * n];
+        M[k + (size_t)c * n] = M[p + (size_t)c * n];
+        M[p + (size_t)c * n] = tmp;
+      }
+    __syncthreads();
+    // scale the pivot row: M[k,k] <- 1, row k <- row k / pivot
+    const T inv = one<T>() / M[k + (size_t)k * n];
+    __syncthreads();   // every thread has read the pivot before row k changes
+    for (int c = tid; c < n; c += nt) {
+      const T v = c == k ? one<T>() : M[k + (size_t)c * n];
+      M[k + (size_t)c * n] = v * inv;
+    }
+    for (int i = tid; i < n; i += nt) f[i] = i == k ? zero<T>() : M[i + (size_t)k * n];
+    __syncthreads();
+    // eliminate column k from every other row: M[i,:] -= f_i M[k,:] (M[i,k] <- -f_i / pivot)
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e % n, c = e / n;
+      if (i == k) continue;
+      const T base = c == k ? zero<T>() : M[e];
+      M[e] = base - f[i] * M[k + (size_t)c * n];
+    }
+    __syncthreads();
+  }
+  // undo the row swaps as column swaps, last first
+  for (int k = n - 1; k >= 0; --k) {
+    const int p = swaps[k];
+    if (p != k)
+      for (int r = tid; r < n; r += nt) {
+        const T tmp = M[r + (size_t)k * n];
+        M[r + (size_t)k * n] = M[r + (size_t)p * n];
+        M[r + (size_t)p * n] = tmp;
+      }
+    __syncthreads();
+  }
+}
+
 // X (n x N, ld n) <- M^{-1} X using the LU factors of lu_factor (?getrs).
 // Each thread solves whole columns, so no synchronisation is needed inside.
 template <class T>

@@ -564,12 +564,13 @@ __device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, boo
   const int N = c.P.Ns, ns = N / 2;
   gemm_thin<MAXRM, T>(ns, ns, N, BL, ns, BR, N, c.Mss, ns);
   __shared__ int bad;
+  __shared__ T fcol[KDQ_MAX_NS / 2];
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
-  lu_factor(ns, c.Mss, c.piv, &bad);
-  for (int e = threadIdx.x; e < ns * N; e += blockDim.x) c.X[e] = BL[e];
-  __syncthreads();
-  lu_solve(ns, N, c.Mss, c.piv, c.X);
+  // (BL BR)^-1 by Gauss-Jordan, then X = (BL BR)^-1 BL and BR X as block GEMMs
+  // (the reference solves with getrf + getrs; the product is the same)
+  gj_inverse(ns, c.Mss, fcol, c.piv, &bad);
+  gemm_thin<MAXRM, T>(ns, N, ns, c.Mss, ns, BL, ns, c.X, ns);
   gemm_sq<MAXRM, T>(N, N, ns, BR, N, c.X, ns, c.Gd, N);
   double d2 = 0.0, n2 = 0.0;
   for (Walk w(N, N); w.ok(); w.next()) {
