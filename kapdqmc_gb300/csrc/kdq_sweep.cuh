@@ -303,7 +303,7 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
       const cd pc = cd{1.0, 0.0} + Δ * (cd{1.0, 0.0} - g);
       p = abs2(pc) * P.gratio[o * 4 + nv];
       if constexpr (std::is_same_v<T, TW>) {
-        r00 = Δ / pc;
+        if (tu < p) r00 = Δ / pc;
       } else if (tu < p) {   // only the G update uses r, in the working precision
         const cf q = cf{(float)(Δ.x * pc.x + Δ.y * pc.y), (float)(Δ.y * pc.x - Δ.x * pc.y)};
         const float inv = 1.0f / (float)abs2(pc);
@@ -324,12 +324,15 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
       a00 += 1.0;
       a11 += 1.0;
       const double det = a00 * a11 - a01 * a10;
-      const double i00 = a11 / det, i01 = -a01 / det, i10 = -a10 / det, i11 = a00 / det;
-      r00 = from_real<T>(i00 * d00 + i01 * d10);
-      r01 = from_real<T>(i00 * d01 + i01 * d11);
-      r10 = from_real<T>(i10 * d00 + i11 * d10);
-      r11 = from_real<T>(i10 * d01 + i11 * d11);
       p = det * P.gratio[o * 4 + nv];
+      if (tu < p) {   // r = r^-1 Δ, needed only for the update
+        const double rd = 1.0 / det;
+        const double i00 = a11 * rd, i01 = -a01 * rd, i10 = -a10 * rd, i11 = a00 * rd;
+        r00 = from_real<T>(i00 * d00 + i01 * d10);
+        r01 = from_real<T>(i00 * d01 + i01 * d11);
+        r10 = from_real<T>(i10 * d00 + i11 * d10);
+        r11 = from_real<T>(i10 * d01 + i11 * d11);
+      }
     } else {
       // get_r!, src/tUV/GreenMatrix.jl:73-89; weight src/tUV/phy_update.jl:193-197
       const T* t2 = reinterpret_cast<const T*>(P.rtab) + (size_t)(o * 4 + nv) * 2;
@@ -340,13 +343,14 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
       a00 = a00 + one<T>();
       a11 = a11 + one<T>();
       const T det = a00 * a11 - a01 * a10;
-      const T i00 = a11 / det, i01 = (zero<T>() - a01) / det;
-      const T i10 = (zero<T>() - a10) / det, i11 = a00 / det;
-      r00 = i00 * t2[0];
-      r01 = i01 * t2[1];
-      r10 = i10 * t2[0];
-      r11 = i11 * t2[1];
       p = abs2(det) * P.gratio[o * 4 + nv] * P.xtab[o * 4 + nv];
+      if (tu < p) {   // r = r^-1 Δ, needed only for the update
+        const T rd = one<T>() / det;
+        r00 = (a11 * rd) * t2[0];
+        r01 = ((zero<T>() - a01) * rd) * t2[1];
+        r10 = ((zero<T>() - a10) * rd) * t2[0];
+        r11 = (a00 * rd) * t2[1];
+      }
     }
     int acc = tu < p;
     if (!isfinite(p)) {
@@ -384,7 +388,8 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
   }
   __syncthreads();
   if (sm.accept[par] && std::is_same_v<T, TW>) {
-    // FP64: a flat walk over the elements keeps every lane of the FP64 pipe busy
+    // FP64: a flat walk over the elements keeps every lane of the FP64 pipe
+    // busy; four elements per step so that their loads overlap
     for (Walk w(N, N); w.ok(); w.next()) {
       TW v = G[w.e];
       madd(v, -sm.ucol[0][w.i], sm.wrow[0][w.j]);
