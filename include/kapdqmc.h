@@ -177,6 +177,14 @@ int kdq_grover_det(const double* G, int32_t Ns, int32_t g_complex, int32_t npair
  * current time slice. */
 int kdq_grover_det_chains(kdq_handle* h, const int32_t* index, int32_t nA, double* det);
 
+/* Keep a copy of every chain's equal-time G at the middle slice tau = Nt/2
+ * (the G0 of the reference's G4!, src/public/Gupdate.jl:159-212) whenever a
+ * recording sweep passes it, and evaluate the Grover determinant of the chain
+ * pairs (0,1), (2,3), ... on those copies: the independent-replica estimator
+ * of e^{-S2} at the middle of the projection. */
+int kdq_keep_middle_green(kdq_handle* h, int32_t enable);
+int kdq_grover_det_middle(kdq_handle* h, const int32_t* index, int32_t nA, double* det);
+
 /* Allocation-free form of kdq_grover_det, for callers that must not call
  * cudaMalloc (work recorded into a CUDA graph or run where a device
  * synchronisation is unaffordable, and processes whose free device memory is

@@ -40,6 +40,8 @@ _SIGS = {
     "kdq_grover_det": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
                                  C.c_void_p, C.c_int32]),
     "kdq_grover_det_chains": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "kdq_keep_middle_green": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kdq_grover_det_middle": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "kdq_grover_det_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                          C.c_int32, C.c_void_p, C.c_void_p]),
 }

@@ -92,6 +92,7 @@ struct SweepParams {
   double* drift;
   int drift_cap;
   unsigned long long* phase;    // optional per-chain phase clocks (8 per chain), or NULL
+  void* gmid;                   // optional per-chain FP64 G at tau = Nt/2 (N x N), or NULL
 
   template <class T> __host__ __device__ T* BLs(int c) const { return static_cast<T*>(BLs_) + (size_t)c * sz_chainB; }
   template <class T> __host__ __device__ T* BRs(int c) const { return static_cast<T*>(BRs_) + (size_t)c * sz_chainB; }

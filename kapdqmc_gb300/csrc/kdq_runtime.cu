@@ -62,6 +62,7 @@ struct kdq_handle {
   size_t esz_w = 16;       // bytes per working-precision G element
   DevBuf Yw, Y2w, Gd, eKw, eKinvw, HalfeKw, HalfeKinvw;
   DevBuf phase;            // per-chain phase clocks when enabled
+  DevBuf gmid;             // per-chain G at tau = Nt/2 when enabled
   // outputs
   DevBuf obs, acc_log, drift, tape_k, tape_u;
   // Grover-determinant workspace
@@ -909,6 +910,45 @@ int kdq_grover_det(const double* G, int32_t Ns, int32_t g_complex, int32_t npair
                               dDet.as<double>(), nullptr)) ||
       (e = cudaMemcpy(det, dDet.p, (size_t)2 * npairs * sizeof(double), cudaMemcpyDeviceToHost)))
     return set_err(KDQ_ERR_CUDA, cudaGetErrorString(e));
+  return KDQ_OK;
+}
+
+int kdq_keep_middle_green(kdq_handle* h, int32_t enable) {
+  if (!h) return KDQ_ERR_ARG;
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (enable) {
+    const size_t b = (size_t)h->nchains * h->Ns * h->Ns * h->esz;
+    if (h->gmid.bytes != b) KDQ_CUDA(h, h->gmid.alloc(b));
+    KDQ_CUDA(h, cudaMemset(h->gmid.p, 0, b));
+    h->P.gmid = h->gmid.p;
+  } else {
+    h->gmid.alloc(0);
+    h->P.gmid = nullptr;
+  }
+  return KDQ_OK;
+}
+
+int kdq_grover_det_middle(kdq_handle* h, const int32_t* index, int32_t nA, double* det) {
+  if (!h || !det) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  if (!h->P.gmid) return fail(h, KDQ_ERR_STATE, "kdq_keep_middle_green is not enabled");
+  std::string why;
+  if (check_region(index, nA, h->Ns, why)) return fail(h, KDQ_ERR_ARG, why);
+  const int npairs = h->nchains / 2;
+  if (npairs == 0) return fail(h, KDQ_ERR_ARG, "need at least two chains");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  const size_t sb = kdq::grover_scratch_bytes(nA, npairs, h->gc);
+  if (h->gr_scratch.bytes < sb) KDQ_CUDA(h, h->gr_scratch.alloc(sb));
+  if (h->gr_piv.bytes < (size_t)npairs * nA * sizeof(int)) KDQ_CUDA(h, h->gr_piv.alloc((size_t)npairs * nA * sizeof(int)));
+  if (h->gr_index.bytes < (size_t)nA * sizeof(int)) KDQ_CUDA(h, h->gr_index.alloc((size_t)nA * sizeof(int)));
+  if (h->gr_det.bytes < (size_t)2 * npairs * sizeof(double)) KDQ_CUDA(h, h->gr_det.alloc((size_t)2 * npairs * sizeof(double)));
+  std::vector<int> idx0(nA);
+  for (int i = 0; i < nA; ++i) idx0[i] = index[i] - 1;
+  KDQ_CUDA(h, cudaMemcpyAsync(h->gr_index.p, idx0.data(), (size_t)nA * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  KDQ_CUDA(h, kdq::launch_grover(h->gmid.p, h->Ns, h->gc, h->gr_index.as<int>(), nA, npairs, h->gr_scratch.p,
+                                 h->gr_piv.as<int>(), h->gr_det.as<double>(), h->stream));
+  KDQ_CUDA(h, cudaMemcpyAsync(det, h->gr_det.p, (size_t)2 * npairs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
   return KDQ_OK;
 }
 

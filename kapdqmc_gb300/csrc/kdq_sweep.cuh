@@ -683,6 +683,18 @@ __device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute
 }
 
 // ------------------------------------------------------------ measurement
+// At t0 = Nt/2 the current G is the equal-time Green's function at the
+// middle of the projection, which the Rényi-2 Grover determinant of replica
+// pairs is evaluated on; keep an FP64 copy when the caller asked for it.
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void keep_middle(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
+  const SweepParams& P = c.P;
+  if (!P.gmid || 2 * t0 != P.Nt) return;
+  T* dst = static_cast<T*>(P.gmid) + (size_t)c.chain * P.sz_NN;
+  for (int e = threadIdx.x; e < P.Ns * P.Ns; e += blockDim.x) dst[e] = cvt<T>(c.G[e]);
+  __syncthreads();
+}
+
 __device__ inline double re_prod(double k, double g) { return k * g; }
 __device__ inline double re_prod(double k, cd g) { return k * g.x; }
 __device__ inline double re_prod(cd k, cd g) { return k.x * g.x - k.y * g.y; }
@@ -700,6 +712,7 @@ __device__ void observables(Ctx<KIND, T, KT, TW, KW>& c, const TW* G0);
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void measure(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
   const SweepParams& P = c.P;
+  keep_middle(c, t0);
   const int N = P.Ns, Nt = P.Nt, half = Nt / 2;
   TW* G0 = c.W2;
   TW* W = c.W1;
@@ -929,6 +942,7 @@ __device__ void mul_slice(Ctx<KIND, T, KT, TW, KW>& c, TW* X, TW* W, int lt, con
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void measure_fast(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
   const SweepParams& P = c.P;
+  keep_middle(c, t0);
   const int N = P.Ns, half = P.Nt / 2, nf = P.n_field;
   TW* L = static_cast<TW*>(P.Lm) + (size_t)c.chain * P.sz_NN;
   TW* R = static_cast<TW*>(P.Rm) + (size_t)c.chain * P.sz_NN;

@@ -222,6 +222,17 @@ class Sweeper:
         self._ck(self.lib.kdq_grover_det_chains(self.h, idx.ctypes.data, idx.size, out.ctypes.data))
         return out.view(np.complex128)
 
+    def keep_middle_green(self, enable: bool = True):
+        """Keep each chain's G at tau = Nt/2 during recording sweeps."""
+        self._ck(self.lib.kdq_keep_middle_green(self.h, int(bool(enable))))
+
+    def grover_det_middle(self, index):
+        """Grover determinants of the chain pairs on their G at tau = Nt/2."""
+        idx = np.ascontiguousarray(np.asarray(index, dtype=np.int32))
+        out = np.empty(2 * (self.nchains // 2))
+        self._ck(self.lib.kdq_grover_det_middle(self.h, idx.ctypes.data, idx.size, out.ctypes.data))
+        return out.view(np.complex128)
+
     def drift(self, sweeps: int):
         n = sweeps * 2 * (len(self.model.nodes) - 1)
         out = np.empty(self.nchains * n)

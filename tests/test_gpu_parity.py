@@ -215,3 +215,35 @@ def test_graph_replay_equals_direct_launches():
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][2], out[1][2])
     np.testing.assert_array_equal(out[0][3], out[1][3])
+
+
+def test_grover_det_at_middle_slice():
+    """Pairs of chains on their G at tau = Nt/2, as the oracle holds it when the
+    sweep passes the middle slice (the last pass is the backward one)."""
+    model = cases.tuv_square()
+    fields = np.stack([Initial_s(model, 60 + c) for c in range(4)])
+    index = list(range(1, 9))
+    seed = 13
+    with Sweeper(model, 4) as sw:
+        sw.keep_middle_green(True)
+        sw.set_fields(fields)
+        sw.set_rng(seed)
+        sw.phy_update(1, 2)
+        dets = sw.grover_det_middle(index)
+    mids = []
+    for c in range(4):
+        n = O.proposals_per_sweep(model)
+        k, u = philox.tape(seed, c, 0, n)
+        sw_o = O._TUVSweep(model, fields[c], O.Tape(k, u), True)
+        held = {}
+        orig = sw_o.measure
+
+        def grab(t0, _orig=orig, _held=held):
+            if 2 * t0 == model.Nt:
+                _held["G"] = sw_o.G.copy()
+            return _orig(t0)
+        sw_o.measure = grab
+        sw_o.run(1)
+        mids.append(held["G"])
+    want = [O.grover_det(mids[0], mids[1], index), O.grover_det(mids[2], mids[3], index)]
+    np.testing.assert_allclose(dets, want, rtol=1e-8, atol=1e-12)
