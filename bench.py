@@ -401,9 +401,9 @@ def run_gpu(args):
     roof = {"bound": "fp64", "pipe": pipe, "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
-            "traffic": traffic_per_launch() if WL is WORKLOADS["c2"] else None,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean over every k_block "
-                              "launch of the same workload (profiles/k_block_tv6x6_launches.md)",
+            "traffic": traffic_per_launch() if WL is WORKLOADS["c2"] and PRECISION == "fp64" else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean over the sweep's "
+                              "k_block launches of the same workload (profiles/k_block_tv6x6_launches.md)",
             "flops_per_launch": flops_per_launch,
             "flops_per_chain_sweep": fl}
     if PRECISION == "mixed":
