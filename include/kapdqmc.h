@@ -152,6 +152,18 @@ int kdq_get_green(kdq_handle* h, int32_t chain, double* G, size_t len);
 /* Statistics of the last kdq_phy_update / kdq_sweep call. */
 int kdq_get_stats(kdq_handle* h, kdq_stats* st);
 
+/* Log-weight of each chain's current fields: logdet[c] = log|det(P^H B(Theta,0) P)|
+ * with B(Theta,0) the product of all slice matrices, and phase[2c], phase[2c+1]
+ * = det/|det| (re, im), as of the last G recompute (the end of kdq_init and of
+ * every sweep).  The stabilised B chains keep the log|det| of the triangular
+ * factors the QR steps drop; the reference discards them (src/tU/phy_update.jl:
+ * 85-86,133-134), so this has no counterpart there.  The full configuration
+ * weight adds the local factors: t-U and complex t-UV |det|^2 prod gamma, t-V
+ * det prod gamma, real t-UV det^2 prod gamma e^{-(a+1) eta}
+ * (the ratios of src/tU/phy_update.jl:261, src/tV/phy_update.jl:196-199,
+ * src/tUV/phy_update.jl:192-197).  len counts chains. */
+int kdq_get_log_det(kdq_handle* h, double* logdet, double* phase, size_t len);
+
 /* Debug record of accept decisions (1 byte per proposal, chain-major, in
  * tape order) of the next calls; enable before kdq_phy_update.  Replaces the
  * reference's commented-out checks (src/tV/phy_update.jl:74-90). */

@@ -32,6 +32,7 @@ _SIGS = {
     "kdq_enable_accept_log": (C.c_int, [C.c_void_p, C.c_size_t]),
     "kdq_get_accept_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "kdq_get_drift": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kdq_get_log_det": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
     "kdq_stream": (C.c_void_p, [C.c_void_p]),
     "kdq_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
     "kdq_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),

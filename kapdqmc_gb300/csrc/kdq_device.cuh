@@ -278,10 +278,16 @@ __device__ void bgemm_t(int M, int N, int K, const TA* __restrict__ A, int lda,
 // H = I - w w^H * (2 / w^H w) with w = x + e^{i arg x0} |x| e1 (Householder
 // 1958; the LAPACK ?geqrf + ?orgqr pair restated with Hermitian reflectors).
 // Scratch: wn (n doubles: 2/(w^H w)), red (>= 32 doubles) in shared memory.
+// The discarded triangle has R_jj = -e^{i arg x0} |x|; when given, log_out and
+// phase_out receive sum_j log|R_jj| and prod_j R_jj/|R_jj| (the log-weight
+// of the stabilised B chain).
 template <class T>
-__device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red) {
+__device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red,
+                              double* log_out = nullptr, cd* phase_out = nullptr) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  double lgs = 0.0;          // sum of log |R_jj| (thread 0)
+  cd phs = mkc(1.0, 0.0);    // product of R_jj / |R_jj| (thread 0)
   for (int j = 0; j < n; ++j) {
     T* x = Y + (size_t)j * N;
     double s = 0.0;
@@ -296,6 +302,8 @@ __device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red)
       double ww = 2.0 * nrm * (nrm + aa);     // w^H w
       wn[j] = ww > 0.0 ? 2.0 / ww : 0.0;
       x[j] = wj;
+      lgs += log(nrm);             // R_jj = -ph * nrm
+      phs = phs * (-cvt<cd>(ph));
     }
     __syncthreads();
     // trailing columns c > j: A[:,c] -= (2/ww) w (w^H A[:,c])
@@ -326,6 +334,10 @@ __device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red)
       for (int i = j + lane; i < N; i += 32) q[i] = q[i] - x[i] * t;
     }
     __syncthreads();
+  }
+  if (tid == 0) {
+    if (log_out) *log_out = lgs;
+    if (phase_out) *phase_out = phs;
   }
 }
 
@@ -382,11 +394,15 @@ __device__ void lu_factor(int n, T* M, int* piv, int* bad) {
 // with partial (row) pivoting; every elimination step is one parallel
 // rank-1 update of M, so the inverse costs n^3 multiply-adds at block-GEMM
 // parallelism.  f (n elements of shared memory) stages the pivot column;
-// cols (n ints) records the row swaps.  *bad is set on a zero pivot.
+// cols (n ints) records the row swaps.  *bad is set on a zero pivot.  When
+// given, log_out and phase_out receive log|det M| and det M / |det M|.
 template <class T>
-__device__ void gj_inverse(int n, T* M, T* f, int* swaps, int* bad) {
+__device__ void gj_inverse(int n, T* M, T* f, int* swaps, int* bad, double* log_out = nullptr,
+                           cd* phase_out = nullptr) {
   const int tid = threadIdx.x, nt = blockDim.x;
   __shared__ int sp;
+  double lgs = 0.0;          // log |det M| (thread 0)
+  cd phs = mkc(1.0, 0.0);    // det M / |det M| (thread 0)
   for (int k = 0; k < n; ++k) {
     if (tid < 32) {
       double best = -1.0;
@@ -418,6 +434,13 @@ __device__ void gj_inverse(int n, T* M, T* f, int* swaps, int* bad) {
     __syncthreads();
     // scale the pivot row: M[k,k] <- 1, row k <- row k / pivot
     const T inv = one<T>() / M[k + (size_t)k * n];
+    if (tid == 0) {    // det M = (-1)^(row swaps) * product of the pivots
+      const cd pv = cvt<cd>(M[k + (size_t)k * n]);
+      const double a = sqrt(abs2(pv));
+      lgs += log(a);
+      phs = phs * (a > 0.0 ? pv / a : mkc(1.0, 0.0));
+      if (p != k) phs = -phs;
+    }
     __syncthreads();   // every thread has read the pivot before row k changes
     for (int c = tid; c < n; c += nt) {
       const T v = c == k ? one<T>() : M[k + (size_t)c * n];
@@ -444,6 +467,10 @@ __device__ void gj_inverse(int n, T* M, T* f, int* swaps, int* bad) {
         M[r + (size_t)p * n] = tmp;
       }
     __syncthreads();
+  }
+  if (tid == 0) {
+    if (log_out) *log_out = lgs;
+    if (phase_out) *phase_out = phs;
   }
 }
 

@@ -30,6 +30,8 @@ struct ChainCtl {
   int meas_n;           // slice factors held in the fast-measurement products
   double max_drift;
   double obs_acc[KDQ_MAX_OBS];
+  // log|det(P^H B(Theta,0) P)| and det/|det| of the fields at the last G recompute
+  double logdet, det_re, det_im;
 };
 
 struct SweepParams {
@@ -93,6 +95,10 @@ struct SweepParams {
   int drift_cap;
   unsigned long long* phase;    // optional per-chain phase clocks (8 per chain), or NULL
   void* gmid;                   // optional per-chain FP64 G at tau = Nt/2 (N x N), or NULL
+  // per chain, per node k (1-based) and side (0: BLs, 1: BRs): log|det| and det/|det|
+  // of the triangular factors dropped from that side's chain, at
+  // lw[((side * NN) + k - 1) * 3 + {0, 1, 2}] (log, re, im)
+  double* lw;
 
   template <class T> __host__ __device__ T* BLs(int c) const { return static_cast<T*>(BLs_) + (size_t)c * sz_chainB; }
   template <class T> __host__ __device__ T* BRs(int c) const { return static_cast<T*>(BRs_) + (size_t)c * sz_chainB; }

@@ -63,6 +63,7 @@ struct kdq_handle {
   DevBuf Yw, Y2w, Gd, eKw, eKinvw, HalfeKw, HalfeKinvw;
   DevBuf phase;            // per-chain phase clocks when enabled
   DevBuf gmid;             // per-chain G at tau = Nt/2 when enabled
+  DevBuf lw;               // per-chain log|det| of the dropped QR factors per node
   // outputs
   DevBuf obs, acc_log, drift, tape_k, tape_u;
   // Grover-determinant workspace
@@ -151,8 +152,15 @@ cudaError_t launch(kdq_handle* h, int mode, int k) {
 }
 
 __global__ void k_seed_chains(void* BRs, void* BLs, const void* Pt, const void* PtH, size_t fs,
-                              size_t chainB, int NN, size_t esz) {
-  // BRs[1] = Pt, BLs[NN] = Pt^H for chain blockIdx.x (byte copies)
+                              size_t chainB, int NN, size_t esz, double* lw) {
+  // BRs[1] = Pt, BLs[NN] = Pt^H for chain blockIdx.x (byte copies); no
+  // factor has been dropped from either end yet (log 0, phase 1)
+  if (threadIdx.x < 2) {
+    double* w = lw + ((size_t)blockIdx.x * 2 * NN + (threadIdx.x == 0 ? NN - 1 : NN)) * 3;
+    w[0] = 0.0;
+    w[1] = 1.0;
+    w[2] = 0.0;
+  }
   const size_t bytes = fs * esz;
   uint8_t* br = static_cast<uint8_t*>(BRs) + (size_t)blockIdx.x * chainB * esz;
   uint8_t* bl = static_cast<uint8_t*>(BLs) + ((size_t)blockIdx.x * chainB + (size_t)(NN - 1) * fs) * esz;
@@ -456,6 +464,8 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
   KDQ_CK(h->s.alloc(C * Nt * h->n_field));
   KDQ_CK(h->ctl.alloc(C * sizeof(ChainCtl)));
   KDQ_CK(cudaMemset(h->ctl.p, 0, C * sizeof(ChainCtl)));
+  KDQ_CK(h->lw.alloc(C * 6 * (size_t)h->NN * sizeof(double)));
+  KDQ_CK(cudaMemset(h->lw.p, 0, C * 6 * (size_t)h->NN * sizeof(double)));
   KDQ_CK(cudaMemset(h->G.p, 0, C * NNe * e));
   KDQ_CK(h->obs.alloc(8));
 
@@ -472,7 +482,7 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
   P.G = h->G.p; P.W1 = h->W1.p; P.W2 = h->W2.p; P.Y = h->Y.p; P.Y2 = h->Y2.p; P.Mss = h->Mss.p;
   P.Yw = h->Y.p; P.Y2w = h->Y2.p; P.Gd = h->W1.p;
   P.X = h->X.p; P.BLs_ = h->BLs.p; P.BRs_ = h->BRs.p; P.piv = h->piv.as<int>();
-  P.s = h->s.as<uint8_t>(); P.ctl = h->ctl.as<ChainCtl>();
+  P.s = h->s.as<uint8_t>(); P.ctl = h->ctl.as<ChainCtl>(); P.lw = h->lw.as<double>();
   P.sz_NN = NNe; P.sz_Nn = (size_t)N * ns; P.sz_nn = (size_t)ns * ns; P.sz_chainB = chainB;
   P.seed = 0; P.tape_k = nullptr; P.tape_u = nullptr; P.tape_len = 0;
   P.obs = h->obs.as<double>(); P.obs_cap = 0;
@@ -570,7 +580,7 @@ int kdq_init(kdq_handle* h) {
   KDQ_CUDA(h, cudaSetDevice(h->device));
   const size_t fs = (size_t)h->Ns * h->ns;
   k_seed_chains<<<h->nchains, 256, 0, h->stream>>>(h->BRs.p, h->BLs.p, h->Pt.p, h->PtH.p, fs,
-                                                   h->P.sz_chainB, h->NN, h->esz);
+                                                   h->P.sz_chainB, h->NN, h->esz, h->P.lw);
   KDQ_CUDA(h, cudaGetLastError());
   k_reset_ctl<<<(h->nchains + 127) / 128, 128, 0, h->stream>>>(h->ctl.as<ChainCtl>(), h->nchains, 1);
   KDQ_CUDA(h, cudaGetLastError());
@@ -868,6 +878,22 @@ int kdq_get_stats(kdq_handle* h, kdq_stats* st) {
     if (!(c.max_drift <= st->max_drift)) st->max_drift = c.max_drift;
   }
   st->seconds = h->last_seconds;
+  return KDQ_OK;
+}
+
+int kdq_get_log_det(kdq_handle* h, double* logdet, double* phase, size_t len) {
+  if (!h || !logdet || !phase) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  if (len != (size_t)h->nchains) return fail(h, KDQ_ERR_ARG, "len must equal the number of chains");
+  if (!h->initialised) return fail(h, KDQ_ERR_STATE, "kdq_init must precede kdq_get_log_det");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<ChainCtl> ctl(h->nchains);
+  KDQ_CUDA(h, cudaMemcpy(ctl.data(), h->ctl.p, ctl.size() * sizeof(ChainCtl), cudaMemcpyDeviceToHost));
+  for (size_t c = 0; c < ctl.size(); ++c) {
+    logdet[c] = ctl[c].logdet;
+    phase[2 * c] = ctl[c].det_re;
+    phase[2 * c + 1] = ctl[c].det_im;
+  }
   return KDQ_OK;
 }
 

@@ -562,10 +562,20 @@ __device__ TW* apply_slice_right(Ctx<KIND, T, KT, TW, KW>& c, TW* Z, TW* Z2, int
   return Z2;
 }
 
+// log|det| and phase of the triangular factors dropped from one side of a
+// chain's B-chain up to node k (side 0: BLs, 1: BRs).
+__device__ inline double* lw_at(const SweepParams& P, int chain, int side, int k) {
+  return P.lw + ((size_t)chain * 2 * P.NN + (size_t)side * P.NN + (k - 1)) * 3;
+}
+
 // G = I - BR (BL BR)^-1 BL (get_G!, src/public/Gupdate.jl:139-157); records
-// the drift against the wrapped G when `drift` is set.
+// the drift against the wrapped G when `drift` is set.  BL, BR are the
+// factors at node `node` (1-based): with the dropped factors of both sides
+// the pivots of (BL BR) give log|det(P^H B(Theta,0) P)| of the current
+// fields, kept in ChainCtl (no counterpart in the reference, which discards
+// the R factors).
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
-__device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, bool drift) {
+__device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, bool drift, int node) {
   const int N = c.P.Ns, ns = N / 2;
   gemm_thin<MAXRM, T>(ns, ns, N, BL, ns, BR, N, c.Mss, ns);
   __shared__ int bad;
@@ -574,7 +584,17 @@ __device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, boo
   __syncthreads();
   // (BL BR)^-1 by Gauss-Jordan, then X = (BL BR)^-1 BL and BR X as block GEMMs
   // (the reference solves with getrf + getrs; the product is the same)
-  gj_inverse(ns, c.Mss, fcol, c.piv, &bad);
+  __shared__ double mlg;   // written and read by thread 0 only
+  __shared__ cd mph;
+  gj_inverse(ns, c.Mss, fcol, c.piv, &bad, &mlg, &mph);
+  if (threadIdx.x == 0) {
+    const double* l = lw_at(c.P, c.chain, 0, node);
+    const double* r = lw_at(c.P, c.chain, 1, node);
+    const cd ph = mph * mkc(l[1], l[2]) * mkc(r[1], r[2]);
+    c.ctl->logdet = mlg + l[0] + r[0];
+    c.ctl->det_re = ph.x;
+    c.ctl->det_im = ph.y;
+  }
   gemm_thin<MAXRM, T>(ns, N, ns, c.Mss, ns, BL, ns, c.X, ns);
   gemm_sq<MAXRM, T>(N, N, ns, BR, N, c.X, ns, c.Gd, N);
   double d2 = 0.0, n2 = 0.0;
@@ -629,10 +649,20 @@ __device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
     src = c.Y;
   }
   c.clk.lap(3);
-  householder_q(N, ns, src, BRn, c.sm.wn, c.sm.red);
+  __shared__ double qlg;   // written and read by thread 0 only
+  __shared__ cd qph;
+  householder_q(N, ns, src, BRn, c.sm.wn, c.sm.red, &qlg, &qph);
+  if (threadIdx.x == 0) {   // B(tau_{k+1}, 0) P = BRs[k+1] R_{k+1} ... R_1
+    const double* a = lw_at(P, c.chain, 1, k);
+    double* b = lw_at(P, c.chain, 1, k + 1);
+    const cd ph = mkc(a[1], a[2]) * qph;
+    b[0] = a[0] + qlg;
+    b[1] = ph.x;
+    b[2] = ph.y;
+  }
   c.clk.lap(4);
   const T* BLn = P.BLs<T>(c.chain) + (size_t)k * fs;
-  get_G<MAXRM>(c, BLn, BRn, true);
+  get_G<MAXRM>(c, BLn, BRn, true, k + 1);
   c.clk.lap(5);
   if (threadIdx.x == 0) c.ctl->idx = k + 1;
 }
@@ -670,14 +700,24 @@ __device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute
   }
   __syncthreads();
   c.clk.lap(3);
-  householder_q(N, ns, A, Q, c.sm.wn, c.sm.red);
+  __shared__ double qlg;   // written and read by thread 0 only
+  __shared__ cd qph;
+  householder_q(N, ns, A, Q, c.sm.wn, c.sm.red, &qlg, &qph);
   for (size_t e = threadIdx.x; e < fs; e += blockDim.x) {
     const int r = e % ns, col = e / ns;
     BLk[e] = conjg(Q[col + (size_t)r * N]);
   }
+  if (threadIdx.x == 0) {   // P^H B(Theta, tau_k) = R_k^H ... BLs[k]: the factor is R^H
+    const double* a = lw_at(P, c.chain, 0, k + 1);
+    double* b = lw_at(P, c.chain, 0, k);
+    const cd ph = mkc(a[1], a[2]) * conjg(qph);
+    b[0] = a[0] + qlg;
+    b[1] = ph.x;
+    b[2] = ph.y;
+  }
   __syncthreads();
   c.clk.lap(4);
-  if (recompute) get_G<MAXRM>(c, BLk, P.BRs<T>(c.chain) + (size_t)(k - 1) * fs, drift);
+  if (recompute) get_G<MAXRM>(c, BLk, P.BRs<T>(c.chain) + (size_t)(k - 1) * fs, drift, k);
   c.clk.lap(5);
   if (threadIdx.x == 0) c.ctl->idx = k;
 }

@@ -17,7 +17,7 @@ import threading
 import numpy as np
 
 from . import _lib
-from .model import KIND_TU, KIND_TV
+from .model import KIND_TU, KIND_TUV, KIND_TV
 
 _LATTICE_ID = {"SQUARE45": 0, "SQUARE90": 1, "HoneyComb120": 2, "HoneyComb60": 3}
 _CSV_LOCKS: dict = {}
@@ -233,11 +233,43 @@ class Sweeper:
         self._ck(self.lib.kdq_grover_det_middle(self.h, idx.ctypes.data, idx.size, out.ctypes.data))
         return out.view(np.complex128)
 
+    def log_det(self):
+        """log|det(P^H B(Theta,0) P)| (n_chains,) and det/|det| (complex, n_chains,)
+        of every chain's current fields, from the stabilised B chains."""
+        ld = np.empty(self.nchains)
+        ph = np.empty(2 * self.nchains)
+        self._ck(self.lib.kdq_get_log_det(self.h, ld.ctypes.data, ph.ctypes.data, self.nchains))
+        return ld, ph[0::2] + 1j * ph[1::2]
+
+    def log_weight(self, fields=None):
+        """Full log-weight log|W(s)| of every chain (see ``log_weight``)."""
+        ld, _ = self.log_det()
+        s = self.get_fields() if fields is None else fields
+        return np.array([log_weight(self.model, s[c], ld[c]) for c in range(self.nchains)])
+
     def drift(self, sweeps: int):
         n = sweeps * 2 * (len(self.model.nodes) - 1)
         out = np.empty(self.nchains * n)
         self._ck(self.lib.kdq_get_drift(self.h, out.ctypes.data, out.size))
         return out.reshape(self.nchains, n)
+
+
+def log_weight(model, s, logdet: float) -> float:
+    """log|W(s)| of one configuration from log|det(P^H B(Theta,0) P)|.
+
+    W is the weight whose ratios the sweep accepts with: t-U and complex t-UV
+    |det|^2 prod gamma[s] (src/tU/phy_update.jl:260-261, src/tUV/GreenMatrix.jl:
+    73-89), t-V det prod gamma[s] (src/tV/GreenMatrix.jl:76-89 with
+    src/tV/phy_update.jl:196-199), real t-UV det^2 prod gamma[s] e^{-(a+1) eta[s]}
+    (src/tUV/phy_update.jl:192-197).
+    """
+    s = np.asarray(s).astype(np.int64).ravel() - 1
+    loc = float(np.log(np.asarray(model.γ, dtype=float))[s].sum())
+    if model.kind == KIND_TV:
+        return loc + logdet
+    if model.kind == KIND_TUV and not model.is_complex:
+        loc -= (model.a + 1.0) * float(np.asarray(model.η, dtype=float)[s].sum())
+    return loc + 2.0 * logdet
 
 
 def grover_det(G1, G2, index, device: int = 0):

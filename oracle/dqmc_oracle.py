@@ -611,6 +611,50 @@ def G_tau(model, s, τ: int):
     return np.eye(model.Ns) - BR @ np.linalg.inv(BL @ BR) @ BL
 
 
+def log_det(model, s):
+    """log|det(P^H B(Theta,0) P)| and det/|det| of the fields ``s``.
+
+    B(Theta,0) is the product of all Nt slice matrices (BM_F!, src/tU/
+    GreenMatrix.jl:10-27 and siblings), applied to P from the left with a QR
+    every BatchSize slices as in the reference's right chain
+    (src/tU/phy_update.jl:84-87); the log|R_jj| and phases of the dropped
+    triangles, which the reference discards, are summed here.
+    """
+    sw = _SWEEPS[model.kind](model, s, Tape([], []), False)
+    dt = sw.dtype
+    BR = model.Pt.astype(dt)
+    lg, ph = 0.0, 1.0 + 0j
+    cnt = 0
+    for i in range(1, model.Nt + 1):
+        BR = sw.B_left(i, BR)
+        cnt += 1
+        if cnt == model.BatchSize or i == model.Nt:
+            cnt = 0
+            Q, R = np.linalg.qr(BR)
+            d = np.diag(R)
+            lg += float(np.log(np.abs(d)).sum())
+            ph *= complex(np.prod(d / np.abs(d)))
+            BR = Q
+    sgn, lm = np.linalg.slogdet(model.Pt.conj().T.astype(dt) @ BR)
+    return lg + float(lm), complex(ph * sgn)
+
+
+def log_weight(model, s):
+    """log|W(s)|: the local HS weights times the determinant part whose ratios
+    the sweep accepts with (src/tU/phy_update.jl:260-261; src/tV/GreenMatrix.jl:
+    76-89 and src/tV/phy_update.jl:196-199; src/tUV/GreenMatrix.jl:73-89 and
+    src/tUV/phy_update.jl:192-197): |det|^2 for t-U and complex t-UV, det for
+    t-V, det^2 with e^{-(a+1) eta} for real t-UV."""
+    ld, _ = log_det(model, s)
+    idx = np.asarray(s).astype(np.int64).ravel() - 1
+    loc = 0.0
+    for i in idx:
+        loc += math.log(model.γ[i])
+        if model.kind == KIND_TUV and not model.is_complex:
+            loc -= (model.a + 1.0) * model.η[i]
+    return loc + (ld if model.kind == KIND_TV else 2.0 * ld)
+
+
 def grover_det(G1, G2, index):
     """det of the Grover matrix on region A: 2 G1 G2 - G1 - G2 + I.
 
