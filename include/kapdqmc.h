@@ -244,6 +244,39 @@ int kdq_set_graphs(kdq_handle* h, int32_t enable);
 /* CUDA stream (cudaStream_t) of the handle, for event timing by callers. */
 void* kdq_stream(kdq_handle* h);
 
+/* ---------------------------------------------------------------------
+ * Self-learning Monte Carlo (t-U).  No counterpart in the reference, which
+ * has local updates only (src/tU/phy_update.jl:256-267).
+ *
+ * Effective model: a periodic three-layer convolutional net (16 channels,
+ * 3x3 kernels, tanh) over the slice x site field s (Nt rows of Ns sites; a
+ * configuration is laid out as the sweep's fields, s[t * Ns + i] in 1..4),
+ * whose output summed over all positions, F(s), is fitted to the fermion part
+ * 2 log|det(P^H B(Theta,0) P)| of the log-weight (kdq_get_log_det).
+ * params: KDQ_CNN_NPARAM floats, in the order W1[16][4][3][3] (one-hot
+ * input channels), b1[16], W2[16][16][3][3], b2[16], W3[1][16][3][3], b3;
+ * the kernels compute with the bf16-rounded weights and FP32 accumulation.
+ * The three calls below are handle-free; errors go to kdq_last_error(NULL). */
+#define KDQ_CNN_PARAMS 3057
+
+/* F(s_b) of n_cfg configurations. */
+int kdq_cnn_forward(const uint8_t* fields, int32_t n_cfg, int32_t Nt, int32_t Ns, const float* params,
+                    double* F, int32_t device);
+
+/* Gradient of sum_b dF[b] F(s_b) with respect to params (KDQ_CNN_PARAMS floats). */
+int kdq_cnn_grad(const uint8_t* fields, const double* dF, int32_t n_cfg, int32_t Nt, int32_t Ns,
+                 const float* params, float* grad, int32_t device);
+
+/* Fits F to target[b] by minimising the mean squared error with Adam
+ * (beta 0.9, 0.999, eps 1e-8, learning rate lr) over `epochs` passes in
+ * shuffled mini-batches of `batch` configurations (shuffle seeded by seed);
+ * params is updated in place and loss_per_epoch (epochs doubles, may be NULL)
+ * receives each epoch's squared error averaged over its batches, each batch
+ * measured before its own update. */
+int kdq_cnn_train(const uint8_t* fields, const double* target, int32_t n_cfg, int32_t Nt, int32_t Ns,
+                  int32_t epochs, int32_t batch, float lr, uint64_t seed, float* params,
+                  double* loss_per_epoch, int32_t device);
+
 #ifdef __cplusplus
 }
 #endif
