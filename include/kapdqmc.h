@@ -229,8 +229,8 @@ int kdq_set_precision(kdq_handle* h, int32_t mode);
 
 /* Per-stage clock counts of the sweep (SM clock cycles, summed over chains):
  * cycles[0] wraps, [1] proposals and updates, [2] measurements, [3] block
- * products of the stabilisation chain, [4] Householder QR, [5] G recompute
- * (cycles has 8 entries).  Enabling resets the counters and adds a barrier
+ * products of the stabilisation chain, [4] Householder QR, [5] G recompute,
+ * [6] self-learning cluster moves (cycles has 8 entries).  Enabling resets the counters and adds a barrier
  * per stage.  No counterpart in the reference (which has no tracing). */
 int kdq_enable_phase_timing(kdq_handle* h, int32_t enable);
 int kdq_get_phase_cycles(kdq_handle* h, double* cycles);
@@ -276,6 +276,28 @@ int kdq_cnn_grad(const uint8_t* fields, const double* dF, int32_t n_cfg, int32_t
 int kdq_cnn_train(const uint8_t* fields, const double* target, int32_t n_cfg, int32_t Nt, int32_t Ns,
                   int32_t epochs, int32_t batch, float lr, uint64_t seed, float* params,
                   double* loss_per_epoch, int32_t device);
+
+/* Self-learning cluster moves in the t-U sweep.  After the local updates of
+ * every slice (both sweep directions) the sweep makes moves_per_slice moves:
+ * each picks cluster_len consecutive sites of the slice (random start, sites
+ * mod Ns), runs eff_steps single-site Metropolis steps on the effective
+ * weight exp(F(s)) prod gamma[s] of the model `params` (KDQ_CNN_PARAMS floats,
+ * evaluated incrementally in FP32 with bf16 weights), and accepts the changed
+ * sites S together with probability min(1, |det(I + Delta_S (I - G_SS))|^2
+ * exp(-(F(s') - F(s)))), the exact FP64 ratio of the full weight over the
+ * effective one; G then takes the rank-|S| form of Gupdate!
+ * (src/public/Gupdate.jl:5-11).  Random numbers come from Philox4x32-10 on
+ * the kdq_set_rng seed with a stream of their own, also when a tape is set.
+ * moves_per_slice = 0 turns the moves off.  Needs cluster_len <= min(32,
+ * Ns/2, Ns-8) and Nt >= 9. */
+int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice, int32_t cluster_len,
+                    int32_t eff_steps);
+
+/* Cluster moves of the last kdq_phy_update / kdq_sweep call, summed over
+ * chains: counts[0] proposed, counts[1] accepted, counts[2] proposals in
+ * which the effective-model chain changed no site (accepted trivially, not
+ * counted in counts[1]). */
+int kdq_get_slmc_stats(kdq_handle* h, int64_t* counts);
 
 #ifdef __cplusplus
 }

@@ -33,6 +33,8 @@ _SIGS = {
     "kdq_get_accept_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "kdq_get_drift": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "kdq_get_log_det": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kdq_slmc_enable": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "kdq_get_slmc_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
     "kdq_cnn_forward": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
     "kdq_cnn_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                C.c_int32]),

@@ -44,6 +44,15 @@ struct __align__(16) CnnW {
   float b3;
 };
 
+// Shared-memory bytes of the sweep's cluster moves for clusters of Lc sites:
+// the weights, the layer-1 window (7 rows x Lc+6 sites x 16 channels), the
+// layer-2 window (5 x Lc+4 x 16), the trial activations of the 3x3 and 5x5
+// neighbourhoods of a site and three index arrays of 32.
+__host__ __device__ inline size_t slmc_smem_bytes(int Lc) {
+  const size_t w = (sizeof(CnnW) + 15) & ~size_t(15);
+  return w + sizeof(float) * (7 * 16 * (size_t)(Lc + 6) + 5 * 16 * (size_t)(Lc + 4) + 144 + 400) + 3 * 32 * sizeof(int);
+}
+
 __device__ inline void load_cnn_weights(CnnW& w, const __nv_bfloat16* p) {
   for (int e = threadIdx.x; e < KDQ_CNN_CH * 36; e += blockDim.x) w.w1[e] = __bfloat162float(p[KDQ_CNN_OFF_W1 + e]);
   for (int e = threadIdx.x; e < KDQ_CNN_CH * 144; e += blockDim.x) {

@@ -20,6 +20,10 @@ cudaError_t launch_tv_mixed(const SweepParams& P, int mode, int k, int maxrm, in
                             cudaStream_t st);
 cudaError_t launch_tuv_mixed(const SweepParams& P, int mode, int k, int maxrm, bool g_complex,
                              int nchains, size_t dyn, cudaStream_t st);
+// Allow `dyn` bytes of dynamic shared memory for every t-U sweep kernel
+// (the self-learning cluster moves need more than the default 48 KB).
+cudaError_t prepare_tu(size_t dyn);
+cudaError_t prepare_tu_mixed(size_t dyn);
 // Grover determinants of npairs replica pairs (matrices 2p, 2p+1 of G).
 // scratch: npairs * 3 * nA^2 elements of the G type; pivs: npairs * nA.
 cudaError_t launch_grover(const void* G, int Ns, bool g_complex, const int* index, int nA, int npairs,

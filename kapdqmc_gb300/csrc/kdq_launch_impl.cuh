@@ -27,6 +27,20 @@ cudaError_t launch_tu_impl(const SweepParams& P, int mode, int k, int maxrm, boo
   return go_rm<KDQ_TU, cd, double, MIXED>(P, mode, k, maxrm, nch, dyn, st);
 }
 
+template <bool MIXED>
+cudaError_t prepare_tu_impl(size_t dyn) {
+  const int b = (int)dyn;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_block<KDQ_TU, cd, cd, 1, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)) ||
+      (e = cudaFuncSetAttribute(k_block<KDQ_TU, cd, cd, 3, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)) ||
+      (e = cudaFuncSetAttribute(k_block<KDQ_TU, cd, cd, 6, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)) ||
+      (e = cudaFuncSetAttribute(k_block<KDQ_TU, cd, double, 1, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)) ||
+      (e = cudaFuncSetAttribute(k_block<KDQ_TU, cd, double, 3, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)) ||
+      (e = cudaFuncSetAttribute(k_block<KDQ_TU, cd, double, 6, MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
+    return e;
+  return cudaSuccess;
+}
+
 // t-V: real sweep with 2x2 bond rotations
 template <bool MIXED>
 cudaError_t launch_tv_impl(const SweepParams& P, int mode, int k, int maxrm, int nch, size_t dyn,

@@ -32,6 +32,9 @@ struct ChainCtl {
   double obs_acc[KDQ_MAX_OBS];
   // log|det(P^H B(Theta,0) P)| and det/|det| of the fields at the last G recompute
   double logdet, det_re, det_im;
+  // self-learning cluster moves of the current call: proposed, accepted,
+  // proposals whose effective-model chain changed no site
+  long long slmc_prop, slmc_acc, slmc_noop;
 };
 
 struct SweepParams {
@@ -99,6 +102,13 @@ struct SweepParams {
   // of the triangular factors dropped from that side's chain, at
   // lw[((side * NN) + k - 1) * 3 + {0, 1, 2}] (log, re, im)
   double* lw;
+  // self-learning cluster moves (t-U): per slice visit, slmc_moves moves of
+  // slmc_steps effective-model Metropolis steps on slmc_len consecutive sites;
+  // slmc_prm holds the effective model's bf16 weights; the move's shared
+  // memory starts slmc_off bytes into the dynamic shared memory
+  int slmc_moves, slmc_len, slmc_steps;
+  size_t slmc_off;
+  const void* slmc_prm;
 
   template <class T> __host__ __device__ T* BLs(int c) const { return static_cast<T*>(BLs_) + (size_t)c * sz_chainB; }
   template <class T> __host__ __device__ T* BRs(int c) const { return static_cast<T*>(BRs_) + (size_t)c * sz_chainB; }

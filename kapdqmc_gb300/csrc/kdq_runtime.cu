@@ -1,6 +1,7 @@
 // Host runtime of libkapdqmc_gpu.so: handle lifecycle, model upload,
 // precomputed slice tables, launch sequencing of the sweep, and the C ABI
 // declared in include/kapdqmc.h.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -10,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "kdq_cnn.cuh"
 #include "kdq_launch.h"
 #include "kdq_params.h"
 
@@ -48,6 +50,7 @@ struct kdq_handle {
   int maxrm = 1;
   size_t esz = 16;   // bytes per G element
   size_t dyn = 0;    // dynamic shared memory per CTA
+  size_t dyn_base = 0;   // the tape slice's part of it
   cudaStream_t stream = nullptr;
   std::string err;
   SweepParams P{};
@@ -64,6 +67,7 @@ struct kdq_handle {
   DevBuf phase;            // per-chain phase clocks when enabled
   DevBuf gmid;             // per-chain G at tau = Nt/2 when enabled
   DevBuf lw;               // per-chain log|det| of the dropped QR factors per node
+  DevBuf slmc_prm;         // effective-model weights (bf16) of the cluster moves
   // outputs
   DevBuf obs, acc_log, drift, tape_k, tape_u;
   // Grover-determinant workspace
@@ -193,6 +197,7 @@ __global__ void k_reset_ctl(ChainCtl* ctl, int n, int full) {
   x.log_pos = 0;
   x.drift_pos = 0;
   x.max_drift = 0.0;
+  x.slmc_prop = x.slmc_acc = x.slmc_noop = 0;
 }
 
 __global__ void k_set_sweep(ChainCtl* ctl, int n, long long sweep, int reset_tape) {
@@ -299,6 +304,7 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
   h->n_obs = m->kind == KDQ_TU ? 6 : (m->kind == KDQ_TV ? 10 : 7);
   h->maxrm = m->Ns <= 32 ? 1 : (m->Ns <= 96 ? 3 : 6);
   h->dyn = ((size_t)h->n_field * 9 + 15) & ~(size_t)15;
+  h->dyn_base = h->dyn;
   auto bail = [&](int code) {
     int rc = set_err(code, h->err);
     kdq_destroy(h);
@@ -778,6 +784,8 @@ int kdq_set_precision(kdq_handle* h, int32_t mode) {
   if (mode == h->precision) return KDQ_OK;
   KDQ_CUDA(h, cudaSetDevice(h->device));
   KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->P.slmc_moves > 0)
+    KDQ_CUDA(h, mode == KDQ_PREC_MIXED ? kdq::prepare_tu_mixed(h->dyn) : kdq::prepare_tu(h->dyn));
   const size_t C = h->nchains, NNe = (size_t)h->Ns * h->Ns, Nn = (size_t)h->Ns * h->ns;
   h->esz_w = mode == KDQ_PREC_MIXED ? h->esz / 2 : h->esz;
   KDQ_CUDA(h, h->G.alloc(C * NNe * h->esz_w));
@@ -893,6 +901,68 @@ int kdq_get_log_det(kdq_handle* h, double* logdet, double* phase, size_t len) {
     logdet[c] = ctl[c].logdet;
     phase[2 * c] = ctl[c].det_re;
     phase[2 * c + 1] = ctl[c].det_im;
+  }
+  return KDQ_OK;
+}
+
+namespace {
+uint16_t to_bf16_bits(float f) {   // round to nearest even (finite values)
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+}  // namespace
+
+int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice, int32_t cluster_len,
+                    int32_t eff_steps) {
+  if (!h) return KDQ_ERR_ARG;
+  if (moves_per_slice < 0) return fail(h, KDQ_ERR_ARG, "moves_per_slice must be >= 0");
+  if (moves_per_slice == 0) {
+    KDQ_CUDA(h, cudaSetDevice(h->device));
+    KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->P.slmc_moves = 0;
+    h->dyn = h->dyn_base;
+    return KDQ_OK;
+  }
+  if (h->kind != KDQ_TU) return fail(h, KDQ_ERR_ARG, "self-learning cluster moves are implemented for t-U only");
+  if (!params) return fail(h, KDQ_ERR_ARG, "NULL params");
+  const int lmax = std::min(32, std::min(h->ns, h->Ns - 8));
+  if (cluster_len < 1 || cluster_len > lmax)
+    return fail(h, KDQ_ERR_ARG, "cluster_len must be in [1, min(32, Ns/2, Ns-8)] = [1, " + std::to_string(lmax) + "]");
+  if (h->Nt < 9) return fail(h, KDQ_ERR_ARG, "cluster moves need Nt >= 9");
+  if (eff_steps < 1 || eff_steps > (1 << 20)) return fail(h, KDQ_ERR_ARG, "eff_steps must be in [1, 2^20]");
+  for (int i = 0; i < KDQ_CNN_PARAMS; ++i)
+    if (!std::isfinite(params[i])) return fail(h, KDQ_ERR_ARG, "non-finite effective-model parameter");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<uint16_t> b(KDQ_CNN_PARAMS);
+  for (int i = 0; i < KDQ_CNN_PARAMS; ++i) b[i] = to_bf16_bits(params[i]);
+  if (!h->slmc_prm.p) KDQ_CUDA(h, h->slmc_prm.alloc(b.size() * sizeof(uint16_t)));
+  KDQ_CUDA(h, cudaMemcpy(h->slmc_prm.p, b.data(), b.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+  const size_t off = (h->dyn_base + 15) & ~(size_t)15;
+  const size_t dyn = off + kdq::slmc_smem_bytes(cluster_len);
+  KDQ_CUDA(h, h->precision == KDQ_PREC_MIXED ? kdq::prepare_tu_mixed(dyn) : kdq::prepare_tu(dyn));
+  h->P.slmc_moves = moves_per_slice;
+  h->P.slmc_len = cluster_len;
+  h->P.slmc_steps = eff_steps;
+  h->P.slmc_off = off;
+  h->P.slmc_prm = h->slmc_prm.p;
+  h->dyn = dyn;
+  return KDQ_OK;
+}
+
+int kdq_get_slmc_stats(kdq_handle* h, int64_t* counts) {
+  if (!h || !counts) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<ChainCtl> ctl(h->nchains);
+  KDQ_CUDA(h, cudaMemcpy(ctl.data(), h->ctl.p, ctl.size() * sizeof(ChainCtl), cudaMemcpyDeviceToHost));
+  counts[0] = counts[1] = counts[2] = 0;
+  for (auto& c : ctl) {
+    counts[0] += c.slmc_prop;
+    counts[1] += c.slmc_acc;
+    counts[2] += c.slmc_noop;
   }
   return KDQ_OK;
 }

@@ -18,6 +18,7 @@
 #pragma once
 #include <type_traits>
 
+#include "kdq_cnn.cuh"
 #include "kdq_device.cuh"
 #include "kdq_params.h"
 
@@ -128,6 +129,7 @@ struct Ctx {
   const KW* HalfeKinv;
   const KT* Kmat;  // hopping matrix (observables, FP64)
   PhaseClock& clk;
+  unsigned char* slmc = nullptr;   // cluster-move shared memory (dynamic), or NULL
 };
 
 // Walks the elements e = tid, tid + nthreads, ... of a column-major M x N
@@ -429,6 +431,212 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
       }
     }
     if (tid == 0) *sfield = (uint8_t)sm.newv;
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------- self-learning moves (t-U)
+constexpr uint32_t SLMC_STREAM = 0x534C4D43u;
+
+__device__ inline double u53(uint32_t a, uint32_t b) {
+  return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+// Self-learning cluster moves at slice lt with G at that slice (no
+// counterpart in the reference, which makes local moves only).  A move picks
+// Lc consecutive sites i0 .. i0+Lc-1 (mod Ns) of the slice and runs a
+// Metropolis chain of slmc_steps single-site steps on the effective weight
+// W_eff(s) = exp(F(s)) prod gamma[s] (F: the convolutional effective model,
+// evaluated incrementally on the 3x3 / 5x5 neighbourhoods a site change
+// reaches in layers 1 and 2).  The changed sites S are then accepted together
+// with probability min(1, W(s')/W(s) * W_eff(s)/W_eff(s')), which for t-U is
+// |det(I + Delta_S (I - G_SS))|^2 exp(-(F(s') - F(s))): the exact FP64
+// determinant ratio of the rank-|S| change (the multi-site form of get_r!,
+// src/tU/GreenMatrix.jl:49-54), and on acceptance G is updated by the same
+// formula as Gupdate! (src/public/Gupdate.jl:5-11) with r = M^-1 Delta_S.
+// Random numbers: Philox4x32-10 on (q, sweep, chain, SLMC_STREAM) with
+// q = (visit * moves + move) * (steps + 1) + step, visit = the slice's index in
+// the sweep's visiting order (forward lt-1, backward 2 Nt - lt).
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void slmc_moves(Ctx<KIND, T, KT, TW, KW>& c, int lt, int visit) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, Nt = P.Nt, Lc = P.slmc_len, ne = P.slmc_steps;
+  const int C1 = Lc + 6, C2 = Lc + 4;
+  const int tid = threadIdx.x;
+  unsigned char* base = c.slmc;
+  const CnnW& w = *reinterpret_cast<const CnnW*>(base);
+  float* a1w = reinterpret_cast<float*>(base + ((sizeof(CnnW) + 15) & ~size_t(15)));  // [7][16][C1]
+  float* a2w = a1w + 7 * 16 * C1;                                                     // [5][16][C2]
+  float* t1 = a2w + 5 * 16 * C2;                                                      // [9][16]
+  float* t2 = t1 + 144;                                                               // [25][16]
+  int* cur = reinterpret_cast<int*>(t2 + 400);
+  int* orig = cur + 32;
+  int* sidx = orig + 32;
+  __shared__ int s_i0, s_k, s_sx, s_acc, s_m, s_bad;
+  __shared__ double s_u, s_uf, s_dF;
+  __shared__ T s_fm[32];
+  __shared__ double s_lg;
+  __shared__ cd s_ph;
+  const int t0 = lt - 1;
+  uint8_t* row0 = c.s + (size_t)t0 * N;
+  const uint32_t sw = (uint32_t)c.ctl->sweep;
+  const T* dtab = reinterpret_cast<const T*>(P.rtab) + (size_t)(lt - 1) * 16;   // Delta(old -> new)
+  for (int mv = 0; mv < P.slmc_moves; ++mv) {
+    const uint32_t q0 = (uint32_t)(((size_t)visit * P.slmc_moves + mv) * (size_t)(ne + 1));
+    if (tid == 0) {
+      const uint4 r = philox(make_uint4(q0, sw, (uint32_t)c.chain, SLMC_STREAM), (uint32_t)P.seed,
+                             (uint32_t)(P.seed >> 32));
+      s_i0 = (int)(((uint64_t)r.x * (uint32_t)N) >> 32);
+      s_uf = u53(r.y, r.z);
+      s_dF = 0.0;
+    }
+    __syncthreads();
+    const int i0 = s_i0;
+    for (int k = tid; k < Lc; k += blockDim.x) cur[k] = orig[k] = row0[wrapi(i0 + k, N)];
+    __syncthreads();
+    // field value at a physical (row, col), with the cluster's proposed values
+    auto fld = [&](int row, int col) -> int {
+      if (row == t0) {
+        int kk = col - i0;
+        kk += kk < 0 ? N : 0;
+        if (kk < Lc) return cur[kk];
+      }
+      return c.s[(size_t)row * N + col];
+    };
+    // layer-1 window: rows t0-3 .. t0+3, columns i0-3 .. i0+Lc+2
+    for (int e = tid; e < 7 * 16 * C1; e += blockDim.x) {
+      const int col = e % C1, ch = (e / C1) % 16, row = e / (16 * C1);
+      a1w[e] = cnn_a1(w, ch, [&](int dt, int dj) {
+        return fld(wrapi(t0 - 3 + row + dt, Nt), wrapi(i0 - 3 + col + dj, N));
+      });
+    }
+    __syncthreads();
+    // layer-2 window: rows t0-2 .. t0+2, columns i0-2 .. i0+Lc+1
+    for (int p = tid; p < 5 * C2; p += blockDim.x) {
+      const int row = p / C2, col = p % C2;
+      float z[KDQ_CNN_CH];
+      cnn_z2(w, z, [&](int ch, int dt, int dj) { return a1w[((row + 1 + dt) * 16 + ch) * C1 + col + 1 + dj]; });
+#pragma unroll
+      for (int o = 0; o < KDQ_CNN_CH; ++o) a2w[(row * 16 + o) * C2 + col] = tanhf(z[o]);
+    }
+    __syncthreads();
+    // Metropolis chain on the effective weight
+    for (int st = 1; st <= ne; ++st) {
+      if (tid == 0) {
+        const uint4 r = philox(make_uint4(q0 + st, sw, (uint32_t)c.chain, SLMC_STREAM), (uint32_t)P.seed,
+                               (uint32_t)(P.seed >> 32));
+        const int k = (int)(((uint64_t)r.x * (uint32_t)Lc) >> 32);
+        const int kv = (int)(((uint64_t)r.y * 3u) >> 32);
+        const int sold = cur[k];
+        s_k = k;
+        s_sx = kv + (kv + 1 >= sold ? 2 : 1);
+        s_u = u53(r.z, r.w);
+      }
+      __syncthreads();
+      const int k = s_k, sx = s_sx, j = wrapi(i0 + k, N);
+      // layer 1 at the 3x3 neighbourhood of (t0, j) with the new value
+      if (tid < 144) {
+        const int pos = tid >> 4, ch = tid & 15, dy = pos / 3, dx = pos % 3;
+        const int pr = wrapi(t0 - 1 + dy, Nt), pc = wrapi(j - 1 + dx, N);
+        t1[tid] = cnn_a1(w, ch, [&](int dt, int dj) {
+          const int rr = wrapi(pr + dt, Nt), cc = wrapi(pc + dj, N);
+          return (rr == t0 && cc == j) ? sx : fld(rr, cc);
+        });
+      }
+      __syncthreads();
+      // layer 2 at the 5x5 neighbourhood and the change of F
+      double dsum = 0.0;
+      for (int idx = tid; idx < 400; idx += blockDim.x) {
+        const int p = idx >> 4, o = idx & 15, row = p / 5, col = k + p % 5;
+        float z = w.b2[o];
+        for (int ch = 0; ch < 16; ++ch)
+#pragma unroll
+          for (int tap = 0; tap < 9; ++tap) {
+            const int ar = row + tap / 3, ac = col + tap % 3;   // layer-1 window row, column
+            const bool chg = ar >= 2 && ar <= 4 && ac >= k + 2 && ac <= k + 4;
+            const float v = chg ? t1[((ar - 2) * 3 + (ac - k - 2)) * 16 + ch] : a1w[(ar * 16 + ch) * C1 + ac];
+            z = fmaf(w.w2f[(ch * 9 + tap) * 16 + o], v, z);
+          }
+        const float a = tanhf(z);
+        t2[idx] = a;
+        dsum += (double)w.w3s[o] * (double)(a - a2w[(row * 16 + o) * C2 + col]);
+      }
+      const double dF = block_sum(dsum, c.sm.red);
+      if (tid == 0) {
+        const int sold = cur[k];
+        const double p = exp(dF) * P.gratio[(sold - 1) * 4 + sx - 1];
+        const int acc = s_u < p;
+        s_acc = acc;
+        if (acc) {
+          s_dF += dF;
+          cur[k] = sx;
+        }
+      }
+      __syncthreads();
+      if (s_acc) {
+        if (tid < 144) {
+          const int pos = tid >> 4, ch = tid & 15;
+          a1w[((2 + pos / 3) * 16 + ch) * C1 + k + 2 + pos % 3] = t1[tid];
+        }
+        for (int idx = tid; idx < 400; idx += blockDim.x) {
+          const int p = idx >> 4, o = idx & 15;
+          a2w[((p / 5) * 16 + o) * C2 + k + p % 5] = t2[idx];
+        }
+      }
+      __syncthreads();
+    }
+    // the changed sites and the exact FP64 ratio
+    if (tid == 0) {
+      int m = 0;
+      for (int k = 0; k < Lc; ++k)
+        if (cur[k] != orig[k]) sidx[m++] = k;
+      s_m = m;
+      s_bad = 0;
+      c.ctl->slmc_prop += 1;
+      if (!m) c.ctl->slmc_noop += 1;
+    }
+    __syncthreads();
+    const int m = s_m;
+    if (!m) continue;
+    T* M = c.Mss;   // m x m, free between recomputes
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int a = e % m, b = e / m;
+      const int ja = wrapi(i0 + sidx[a], N), jb = wrapi(i0 + sidx[b], N);
+      const T d = dtab[(orig[sidx[a]] - 1) * 4 + cur[sidx[a]] - 1];
+      T v = zero<T>() - cvt<T>(c.G[ja + (size_t)jb * N]);
+      if (a == b) v = v + one<T>();
+      v = d * v;
+      if (a == b) v = v + one<T>();
+      M[e] = v;
+    }
+    __syncthreads();
+    gj_inverse(m, M, s_fm, c.piv, &s_bad, &s_lg, &s_ph);   // M <- M^-1, log|det M|
+    if (tid == 0) {
+      const double la = 2.0 * s_lg - s_dF;
+      const int acc = !s_bad && isfinite(la) && s_uf < exp(la);
+      s_acc = acc;
+      c.ctl->slmc_acc += acc;
+    }
+    __syncthreads();
+    if (!s_acc) continue;
+    // U = G[:,S] M^-1 Delta_S (N x m) and Wr = E_S - G[S,:] (m x N)
+    TW* U = c.Yw;
+    TW* Wr = c.Y2w;
+    for (int e = tid; e < N * m; e += blockDim.x) {
+      const int i = e % N, a = e / N;
+      T acc = zero<T>();
+      for (int b = 0; b < m; ++b) madd(acc, cvt<T>(c.G[i + (size_t)wrapi(i0 + sidx[b], N) * N]), M[b + (size_t)a * m]);
+      U[e] = cvt<TW>(acc * dtab[(orig[sidx[a]] - 1) * 4 + cur[sidx[a]] - 1]);
+    }
+    for (int e = tid; e < m * N; e += blockDim.x) {
+      const int a = e % m, col = e / m;
+      const int ja = wrapi(i0 + sidx[a], N);
+      Wr[e] = (col == ja ? one<TW>() : zero<TW>()) - c.G[ja + (size_t)col * N];
+    }
+    __syncthreads();
+    gemm_sq<MAXRM, TW>(N, N, m, U, N, Wr, m, c.W1, N);
+    for (Walk wk(N, N); wk.ok(); wk.next()) c.G[wk.e] = c.G[wk.e] - c.W1[wk.e];
+    for (int a = tid; a < m; a += blockDim.x) row0[wrapi(i0 + sidx[a], N)] = (uint8_t)cur[sidx[a]];
     __syncthreads();
   }
 }
@@ -1080,6 +1288,12 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, i
                              static_cast<const KW*>(P.HalfeKinv),
                              static_cast<const KT*>(P.K),
                              clk};
+  if constexpr (KIND == KDQ_TU) {
+    if (P.slmc_moves > 0 && mode != KDQ_MODE_INIT) {
+      c.slmc = reinterpret_cast<unsigned char*>(dyn_d) + P.slmc_off;
+      load_cnn_weights(*reinterpret_cast<CnnW*>(c.slmc), static_cast<const __nv_bfloat16*>(P.slmc_prm));
+    }
+  }
   if (mode == KDQ_MODE_INIT) {
     node_backward<MAXRM>(c, k, k == 1, false);
     return;
@@ -1104,6 +1318,12 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, i
         clk.lap(0);
         update_layer<MAXRM>(c, lt, 0, true);
         clk.lap(1);
+        if constexpr (KIND == KDQ_TU) {
+          if (c.slmc) {
+            slmc_moves<MAXRM>(c, lt, lt - 1);
+            clk.lap(6);
+          }
+        }
       }
       if (rec) {
         if (P.record == 2) measure_fast<MAXRM>(c, lt);
@@ -1136,6 +1356,12 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, i
       } else {
         update_layer<MAXRM>(c, lt, 0, false);
         clk.lap(1);
+        if constexpr (KIND == KDQ_TU) {
+          if (c.slmc) {
+            slmc_moves<MAXRM>(c, lt, 2 * P.Nt - lt);
+            clk.lap(6);
+          }
+        }
         if (rec) {
           if (P.record == 2) measure_fast<MAXRM>(c, lt);
           else measure<MAXRM>(c, lt);

@@ -247,6 +247,20 @@ class Sweeper:
         s = self.get_fields() if fields is None else fields
         return np.array([log_weight(self.model, s[c], ld[c]) for c in range(self.nchains)])
 
+    def slmc_enable(self, params, moves_per_slice: int = 1, cluster_len: int = 32, eff_steps: int = 64):
+        """Turn on the self-learning cluster moves (t-U) with the effective
+        model ``params`` (see ``kapdqmc_gb300.slmc``); moves_per_slice=0 turns them off."""
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32))
+        if p.shape != (3057,):
+            raise ValueError("params must hold 3057 floats")
+        self._ck(self.lib.kdq_slmc_enable(self.h, p.ctypes.data, moves_per_slice, cluster_len, eff_steps))
+
+    def slmc_stats(self):
+        """(proposed, accepted, no-change) cluster moves of the last call."""
+        out = np.zeros(3, dtype=np.int64)
+        self._ck(self.lib.kdq_get_slmc_stats(self.h, out.ctypes.data))
+        return {"proposed": int(out[0]), "accepted": int(out[1]), "unchanged": int(out[2])}
+
     def drift(self, sweeps: int):
         n = sweeps * 2 * (len(self.model.nodes) - 1)
         out = np.empty(self.nchains * n)

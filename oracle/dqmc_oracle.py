@@ -125,6 +125,9 @@ class _Sweep:
         self.accepts: list = []
         self.drift: list = []
         self.obs_rows: list = []
+        self.sweep_no = 0          # Philox sweep counter of the cluster moves
+        self.slmc = None           # cluster-move configuration (t-U), see phy_update
+        self.slmc_log: list = []   # (u, p) of every cluster-move decision
 
     def node(self, k):  # 1-based access to nodes
         return self.nodes[k - 1]
@@ -202,6 +205,75 @@ class _TUSweep(_Sweep):
                 Gupdate(G, [i], np.array([[r]]))
                 s[i, lt - 1] = sx
 
+    def after_update(self, lt, visit):
+        if self.slmc is not None:
+            self.slmc_moves(lt, visit)
+
+    def slmc_moves(self, lt, visit):
+        """Self-learning cluster moves at slice lt (no counterpart in the
+        reference).  ``Lc`` consecutive sites from a random start, ``steps``
+        Metropolis steps on exp(F) prod gamma with F the effective model
+        (recomputed in full for every trial here), then the changed sites are
+        accepted with |det(I + Delta_S (I - G_SS))|^2 exp(-(F' - F)) and G is
+        updated by Gupdate! (src/public/Gupdate.jl:5-11) with
+        r = (I + Delta_S (I - G_SS))^-1 Delta_S.  Random numbers: Philox4x32-10
+        on (q, sweep, chain, 0x534C4D43) with q = (visit moves + move)(steps + 1) + step."""
+        import cnn_oracle
+        import philox
+
+        cfg, m, G, s = self.slmc, self.m, self.G, self.s
+        N, Lc, ne, t0 = m.Ns, cfg["cluster_len"], cfg["steps"], lt - 1
+        key = (cfg["seed"] & 0xFFFFFFFF, cfg["seed"] >> 32)
+
+        def draw(q):
+            return [int(v) for v in philox.philox4x32_10(q & 0xFFFFFFFF, self.sweep_no & 0xFFFFFFFF,
+                                                         cfg["chain"], 0x534C4D43, *key)]
+
+        def u53(a, b):
+            return ((a >> 5) * 67108864.0 + (b >> 6)) * (1.0 / 9007199254740992.0)
+
+        for mv in range(cfg["moves"]):
+            q0 = (visit * cfg["moves"] + mv) * (ne + 1)
+            r = draw(q0)
+            i0 = (r[0] * N) >> 32
+            uf = u53(r[1], r[2])
+            sites = [(i0 + k) % N for k in range(Lc)]
+            orig = [int(s[j, t0]) for j in sites]
+            cur = list(orig)
+            field = np.ascontiguousarray(np.asarray(s, dtype=np.uint8).T)[None].copy()
+            F = cnn_oracle.forward(field, cfg["params"])[0][0]
+            dF_tot = 0.0
+            for st in range(1, ne + 1):
+                r = draw(q0 + st)
+                k = (r[0] * Lc) >> 32
+                kv = (r[1] * 3) >> 32
+                u = u53(r[2], r[3])
+                sold = cur[k]
+                sx = _sx(sold, kv)
+                trial = field.copy()
+                trial[0, t0, sites[k]] = sx
+                F1 = cnn_oracle.forward(trial, cfg["params"])[0][0]
+                p = math.exp(F1 - F) * (m.γ[sx - 1] / m.γ[sold - 1])
+                self.slmc_log.append((u, p))
+                if u < p:
+                    cur[k] = sx
+                    field = trial
+                    dF_tot += F1 - F
+                    F = F1
+            S = [k for k in range(Lc) if cur[k] != orig[k]]
+            if not S:
+                continue
+            idx = [sites[k] for k in S]
+            Δ = np.array([np.exp(1j * m.α[lt - 1] * (m.η[cur[k] - 1] - m.η[orig[k] - 1])) - 1 for k in S])
+            M = np.eye(len(S)) + Δ[:, None] * (np.eye(len(S)) - G[np.ix_(idx, idx)])
+            _, ld = np.linalg.slogdet(M)
+            p = math.exp(2.0 * ld - dF_tot)
+            self.slmc_log.append((uf, p))
+            if uf < p:
+                Gupdate(G, idx, np.linalg.inv(M) * Δ[None, :])
+                for k in S:
+                    s[sites[k], t0] = cur[k]
+
     def measure(self, lt):  # phy_measure, phy_update.jl:154-254
         m = self.m
         G0 = self.G.copy()
@@ -230,6 +302,7 @@ class _TUSweep(_Sweep):
             for lt in range(1, m.Nt + 1):
                 self.G = self.wrap_forward(self.G, lt)
                 self.update_layer(lt)
+                self.after_update(lt, lt - 1)
                 if self.record and 0 <= self.Θidx - self.idx <= 1:
                     acc += self.measure(lt)
                     cnt += 1
@@ -237,6 +310,7 @@ class _TUSweep(_Sweep):
                     self.node_forward()
             for lt in range(m.Nt, 0, -1):
                 self.update_layer(lt)
+                self.after_update(lt, 2 * m.Nt - lt)
                 if self.record and 0 <= self.idx - self.Θidx <= 1:
                     acc += self.measure(lt)
                     cnt += 1
@@ -245,6 +319,7 @@ class _TUSweep(_Sweep):
                     self.node_backward()
             if self.record:
                 self.obs_rows.append(acc / cnt)
+            self.sweep_no += 1
         return self
 
 
@@ -572,14 +647,20 @@ def proposals_per_sweep(model) -> int:
     return 2 * model.Nt * model.n_field
 
 
-def phy_update(model, s, sweeps: int, tape: Tape, record: bool = False):
+def phy_update(model, s, sweeps: int, tape: Tape, record: bool = False, slmc=None):
     """Run ``sweeps`` sweeps; returns the sweep object (s, G, accepts, drift, obs_rows).
 
     Mirrors ``phy_update(path, model, s, Sweeps, record)`` without the CSV side
     output: src/tU/phy_update.jl:3-152, src/tV/phy_update.jl:1-188,
-    src/tUV/phy_update.jl:1-186.
+    src/tUV/phy_update.jl:1-186.  ``slmc`` (t-U only) adds the cluster moves:
+    a dict with params, moves, cluster_len, steps, seed and chain.
     """
-    return _SWEEPS[model.kind](model, s, tape, record).run(sweeps)
+    sw = _SWEEPS[model.kind](model, s, tape, record)
+    if slmc is not None:
+        if model.kind != KIND_TU:
+            raise ValueError("cluster moves are restated for t-U only")
+        sw.slmc = slmc
+    return sw.run(sweeps)
 
 
 def G_tau(model, s, τ: int):

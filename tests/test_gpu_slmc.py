@@ -1,0 +1,134 @@
+"""Self-learning cluster moves in the CUDA t-U sweep (through the C ABI)
+against the oracle's restatement, at the benchmark size through
+size-independent properties, and the gain of a trained effective model.
+
+With an all-zero effective model F = 0 exactly on both sides, so every
+decision is made from the same FP64 numbers and the runs must agree exactly.
+With a non-zero model the GPU evaluates F in FP32 and the oracle in FP64:
+the runs must agree unless a decision fell within 1e-5 (relative) of its
+threshold, which the test then reports instead of failing."""
+import numpy as np
+import pytest
+
+import cases
+import cnn_oracle as N
+import dqmc_oracle as O
+import philox
+from kapdqmc_gb300 import Initial_s, slmc
+from kapdqmc_gb300.sweep import Sweeper
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_both(model, params, nchains=2, sweeps=1, Lc=4, steps=8, moves=1, seed=21, record=True):
+    fields = np.stack([Initial_s(model, 60 + c) for c in range(nchains)])
+    n = O.proposals_per_sweep(model) * sweeps
+    with Sweeper(model, nchains) as sw:
+        sw.set_fields(fields)
+        sw.set_rng(seed)
+        sw.enable_accept_log(n)
+        sw.slmc_enable(params, moves, Lc, steps)
+        obs = sw.phy_update(sweeps, record)
+        s_gpu = sw.get_fields()
+        acc = sw.accept_log()
+        G = [sw.green(c) for c in range(nchains)]
+        st = sw.slmc_stats()
+        drift = sw.drift(sweeps)
+    refs = []
+    for c in range(nchains):
+        ks, us = zip(*(philox.tape(seed, c, w, O.proposals_per_sweep(model)) for w in range(sweeps)))
+        cfg = dict(params=params, moves=moves, cluster_len=Lc, steps=steps, seed=seed, chain=c)
+        refs.append(O.phy_update(model, fields[c], sweeps, O.Tape(np.concatenate(ks), np.concatenate(us)),
+                                 record, slmc=cfg))
+    assert st["proposed"] == nchains * sweeps * 2 * model.Nt * moves
+    assert drift.max() < 1e-6
+    return s_gpu, acc, G, obs, st, refs
+
+
+def _assert_same(s_gpu, acc, G, obs, refs, exact=True):
+    for c, ref in enumerate(refs):
+        if not exact:
+            margin = min(abs(u - p) / max(p, 1e-300) for u, p in ref.slmc_log)
+            if not np.array_equal(s_gpu[c], ref.s):
+                pytest.skip(f"chain {c}: trajectories split at a near-tie (closest decision {margin:.1e})")
+        np.testing.assert_array_equal(s_gpu[c], ref.s, err_msg=f"chain {c} fields")
+        np.testing.assert_array_equal(acc[c].astype(bool), np.array(ref.accepts), err_msg=f"chain {c} accepts")
+        rel = np.linalg.norm(G[c] - ref.G) / np.linalg.norm(ref.G)
+        assert rel < 1e-10, rel
+        ro = np.array(ref.obs_rows)
+        assert np.abs(obs[c] - ro).max() / max(1.0, np.abs(ro).max()) < 1e-9
+
+
+def test_zero_model_matches_oracle_exactly():
+    m = cases.tu_square()
+    out = _run_both(m, np.zeros(N.NPARAM, np.float32), sweeps=2)
+    s_gpu, acc, G, obs, st, refs = out
+    assert st["accepted"] > 0
+    _assert_same(s_gpu, acc, G, obs, refs)
+
+
+@pytest.mark.parametrize("make,Lc", [(cases.tu_square, 4), (cases.tu_honeycomb, 6)])
+def test_random_model_matches_oracle(make, Lc):
+    m = make()
+    params = (N.init_params(7) * 0.5).astype(np.float32)
+    s_gpu, acc, G, obs, st, refs = _run_both(m, params, Lc=Lc, steps=12)
+    assert st["accepted"] > 0
+    _assert_same(s_gpu, acc, G, obs, refs, exact=False)
+
+
+def test_cluster_moves_at_benchmark_size_keep_G_and_log_weight_consistent():
+    # 9x9 honeycomb, 200 slices, 32-site clusters: after a sweep with cluster
+    # moves, the carried log|det| equals that of a chain rebuilt on the final
+    # fields and the drift at every recompute stays at the FP64 level
+    m = cases.c5()
+    nch = 2
+    fields = np.stack([Initial_s(m, 3 + c) for c in range(nch)])
+    with Sweeper(m, nch) as sw:
+        sw.set_fields(fields)
+        sw.set_rng(9)
+        sw.slmc_enable(slmc.init_params(1) * 0.05, 1, 32, 64)
+        sw.phy_update(1, False)
+        ld, _ = sw.log_det()
+        s1 = sw.get_fields()
+        st = sw.slmc_stats()
+        drift = sw.drift(1)
+    assert st["proposed"] == nch * 2 * m.Nt
+    assert st["accepted"] > 0
+    assert drift.max() < 1e-5
+    with Sweeper(m, nch) as sw2:
+        sw2.set_fields(s1)
+        sw2.init()
+        ld2, _ = sw2.log_det()
+    assert np.all(np.abs(ld - ld2) < 1e-8 * np.maximum(1.0, np.abs(ld2)))
+
+
+def test_trained_model_raises_cluster_acceptance():
+    # train the effective model on configurations the sweep itself generates
+    # and compare the cluster moves' acceptance against an untrained (zero) model
+    m = cases.tu_honeycomb()
+    nch = 64
+    fields = np.stack([Initial_s(m, 200 + c) for c in range(nch)])
+    cfgs, lds = [], []
+    with Sweeper(m, nch) as sw:
+        sw.set_fields(fields)
+        sw.set_rng(3)
+        sw.phy_update(5, False)
+        for _ in range(12):
+            sw.phy_update(1, False)
+            cfgs.append(slmc.cnn_fields(sw.get_fields()))
+            lds.append(sw.log_det()[0])
+        s_eq = sw.get_fields()
+    X = np.concatenate(cfgs)
+    y = np.concatenate(lds)
+    params, loss, _ = slmc.fit_effective_model(X, y, epochs=30, batch=32, lr=3e-3, seed=0)
+    assert loss[-1] < 0.5 * loss[0]
+    rates = {}
+    for name, p in (("zero", np.zeros(N.NPARAM, np.float32)), ("trained", params)):
+        with Sweeper(m, nch) as sw:
+            sw.set_fields(s_eq)
+            sw.set_rng(17)
+            sw.slmc_enable(p, 1, 6, 24)
+            sw.phy_update(2, False)
+            st = sw.slmc_stats()
+        rates[name] = st["accepted"] / max(1, st["proposed"] - st["unchanged"])
+    assert rates["trained"] > rates["zero"], rates
