@@ -469,6 +469,123 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_slmc(args):
+    """Self-learning proposals against the plain local-update sweep (t-U).
+
+    1. Equilibrate the chains, then collect `--slmc-train-sweeps` sweeps of
+       configurations (chains x sweeps of them) with their log|det|.
+    2. Fit the effective model with the library's CUDA training kernels.
+    3. From the same equilibrated fields run two arms of `--steps` timed
+       sweeps each, measuring every sweep: local updates only, and local
+       updates plus the cluster moves.  τ_int of the energy and of the AF
+       structure factor (SDW0 column) come from each arm's own series.
+    4. The plain FP64 sweep's chain-sweeps/s is timed on the same fields, so
+       the gain is against the plain FP64 GPU method.
+    One JSON line; value = the cluster-move arm's effective samples/s (the
+    slower of the two observables)."""
+    import torch
+    from kapdqmc_gb300 import Initial_s, slmc
+    from kapdqmc_gb300.sweep import Sweeper
+
+    model = make_model()
+    if model.kind != 0:
+        print(json.dumps({"slmc": "unavailable", "why": "cluster moves are implemented for t-U only"}))
+        return
+    dev = torch.device("cuda", 0)
+    seed = 777
+    fields = np.stack([Initial_s(model, 3000 + c) for c in range(NCHAINS)])
+
+    def sweeper(prec, s0, rng):
+        sw = Sweeper(model, NCHAINS)
+        sw.set_precision(prec)
+        sw.set_fields(s0)
+        sw.set_rng(rng)
+        return sw
+
+    def timed(sw, n):
+        stream = torch.cuda.ExternalStream(sw.stream, device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sw.sweep(n, record=RECORD)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3
+
+    # 1. equilibrate and collect training data
+    sw = sweeper(PRECISION, fields, seed)
+    sw.init()
+    sw.sweep(args.slmc_burn, record=0)
+    t0 = time.perf_counter()
+    X, Y = [], []
+    for _ in range(args.slmc_train_sweeps):
+        sw.sweep(1, record=0)
+        X.append(slmc.cnn_fields(sw.get_fields()))
+        Y.append(sw.log_det()[0])
+    t_collect = time.perf_counter() - t0
+    s_eq = sw.get_fields()
+    sw.close()
+    X = np.concatenate(X)
+    Y = np.concatenate(Y)
+    # 2. fit
+    t0 = time.perf_counter()
+    params, loss, (mu, sd) = slmc.fit_effective_model(X, Y, epochs=args.slmc_epochs, batch=64, lr=2e-3, seed=1)
+    t_train = time.perf_counter() - t0
+    F = slmc.cnn_forward(X[:512], params)
+    resid = float(np.std(F - 2 * Y[:512]))
+
+    # 3. the two arms
+    arms = {}
+    for name, on in (("local", False), ("slmc", True)):
+        sw = sweeper(PRECISION, s_eq, seed + 1)
+        if on:
+            sw.slmc_enable(params, args.slmc_moves, args.slmc_len, args.slmc_steps)
+        sw.init()
+        sw.sweep(args.warmup, record=RECORD)
+        sw.synchronize()
+        secs = timed(sw, args.steps)
+        obs = sw.get_obs(args.warmup + args.steps)[:, args.warmup:, :]
+        st = sw.slmc_stats() if on else None
+        sw.close()
+        cs = NCHAINS * args.steps / secs
+        te, ta = tau_int(obs[:, :, 0]), tau_int(obs[:, :, 4])
+        arm = {"chain_sweeps_per_s": cs, "tau_int_energy": te, "tau_int_af_sf": ta,
+               "eff_samples_per_s": cs / max(te, ta),
+               "energy": [float(obs[:, :, 0].mean()), float(obs[:, :, 0].mean(axis=1).std() / math.sqrt(NCHAINS))],
+               "double_occupancy": [float(obs[:, :, 1].mean() / model.Ns),
+                                    float(obs[:, :, 1].mean(axis=1).std() / math.sqrt(NCHAINS) / model.Ns)],
+               "af_sf": [float(obs[:, :, 4].mean()), float(obs[:, :, 4].mean(axis=1).std() / math.sqrt(NCHAINS))]}
+        if st:
+            arm["cluster_moves"] = dict(st, acceptance=st["accepted"] / max(1, st["proposed"] - st["unchanged"]))
+        arms[name] = arm
+    # 4. the plain FP64 sweep's throughput on the same fields
+    sw = sweeper("fp64", s_eq, seed + 2)
+    sw.init()
+    sw.sweep(1, record=RECORD)
+    sw.synchronize()
+    n64 = max(2, args.steps // 10)
+    cs64 = NCHAINS * n64 / timed(sw, n64)
+    sw.close()
+    base = cs64 / max(arms["local"]["tau_int_energy"], arms["local"]["tau_int_af_sf"])
+
+    def within(a, b, k):
+        return abs(a[k][0] - b[k][0]) <= math.hypot(a[k][1], b[k][1]) * 2.0
+
+    out = {"metric": METRIC, "value": arms["slmc"]["eff_samples_per_s"], "unit": UNIT, "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "c128" if PRECISION == "fp64" else "c64+c128",
+           "data": "synthetic (seeded HS fields and Philox proposal and cluster-move streams)",
+           "config": dict(config(), slmc={"moves_per_slice": args.slmc_moves, "cluster_len": args.slmc_len,
+                                          "eff_steps": args.slmc_steps}),
+           "plain_fp64_eff_samples_per_s": base, "gain_vs_plain_fp64": arms["slmc"]["eff_samples_per_s"] / base,
+           "plain_fp64_chain_sweeps_per_s": cs64, "arms": arms,
+           "obs_agree_2sigma": {k: within(arms["slmc"], arms["local"], k)
+                                for k in ("energy", "double_occupancy", "af_sf")},
+           "training": {"configs": int(X.shape[0]), "collect_s": t_collect, "train_s": t_train,
+                        "epochs": args.slmc_epochs, "loss_first_last": [float(loss[0]), float(loss[-1])],
+                        "target_sd": sd, "residual_sd": resid}}
+    print(json.dumps(out))
+
+
 def dist_max(dist, value: float, device=None) -> float:
     """Max of a per-rank value over all ranks (identity without a process group)."""
     if dist is None:
@@ -509,6 +626,15 @@ def main():
                     help="configuration (default c2, the metric's; the CPU arm exists for c2 only)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="arithmetic of the sweep (mixed: complex sweeps only)")
+    ap.add_argument("--slmc", action="store_true",
+                    help="self-learning cluster moves against local updates (t-U workloads; prints its own line)")
+    ap.add_argument("--slmc-burn", type=int, default=10)
+    ap.add_argument("--slmc-train-sweeps", type=int, default=80,
+                    help="sweeps of configurations collected for training (x chains configurations)")
+    ap.add_argument("--slmc-epochs", type=int, default=10)
+    ap.add_argument("--slmc-moves", type=int, default=1)
+    ap.add_argument("--slmc-len", type=int, default=32)
+    ap.add_argument("--slmc-steps", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -519,7 +645,12 @@ def main():
     if args.impl == "reference" and args.workload != "c2":
         print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement covers the t-V workload only"}))
         return
-    if args.tau_run:
+    if args.slmc:
+        if args.workload == "c2":
+            WL = WORKLOADS["c5"]
+            NCHAINS = args.chains or WL["chains"]
+        run_slmc(args)
+    elif args.tau_run:
         run_tau(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -293,6 +293,28 @@ int kdq_cnn_train(const uint8_t* fields, const double* target, int32_t n_cfg, in
 int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice, int32_t cluster_len,
                     int32_t eff_steps);
 
+/* Coupled incremental SCEE sweep, ctrl_SCEEicr(path, model, indexA, indexB,
+ * Sweeps, lambda, Nlambda, ss, record) (src/tU/SCEE.jl:1-211), t-U in FP64.
+ * Chains 2p and 2p+1 of the handle are the two replicas ss[1], ss[2] of pair
+ * p (fields through kdq_set_fields, random stream through kdq_set_rng or
+ * kdq_set_tape, replica r of pair p drawing from chain 2p+r's stream in the
+ * plain sweep's order).  kdq_scee_enable sets the regions (1-based sites,
+ * at most min(Ns/2, 96) each), lambda in [0,1] and Nlambda.  kdq_scee_run
+ * builds every replica's block products and stabilised chains and runs
+ * `sweeps` coupled sweeps: each site proposal of either replica is accepted
+ * with its local ratio times |det g_A'/det g_A|^(2 lambda) |det g_B'/det g_B|^(2 (1-lambda))
+ * (UpdateSCEELayer!, src/tU/SCEE.jl:230-287).  O receives per pair the
+ * reference's CSV row: O[p (sweeps+1)] = lambda, then per sweep the mean over
+ * slices of (|det g_A|^2 / |det g_B|^2)^(1/Nlambda); len counts doubles.
+ * kdq_scee_get_green copies one replica's Green's function `which`
+ * (0: G(tau,tau), 1: G(tau0,tau0) at the middle node, 2: G(tau,tau0),
+ * 3: G(tau0,tau); complex, 2 Ns^2 doubles) at the end of the run (tau = 0).
+ * After kdq_scee_run, kdq_init must precede a plain sweep. */
+int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB,
+                    double lambda, int32_t n_lambda);
+int kdq_scee_run(kdq_handle* h, int32_t sweeps, double* O, size_t len);
+int kdq_scee_get_green(kdq_handle* h, int32_t chain, int32_t which, double* G, size_t len);
+
 /* Cluster moves of the last kdq_phy_update / kdq_sweep call, summed over
  * chains: counts[0] proposed, counts[1] accepted, counts[2] proposals in
  * which the effective-model chain changed no site (accepted trivially, not

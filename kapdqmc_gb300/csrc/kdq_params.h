@@ -109,6 +109,23 @@ struct SweepParams {
   int slmc_moves, slmc_len, slmc_steps;
   size_t slmc_off;
   const void* slmc_prm;
+  // coupled SCEE sweep (t-U): per chain G0, Gt0, G0t (N x N) and the block
+  // products BMs, BMi ((NN-1) x N x N); per pair the inverse Grover matrices
+  // of regions A and B (scee_nmax^2 each), |det g_A|^2, |det g_B|^2 and the
+  // estimator's running sum and count (4 doubles), and scee_O_cap rows
+  void* scee_G0;
+  void* scee_Gt0;
+  void* scee_G0t;
+  void* scee_BMs;
+  void* scee_BMi;
+  void* scee_inv;
+  const int* scee_idxA;         // 0-based sites
+  const int* scee_idxB;
+  int scee_nA, scee_nB, scee_nmax, scee_nlam;
+  double scee_lam;
+  double* scee_det;
+  double* scee_O;
+  int scee_O_cap;
 
   template <class T> __host__ __device__ T* BLs(int c) const { return static_cast<T*>(BLs_) + (size_t)c * sz_chainB; }
   template <class T> __host__ __device__ T* BRs(int c) const { return static_cast<T*>(BRs_) + (size_t)c * sz_chainB; }

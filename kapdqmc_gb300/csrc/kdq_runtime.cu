@@ -68,6 +68,10 @@ struct kdq_handle {
   DevBuf gmid;             // per-chain G at tau = Nt/2 when enabled
   DevBuf lw;               // per-chain log|det| of the dropped QR factors per node
   DevBuf slmc_prm;         // effective-model weights (bf16) of the cluster moves
+  // coupled SCEE sweep buffers (kdq_scee_enable)
+  DevBuf scee_G0, scee_Gt0, scee_G0t, scee_BMs, scee_BMi, scee_inv, scee_idx, scee_det, scee_O;
+  bool scee = false;
+  double scee_lam = 0.0;
   // outputs
   DevBuf obs, acc_log, drift, tape_k, tape_u;
   // Grover-determinant workspace
@@ -949,6 +953,118 @@ int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice,
   h->P.slmc_off = off;
   h->P.slmc_prm = h->slmc_prm.p;
   h->dyn = dyn;
+  return KDQ_OK;
+}
+
+int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB,
+                    double lambda, int32_t n_lambda) {
+  if (!h) return KDQ_ERR_ARG;
+  if (h->kind != KDQ_TU) return fail(h, KDQ_ERR_ARG, "the coupled SCEE sweep is implemented for t-U only");
+  if (h->nchains % 2) return fail(h, KDQ_ERR_ARG, "the SCEE sweep needs an even number of chains (replica pairs)");
+  if (h->precision != KDQ_PREC_FP64) return fail(h, KDQ_ERR_ARG, "the SCEE sweep runs in FP64 only");
+  if (!indexA || !indexB) return fail(h, KDQ_ERR_ARG, "NULL region");
+  const int nmax_ok = std::min(h->ns, 96);
+  if (nA < 1 || nB < 1 || nA > nmax_ok || nB > nmax_ok)
+    return fail(h, KDQ_ERR_ARG, "region sizes must be in [1, min(Ns/2, 96)] = [1, " + std::to_string(nmax_ok) + "]");
+  std::vector<int32_t> idx;
+  for (int i = 0; i < nA; ++i) idx.push_back(indexA[i] - 1);
+  for (int i = 0; i < nB; ++i) idx.push_back(indexB[i] - 1);
+  for (int v : idx)
+    if (v < 0 || v >= h->Ns) return fail(h, KDQ_ERR_ARG, "region index out of range (1-based)");
+  if (!(lambda >= 0.0 && lambda <= 1.0)) return fail(h, KDQ_ERR_ARG, "lambda must be in [0, 1]");
+  if (n_lambda < 1) return fail(h, KDQ_ERR_ARG, "n_lambda must be >= 1");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  const size_t C = h->nchains, NN2 = (size_t)h->Ns * h->Ns, e = h->esz, pairs = C / 2;
+  const int nmax = std::max(nA, nB);
+  if (!h->scee) {
+    KDQ_CUDA(h, h->scee_G0.alloc(C * NN2 * e));
+    KDQ_CUDA(h, h->scee_Gt0.alloc(C * NN2 * e));
+    KDQ_CUDA(h, h->scee_G0t.alloc(C * NN2 * e));
+    KDQ_CUDA(h, h->scee_BMs.alloc(C * (h->NN - 1) * NN2 * e));
+    KDQ_CUDA(h, h->scee_BMi.alloc(C * (h->NN - 1) * NN2 * e));
+    KDQ_CUDA(h, h->scee_det.alloc(pairs * 4 * sizeof(double)));
+  }
+  KDQ_CUDA(h, h->scee_inv.alloc(pairs * 2 * (size_t)nmax * nmax * e));
+  KDQ_CUDA(h, upload(h->scee_idx, idx));
+  SweepParams& P = h->P;
+  P.scee_G0 = h->scee_G0.p;
+  P.scee_Gt0 = h->scee_Gt0.p;
+  P.scee_G0t = h->scee_G0t.p;
+  P.scee_BMs = h->scee_BMs.p;
+  P.scee_BMi = h->scee_BMi.p;
+  P.scee_inv = h->scee_inv.p;
+  P.scee_idxA = h->scee_idx.as<int32_t>();
+  P.scee_idxB = h->scee_idx.as<int32_t>() + nA;
+  P.scee_nA = nA;
+  P.scee_nB = nB;
+  P.scee_nmax = nmax;
+  P.scee_nlam = n_lambda;
+  P.scee_lam = lambda;
+  P.scee_det = h->scee_det.as<double>();
+  h->scee_lam = lambda;
+  h->scee = true;
+  return KDQ_OK;
+}
+
+int kdq_scee_run(kdq_handle* h, int32_t sweeps, double* O, size_t len) {
+  if (!h) return KDQ_ERR_ARG;
+  if (!h->scee) return fail(h, KDQ_ERR_STATE, "kdq_scee_enable must precede kdq_scee_run");
+  if (sweeps < 0) return fail(h, KDQ_ERR_ARG, "sweeps must be >= 0");
+  const size_t pairs = h->nchains / 2;
+  if (!O || len != pairs * (size_t)(sweeps + 1))
+    return fail(h, KDQ_ERR_ARG, "O must hold n_pairs * (sweeps + 1) doubles");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  if (h->use_tape) {
+    std::vector<ChainCtl> ctl(h->nchains);
+    KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    KDQ_CUDA(h, cudaMemcpy(ctl.data(), h->ctl.p, ctl.size() * sizeof(ChainCtl), cudaMemcpyDeviceToHost));
+    if ((size_t)ctl[0].tape_pos + (size_t)sweeps * 2 * h->Nt * h->Ns > h->tape_len)
+      return fail(h, KDQ_ERR_STATE, "proposal tape too short for the requested sweeps");
+  }
+  const size_t fs = (size_t)h->Ns * h->ns;
+  k_seed_chains<<<h->nchains, 256, 0, h->stream>>>(h->BRs.p, h->BLs.p, h->Pt.p, h->PtH.p, fs, h->P.sz_chainB,
+                                                   h->NN, h->esz, h->P.lw);
+  KDQ_CUDA(h, cudaGetLastError());
+  k_reset_ctl<<<(h->nchains + 127) / 128, 128, 0, h->stream>>>(h->ctl.as<ChainCtl>(), h->nchains, 1);
+  KDQ_CUDA(h, cudaGetLastError());
+  KDQ_CUDA(h, h->scee_O.alloc(pairs * (size_t)std::max(sweeps, 1) * sizeof(double)));
+  KDQ_CUDA(h, cudaMemsetAsync(h->scee_det.p, 0, pairs * 4 * sizeof(double), h->stream));
+  SweepParams P = h->P;
+  P.scee_O = h->scee_O.as<double>();
+  P.scee_O_cap = std::max(sweeps, 1);
+  P.record = 0;
+  const bool kc = h->kc;
+  auto t0 = std::chrono::steady_clock::now();
+  KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_INIT, 0, h->maxrm, kc, (int)pairs, h->stream));
+  for (int w = 0; w < sweeps; ++w) {
+    for (int k = 1; k <= h->NN - 1; ++k) KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_FWD, k, h->maxrm, kc, (int)pairs, h->stream));
+    for (int k = h->NN - 1; k >= 1; --k) KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_BWD, k, h->maxrm, kc, (int)pairs, h->stream));
+  }
+  if (int rc = kdq_synchronize(h)) return rc;
+  h->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::vector<double> rows(pairs * (size_t)std::max(sweeps, 1));
+  if (sweeps > 0)
+    KDQ_CUDA(h, cudaMemcpy(rows.data(), h->scee_O.p, rows.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (size_t p = 0; p < pairs; ++p) {
+    O[p * (sweeps + 1)] = h->scee_lam;
+    for (int w = 0; w < sweeps; ++w) O[p * (sweeps + 1) + 1 + w] = rows[p * std::max(sweeps, 1) + w];
+  }
+  h->initialised = false;   // G and the chains now hold the SCEE state
+  return KDQ_OK;
+}
+
+int kdq_scee_get_green(kdq_handle* h, int32_t chain, int32_t which, double* G, size_t len) {
+  if (!h || !G) return fail(h, KDQ_ERR_ARG, "NULL argument");
+  if (!h->scee) return fail(h, KDQ_ERR_STATE, "kdq_scee_enable must precede kdq_scee_get_green");
+  if (chain < 0 || chain >= h->nchains || which < 0 || which > 3) return fail(h, KDQ_ERR_ARG, "chain or which out of range");
+  const size_t NN2 = (size_t)h->Ns * h->Ns;
+  if (len != NN2 * 2) return fail(h, KDQ_ERR_ARG, "G must hold 2 Ns^2 doubles (complex)");
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  const DevBuf* src[4] = {&h->G, &h->scee_G0, &h->scee_Gt0, &h->scee_G0t};
+  KDQ_CUDA(h, cudaMemcpy(G, static_cast<const uint8_t*>(src[which]->p) + (size_t)chain * NN2 * h->esz,
+                         NN2 * h->esz, cudaMemcpyDeviceToHost));
   return KDQ_OK;
 }
 

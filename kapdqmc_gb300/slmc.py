@@ -29,14 +29,18 @@ def cnn_fields(s):
     return np.ascontiguousarray(np.transpose(s, (0, 2, 1)))
 
 
-def init_params(seed: int = 0) -> np.ndarray:
+def init_params(seed: int = 0, zero_output: bool = False) -> np.ndarray:
     """Random initial parameters (float32, NPARAM): N(0, 1/6) for W1,
-    N(0, 1/12) for W2 and W3, zero biases."""
+    N(0, 1/12) for W2 and W3, zero biases.  ``zero_output`` starts the last
+    layer at zero, so that the untrained F is the constant the standardised
+    target is centred on (the summed output otherwise starts with a spread
+    of order sqrt(Nt Ns) times the target's)."""
     rng = np.random.default_rng(seed)
     p = np.zeros(NPARAM, dtype=np.float32)
     p[0:576] = rng.normal(0, 1 / 6, 576)
     p[592:2896] = rng.normal(0, 1 / 12, 2304)
-    p[2912:3056] = rng.normal(0, 1 / 12, 144)
+    if not zero_output:
+        p[2912:3056] = rng.normal(0, 1 / 12, 144)
     return p
 
 
@@ -104,7 +108,7 @@ def fit_effective_model(fields, logdet, epochs: int = 20, batch: int = 64, lr: f
     f, (n, Nt, Ns) = _shape(fields)
     t = 2.0 * np.asarray(logdet, dtype=np.float64)
     mu, sd = float(t.mean()), float(t.std()) or 1.0
-    p0 = init_params(seed) if params is None else _params(params).copy()
+    p0 = init_params(seed, zero_output=True) if params is None else _params(params).copy()
     p, loss = cnn_train(f, (t - mu) / sd, p0, epochs, batch, lr, seed, device)
     p = p.astype(np.float64)
     p[2912:3056] *= sd                       # W3

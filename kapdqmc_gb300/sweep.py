@@ -255,6 +255,27 @@ class Sweeper:
             raise ValueError("params must hold 3057 floats")
         self._ck(self.lib.kdq_slmc_enable(self.h, p.ctypes.data, moves_per_slice, cluster_len, eff_steps))
 
+    def scee_enable(self, indexA, indexB, lam: float, nlam: int):
+        """Regions (1-based sites), lambda and Nlambda of the coupled SCEE sweep."""
+        a = np.ascontiguousarray(np.asarray(indexA, dtype=np.int32))
+        b = np.ascontiguousarray(np.asarray(indexB, dtype=np.int32))
+        self._ck(self.lib.kdq_scee_enable(self.h, a.ctypes.data, a.size, b.ctypes.data, b.size, float(lam), int(nlam)))
+
+    def scee_run(self, sweeps: int):
+        """Coupled SCEE sweeps of every replica pair; returns (n_pairs, sweeps + 1)
+        rows as ctrl_SCEEicr writes them (lambda, then one estimator per sweep)."""
+        npairs = self.nchains // 2
+        out = np.empty(npairs * (sweeps + 1))
+        self._ck(self.lib.kdq_scee_run(self.h, sweeps, out.ctypes.data, out.size))
+        return out.reshape(npairs, sweeps + 1)
+
+    def scee_green(self, chain: int, which: int):
+        """Green's function `which` (0 Gt, 1 G0, 2 Gt0, 3 G0t) of one replica."""
+        N = self.model.Ns
+        out = np.empty(2 * N * N)
+        self._ck(self.lib.kdq_scee_get_green(self.h, chain, which, out.ctypes.data, out.size))
+        return out.view(np.complex128).reshape(N, N, order="F")
+
     def slmc_stats(self):
         """(proposed, accepted, no-change) cluster moves of the last call."""
         out = np.zeros(3, dtype=np.int64)
@@ -350,6 +371,50 @@ def _append_csv(file, rows):
     with lk, open(file, "a") as io:
         for r in rows:
             io.write(",".join(repr(float(v)) for v in r) + "\n")
+
+
+def _scee_csv_name(path, model, nlam):
+    """src/tU/SCEE.jl:16-32."""
+    def f(x):
+        return repr(float(x))
+
+    site = "[" + ", ".join(str(int(v)) for v in model.site) + "]"
+    name = {"SQUARE90": "□90", "SQUARE45": "□45", "HoneyComb60": "HC", "HoneyComb120": "HC120"}[model.Lattice]
+    if model.Θquench == 0.0:
+        return os.path.join(path, f"tUSCEE{name}_t{f(model.Ht)}U{f(model.Hu1)}size{site}Δt{f(model.Δt)}"
+                                  f"Θ{f(model.Θrelax)}N{nlam}BS{model.BatchSize}.csv")
+    return os.path.join(path, f"tUSCEE{name}_t{f(model.Ht)}U{f(model.Hu1)}_{f(model.Hu2)}size{site}Δt{f(model.Δt)}"
+                              f"Θ{f(model.Θrelax)}_{f(model.Θquench)}N{nlam}BS{model.BatchSize}.csv")
+
+
+def ctrl_SCEEicr(path, model, indexA, indexB, Sweeps: int, λ: float, Nλ: int, ss, record: bool, *,
+                 seed=None, tape=None, device: int = 0):
+    """Coupled incremental SCEE sweep of the replica pair(s) ``ss``
+    (src/tU/SCEE.jl:1-211): returns the updated fields.  ``ss`` is a pair
+    [s1, s2] or a stack of pairs (n_pairs, 2, ...); with ``record`` one CSV row
+    per pair (lambda, then the per-sweep estimator) is appended to the
+    reference's file name under ``path`` and the rows are also returned."""
+    if model.kind != KIND_TU:
+        raise ValueError("ctrl_SCEEicr is implemented for t-U")
+    ss = np.asarray(ss, dtype=np.uint8)
+    single = ss.ndim == 3
+    pairs = ss[None] if single else ss
+    stack = pairs.reshape((-1,) + tuple(model.field_shape))
+    with Sweeper(model, nchains=stack.shape[0], device=device) as sw:
+        sw.set_fields(stack)
+        if tape is not None:
+            sw.set_tape(*tape)
+        else:
+            sw.set_rng(int.from_bytes(os.urandom(8), "little") if seed is None else seed)
+        sw.scee_enable(indexA, indexB, λ, Nλ)
+        O = sw.scee_run(Sweeps)
+        out = sw.get_fields().reshape(pairs.shape)
+    out = out[0] if single else out
+    if record:
+        if path:
+            _append_csv(_scee_csv_name(path, model, Nλ), O)
+        return out, O
+    return out
 
 
 def phy_update(path, model, s, Sweeps: int, record: bool = False, *, seed=None, tape=None,

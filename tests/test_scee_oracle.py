@@ -1,0 +1,112 @@
+"""The coupled SCEE sweep's CPU restatement (oracle/scee_oracle.py) against
+brute-force Green's functions: after updates and node crossings in both
+directions, each replica's G(tau,tau), G(tau0,tau0), G(tau,tau0) and
+G(tau0,tau) equal those computed directly from its fields, and the
+incrementally updated Grover inverse and determinant equal fresh ones."""
+import numpy as np
+import pytest
+
+import cases
+import dqmc_oracle as O
+import philox
+import scee_oracle as S
+from kapdqmc_gb300 import Initial_s, area_index
+
+
+def regions(m):
+    L = m.site[1]
+    A = area_index(m.Lattice, m.site, ([1, 1], [L // 3, L]))
+    B = area_index(m.Lattice, m.site, ([1, 1], [L // 3, 2 * L // 3]))
+    return A, B
+
+
+def brute(sc, r, tau):
+    m, s = sc.m, sc.s[r]
+    sw = O._TUSweep(m, s, O.Tape([], []), False)
+
+    def prod(t2, t1):
+        M = np.eye(m.Ns, dtype=complex)
+        for lt in range(t1 + 1, t2 + 1):
+            M = sw.B_left(lt, M)
+        return M
+
+    t0 = sc.nodes[sc.Θ - 1]
+    Gt, G0 = O.G_tau(m, s, tau), O.G_tau(m, s, t0)
+    I = np.eye(m.Ns)
+    if tau <= t0:
+        return Gt, G0, -(I - Gt) @ np.linalg.inv(prod(t0, tau)), prod(t0, tau) @ Gt
+    return Gt, G0, prod(tau, t0) @ G0, -(I - G0) @ np.linalg.inv(prod(tau, t0))
+
+
+def check(sc, tau, tol=1e-9):
+    for r in range(2):
+        for got, ref in zip((sc.Gt[r], sc.G0[r], sc.Gt0[r], sc.G0t[r]), brute(sc, r, tau)):
+            assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < tol
+    for reg, det, inv in ((sc.A, sc.detA, sc.invA), (sc.B, sc.detB, sc.invB)):
+        d, i = sc.grover(reg)
+        assert abs(det - d) < 1e-9 * d
+        assert np.linalg.norm(inv - i) < 1e-9 * np.linalg.norm(i)
+
+
+@pytest.mark.parametrize("make", [cases.tu_honeycomb, cases.tu_quench])
+def test_scee_state_matches_brute_force(make):
+    m = make()
+    A, B = regions(m)
+    n = S.proposals_per_sweep(m)
+    k, u = philox.tape(9, 0, 0, n)
+    sc = S.SCEE(m, Initial_s(m, 1), Initial_s(m, 2), A, B, 0.5, 2, O.Tape(k, u)).init()
+    check(sc, 0)
+    half = m.Nt // 2
+    for lt in range(1, half + 3):
+        sc.forward_slice(lt)
+        if lt in (2, half - 1, half + 2):
+            check(sc, lt)
+    for lt in range(half + 3, m.Nt + 1):
+        sc.forward_slice(lt)
+    for lt in range(m.Nt, 1, -1):
+        sc.backward_slice(lt)
+        if lt - 1 in (m.Nt - 1, half + 1, 3):
+            check(sc, lt - 1)
+    assert 0 < sum(sc.accepts) < len(sc.accepts)
+
+
+def test_ratio_is_the_reweighted_weight_change():
+    # the acceptance ratio of a replica-1 proposal equals the change of
+    # W(s1) W(s2) |det g_A|^(2 lam) |det g_B|^(2 (1 - lam)) computed from scratch
+    m = cases.tu_honeycomb()
+    A, B = regions(m)
+    lam = 0.3
+    s1, s2 = Initial_s(m, 3), Initial_s(m, 4)
+    sc = S.SCEE(m, s1, s2, A, B, lam, 1, O.Tape([1], [2.0])).init()   # u = 2: rejected, ratio only
+    from kapdqmc_gb300.sweep import log_weight
+
+    def total(ss):
+        t = 0.0
+        for s in ss:
+            t += log_weight(m, s, O.log_det(m, s)[0])
+        G0s = [O.G_tau(m, s, sc.nodes[sc.Θ - 1]) for s in ss]
+        for reg, w in ((sc.A, lam), (sc.B, 1 - lam)):
+            a, b = G0s[0][np.ix_(reg, reg)], G0s[1][np.ix_(reg, reg)]
+            g = 2 * a @ b - a - b + np.eye(len(reg))
+            t += 2 * w * np.log(abs(np.linalg.det(g)))
+        return t
+
+    lt, i = 1, 4
+    for r in range(2):
+        sc.wrap(r, lt, True)
+    sold = int(sc.s[0][i, lt - 1])
+    sx = O._sx(sold, 1)
+    # ratio as the sweep computes it
+    Δ = np.exp(1j * m.α[lt - 1] * (m.η[sx - 1] - m.η[sold - 1])) - 1
+    pc = 1 + Δ * (1 - sc.Gt[0][i, i])
+    rr = Δ / pc
+    p = abs(pc) ** 2 * m.γ[sx - 1] / m.γ[sold - 1]
+    for reg, inv, w in ((sc.A, sc.invA, lam), (sc.B, sc.invB, 1 - lam)):
+        X = 2 * sc.G0[1][np.ix_(reg, reg)] - np.eye(len(reg))
+        a = sc.G0t[0][reg, i] * rr
+        b = (sc.Gt0[0][i, reg] @ X) @ inv
+        p *= abs(1 + b @ a) ** (2 * w)
+    s1n = sc.s[0].copy()
+    s1n[i, lt - 1] = sx
+    dw = total([s1n, sc.s[1]]) - total([sc.s[0], sc.s[1]])
+    assert abs(dw - np.log(p)) < 1e-8, (dw, np.log(p))
