@@ -20,7 +20,7 @@ LIB = PKG / "libkapdqmc_gpu.so"
 INCLUDE = PKG.parent / "include"
 UNITS = ["kdq_runtime.cu", "kdq_tu.cu", "kdq_tv.cu", "kdq_tuv.cu", "kdq_tu_mx.cu", "kdq_tv_mx.cu",
          "kdq_tuv_mx.cu", "kdq_grover.cu", "kdq_noalloc.cu", "kdq_cnn.cu",
-         "kdq_scee.cu"]
+         "kdq_scee.cu", "kdq_scee_1.cu", "kdq_scee_3.cu", "kdq_scee_6.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", f"-I{INCLUDE}"]
 

@@ -95,7 +95,7 @@ __device__ void mcopy(int n, const T* src, T* dst) {
 // Block product of block k and its inverse (BM_F!, BMinv_F!,
 // src/tU/GreenMatrix.jl:10-47): BM = prod D eK, BMinv = prod eKinv D^-1.
 template <int MAXRM, class T, class KT>
-__device__ void scee_block_mats(Ctx<KDQ_TU, T, KT, T, KT>& c, int k, T* BM, T* BMi) {
+__device__ __noinline__ void scee_block_mats(Ctx<KDQ_TU, T, KT, T, KT>& c, int k, T* BM, T* BMi) {
   const SweepParams& P = c.P;
   const int N = P.Ns;
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
@@ -114,7 +114,7 @@ __device__ void scee_block_mats(Ctx<KDQ_TU, T, KT, T, KT>& c, int k, T* BM, T* B
 
 // BR[i] = orth_cols(BMs[i-1] BR[i-1])
 template <int MAXRM, class T, class KT>
-__device__ void scee_br(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int i) {
+__device__ __noinline__ void scee_br(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int i) {
   const int N = c.P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
   const SweepParams& P = c.P;
@@ -125,7 +125,7 @@ __device__ void scee_br(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int
 
 // BL[i] = orth_rows(BL[i+1] BMs[i])
 template <int MAXRM, class T, class KT>
-__device__ void scee_bl(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int i) {
+__device__ __noinline__ void scee_bl(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int i) {
   const int N = c.P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
   const SweepParams& P = c.P;
@@ -147,7 +147,7 @@ __device__ void scee_bl(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int
 
 // out = I - BR (BL BR)^-1 BL at node i (get_G!, src/public/Gupdate.jl:139-157)
 template <int MAXRM, class T, class KT>
-__device__ void scee_green(Ctx<KDQ_TU, T, KT, T, KT>& c, int i, T* out) {
+__device__ __noinline__ void scee_green(Ctx<KDQ_TU, T, KT, T, KT>& c, int i, T* out) {
   const int N = c.P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
   const SweepParams& P = c.P;
@@ -172,7 +172,7 @@ __device__ void scee_green(Ctx<KDQ_TU, T, KT, T, KT>& c, int i, T* out) {
 
 // G4!: the four Green's functions of one replica at node idx
 template <int MAXRM, class T, class KT>
-__device__ void scee_g4(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int idx, bool fwd) {
+__device__ __noinline__ void scee_g4(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int idx, bool fwd) {
   const SweepParams& P = c.P;
   const int N = P.Ns, NN2 = N * N, Th = P.NN / 2 + 1;
   T* Gt = c.G;
@@ -223,7 +223,7 @@ __device__ void scee_g4(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int
 // Grover matrix g = 2 a b - a - b + I of the replicas' G0 on a region; its
 // inverse into inv and |det g|^2 (returned to thread 0)
 template <int MAXRM, class T, class KT>
-__device__ double scee_grover(Ctx<KDQ_TU, T, KT, T, KT>& c, const T* G0a, const T* G0b, const int* idx, int n,
+__device__ __noinline__ double scee_grover(Ctx<KDQ_TU, T, KT, T, KT>& c, const T* G0a, const T* G0b, const int* idx, int n,
                               T* inv, T* wa, T* wb) {
   const int N = c.P.Ns;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -252,7 +252,7 @@ __device__ double scee_grover(Ctx<KDQ_TU, T, KT, T, KT>& c, const T* G0a, const 
 
 // get_ABGM!: four Green's functions of both replicas and both Grover inverses
 template <int MAXRM, class T, class KT>
-__device__ void scee_abgm(Ctx<KDQ_TU, T, KT, T, KT>* c, const SceeChain<T>* q, int idx, bool fwd, int pair) {
+__device__ __noinline__ void scee_abgm(Ctx<KDQ_TU, T, KT, T, KT>* c, const SceeChain<T>* q, int idx, bool fwd, int pair) {
   const SweepParams& P = c[0].P;
   scee_g4<MAXRM>(c[0], q[0], idx, fwd);
   scee_g4<MAXRM>(c[1], q[1], idx, fwd);
