@@ -586,6 +586,72 @@ def run_slmc(args):
     print(json.dumps(out))
 
 
+def run_scee(args):
+    """Coupled SCEE sweep (ctrl_SCEEicr) on a t-U workload: replica pairs of
+    the workload's chains, regions A = the first third of the lattice's
+    columns (all rows), B = its first two thirds of rows (the reference's
+    test regions, test/tU/HCtU_runtests.jl:21-24), lambda = 0.5, Nlambda = 2.
+    Prints pair-sweeps/s on the GPU and, as the CPU baseline, the numpy
+    restatement of the same sweep timed on one host core for one pair."""
+    import torch
+    from kapdqmc_gb300 import Initial_s, area_index
+    from kapdqmc_gb300.sweep import Sweeper
+
+    model = make_model()
+    if model.kind != 0:
+        print(json.dumps({"scee": "unavailable", "why": "the SCEE sweep is implemented for t-U only"}))
+        return
+    L = model.site[1]
+    A = area_index(model.Lattice, model.site, ([1, 1], [L // 3, L]))
+    B = area_index(model.Lattice, model.site, ([1, 1], [L // 3, 2 * L // 3]))
+    pairs = NCHAINS // 2
+    fields = np.stack([Initial_s(model, 9000 + c) for c in range(2 * pairs)])
+    dev = torch.device("cuda", 0)
+    sw = Sweeper(model, 2 * pairs)
+    sw.set_fields(fields)
+    sw.set_rng(4242)
+    sw.scee_enable(A, B, 0.5, 2)
+    sw.scee_run(args.warmup)            # untimed: includes building every block product
+    sw.set_fields(sw.get_fields())
+    stream = torch.cuda.ExternalStream(sw.stream, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    O = sw.scee_run(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    secs = e0.elapsed_time(e1) * 1e-3
+    sw.close()
+    est = O[:, 1:]
+    out = {"metric": "SCEE pair-sweeps/s (ctrl_SCEEicr)", "value": pairs * args.steps / secs,
+           "unit": "pair-sweeps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True, "dtype": "c128",
+           "data": "synthetic (seeded HS fields and Philox stream)",
+           "config": dict(config(), pairs=pairs, nA=len(A), nB=len(B), lam=0.5, nlam=2,
+                          timed="one kdq_scee_run call: block products and chains rebuilt, then the sweeps"),
+           "estimator_mean": float(est.mean()), "estimator_err": float(est.mean(axis=1).std() / math.sqrt(pairs))}
+    if not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import dqmc_oracle as O_
+        import philox
+        import scee_oracle
+        n_rep = 2 * model.Ns * model.Nt
+        k0, u0 = philox.tape(1, 0, 0, n_rep)
+        k1, u1 = philox.tape(1, 1, 0, n_rep)
+        tape = O_.Tape(np.stack([k0, k1], axis=1).ravel(), np.stack([u0, u1], axis=1).ravel())
+        sc = scee_oracle.SCEE(model, fields[0], fields[1], A, B, 0.5, 2, tape).init()
+        n_sl = min(model.Nt, int(model.nodes[3]))     # the first three blocks of the forward sweep
+        t0 = time.perf_counter()
+        for lt in range(1, n_sl + 1):
+            sc.forward_slice(lt)
+        wall = (time.perf_counter() - t0) * (2 * model.Nt) / n_sl
+        cores = os.cpu_count() or 1
+        out["cpu_baseline"] = {"value": cores / wall, "unit": "pair-sweeps/s", "cores": cores, "kind": "port",
+                               "sample": f"numpy restatement of ctrl_SCEEicr, one pair, the first {n_sl} forward "
+                                         f"slices on one core scaled to a sweep ({wall:.1f} s per pair-sweep), "
+                                         f"times the core count"}
+    print(json.dumps(out))
+
+
 def dist_max(dist, value: float, device=None) -> float:
     """Max of a per-rank value over all ranks (identity without a process group)."""
     if dist is None:
@@ -628,6 +694,8 @@ def main():
                     help="arithmetic of the sweep (mixed: complex sweeps only)")
     ap.add_argument("--slmc", action="store_true",
                     help="self-learning cluster moves against local updates (t-U workloads; prints its own line)")
+    ap.add_argument("--scee", action="store_true",
+                    help="coupled SCEE sweep of replica pairs (t-U workloads; prints its own line)")
     ap.add_argument("--slmc-burn", type=int, default=10)
     ap.add_argument("--slmc-train-sweeps", type=int, default=80,
                     help="sweeps of configurations collected for training (x chains configurations)")
@@ -645,7 +713,12 @@ def main():
     if args.impl == "reference" and args.workload != "c2":
         print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement covers the t-V workload only"}))
         return
-    if args.slmc:
+    if args.scee:
+        if args.workload == "c2":
+            WL = WORKLOADS["c5"]
+            NCHAINS = args.chains or WL["chains"]
+        run_scee(args)
+    elif args.slmc:
         if args.workload == "c2":
             WL = WORKLOADS["c5"]
             NCHAINS = args.chains or WL["chains"]

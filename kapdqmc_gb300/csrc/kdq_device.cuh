@@ -164,67 +164,16 @@ __device__ inline double block_sum(double v, double* red) {
 }
 
 // ------------------------------------------------------------------- GEMM
-// C[M x N] = A[M x K] * B[K x N] (column-major, C must not alias A or B).
-// Lane l of a warp owns rows l, l+32, ..., l+32*(MAXRM-1); warps own groups
-// of CB columns.  Each k step loads MAXRM coalesced A values and CB
-// broadcast B values for MAXRM*CB multiply-adds.
-// An optional epilogue scales the result: C[i,j] = rs[i] * acc * cs[j].
-template <int MAXRM, class TA, class TB, class TC, class TS = double>
-__device__ void bgemm(int M, int N, int K, const TA* __restrict__ A, int lda,
-                      const TB* __restrict__ B, int ldb, TC* __restrict__ C, int ldc,
-                      const TS* rs = nullptr, const TS* cs = nullptr) {
-  constexpr int CB = 4;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j0 = warp * CB; j0 < N; j0 += nw * CB) {
-    TC acc[MAXRM][CB];
-#pragma unroll
-    for (int r = 0; r < MAXRM; ++r)
-#pragma unroll
-      for (int c = 0; c < CB; ++c) acc[r][c] = zero<TC>();
-    const TB* Bp[CB];
-#pragma unroll
-    for (int c = 0; c < CB; ++c) Bp[c] = B + (size_t)min(j0 + c, N - 1) * ldb;
-    for (int k = 0; k < K; ++k) {
-      TB b[CB];
-#pragma unroll
-      for (int c = 0; c < CB; ++c) b[c] = Bp[c][k];
-      const TA* Ak = A + (size_t)k * lda;
-#pragma unroll
-      for (int r = 0; r < MAXRM; ++r) {
-        const int i = lane + 32 * r;
-        if (i < M) {
-          TA a = Ak[i];
-#pragma unroll
-          for (int c = 0; c < CB; ++c) madd(acc[r][c], a, b[c]);
-        }
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < CB; ++c) {
-      const int j = j0 + c;
-      if (j >= N) break;
-#pragma unroll
-      for (int r = 0; r < MAXRM; ++r) {
-        const int i = lane + 32 * r;
-        if (i < M) {
-          TC v = acc[r][c];
-          if (rs) v = rs[i] * v;
-          if (cs) v = v * cs[j];
-          C[i + (size_t)j * ldc] = v;
-        }
-      }
-    }
-  }
-  __syncthreads();
-}
-
-// 2-D register-tiled variant: the M x N output is cut into RS x CS micro-
+// C[M x N] = A[M x K] * B[K x N] (column-major, C must not alias A or B),
+// with an optional epilogue C[i,j] = rs[i] * acc * cs[j]; with SUB the
+// result is subtracted from C instead (C -= A B).
+// Register-tiled: the M x N output is cut into RS x CS micro-
 // tiles of TM x TN (RS = ceil(M/TM), CS = ceil(N/TN)); thread t owns the
 // micro-tile (t mod RS, t div RS) with rows r + RS*m and columns c + CS*n,
 // so consecutive lanes load consecutive rows of A and the B values of a
 // warp are near-broadcasts.  When RS*CS is a multiple of 32 no FP64 lane is
 // wasted (the FP64 pipe, not memory, bounds these products on GB300).
-template <int TM, int TN, class TA, class TB, class TC, class TS = double>
+template <int TM, int TN, class TA, class TB, class TC, class TS = double, bool SUB = false>
 __device__ void bgemm_t(int M, int N, int K, const TA* __restrict__ A, int lda,
                         const TB* __restrict__ B, int ldb, TC* __restrict__ C, int ldc,
                         const TS* rs = nullptr, const TS* cs = nullptr) {
@@ -265,6 +214,7 @@ __device__ void bgemm_t(int M, int N, int K, const TA* __restrict__ A, int lda,
         TC v = acc[m][n];
         if (rs) v = rs[i] * v;
         if (cs) v = v * cs[j];
+        if constexpr (SUB) v = C[i + (size_t)j * ldc] - v;   // C -= A B
         C[i + (size_t)j * ldc] = v;
       }
     }

@@ -634,8 +634,7 @@ __device__ void slmc_moves(Ctx<KIND, T, KT, TW, KW>& c, int lt, int visit) {
       Wr[e] = (col == ja ? one<TW>() : zero<TW>()) - c.G[ja + (size_t)col * N];
     }
     __syncthreads();
-    gemm_sq<MAXRM, TW>(N, N, m, U, N, Wr, m, c.W1, N);
-    for (Walk wk(N, N); wk.ok(); wk.next()) c.G[wk.e] = c.G[wk.e] - c.W1[wk.e];
+    bgemm_t<Tiles<MAXRM, TW>::SM, Tiles<MAXRM, TW>::SN, TW, TW, TW, TW, true>(N, N, m, U, N, Wr, m, c.G, N);
     for (int a = tid; a < m; a += blockDim.x) row0[wrapi(i0 + sidx[a], N)] = (uint8_t)cur[sidx[a]];
     __syncthreads();
   }
