@@ -315,6 +315,18 @@ int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int3
 int kdq_scee_run(kdq_handle* h, int32_t sweeps, double* O, size_t len);
 int kdq_scee_get_green(kdq_handle* h, int32_t chain, int32_t which, double* G, size_t len);
 
+/* Disorder-operator sweep ctrl_SCDOPicr(path, model, alpha, indexA, indexB,
+ * Sweeps, lambda, Nlambda, s, record) (src/tU/disorder_operate.jl:1-247),
+ * t-U in FP64: every chain runs on its own, its weight reweighted by
+ * |det X_A|^(2 lambda) |det X_B|^(2 (1-lambda)) with
+ * X = e^{i alpha} I + (1 - e^{i alpha}) G(tau0,tau0)[R,R].  O receives per
+ * chain lambda, then per sweep the mean over slices of
+ * (|det X_A|^2 / |det X_B|^2)^(1/Nlambda); kdq_scee_get_green reads the
+ * chain's Green's functions afterwards. */
+int kdq_dop_enable(kdq_handle* h, double alpha, const int32_t* indexA, int32_t nA, const int32_t* indexB,
+                   int32_t nB, double lambda, int32_t n_lambda);
+int kdq_dop_run(kdq_handle* h, int32_t sweeps, double* O, size_t len);
+
 /* Cluster moves of the last kdq_phy_update / kdq_sweep call, summed over
  * chains: counts[0] proposed, counts[1] accepted, counts[2] proposals in
  * which the effective-model chain changed no site (accepted trivially, not

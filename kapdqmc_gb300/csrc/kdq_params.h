@@ -123,6 +123,8 @@ struct SweepParams {
   const int* scee_idxB;
   int scee_nA, scee_nB, scee_nmax, scee_nlam;
   double scee_lam;
+  int scee_dop;                 // 1: disorder-operator sweep of single chains (ctrl_SCDOPicr)
+  double scee_alpha;            // its angle
   double* scee_det;
   double* scee_O;
   int scee_O_cap;

@@ -956,11 +956,15 @@ int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice,
   return KDQ_OK;
 }
 
-int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB,
-                    double lambda, int32_t n_lambda) {
+namespace {
+// shared set-up of the coupled SCEE sweep (dop = 0: replica pairs) and the
+// disorder-operator sweep (dop = 1: single chains)
+int scee_setup(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB, double lambda,
+               int32_t n_lambda, int dop, double alpha) {
   if (!h) return KDQ_ERR_ARG;
-  if (h->kind != KDQ_TU) return fail(h, KDQ_ERR_ARG, "the coupled SCEE sweep is implemented for t-U only");
-  if (h->nchains % 2) return fail(h, KDQ_ERR_ARG, "the SCEE sweep needs an even number of chains (replica pairs)");
+  if (h->kind != KDQ_TU) return fail(h, KDQ_ERR_ARG, "the SCEE and disorder-operator sweeps are implemented for t-U only");
+  if (!dop && h->nchains % 2) return fail(h, KDQ_ERR_ARG, "the SCEE sweep needs an even number of chains (replica pairs)");
+  if (!std::isfinite(alpha)) return fail(h, KDQ_ERR_ARG, "alpha must be finite");
   if (h->precision != KDQ_PREC_FP64) return fail(h, KDQ_ERR_ARG, "the SCEE sweep runs in FP64 only");
   if (!indexA || !indexB) return fail(h, KDQ_ERR_ARG, "NULL region");
   const int nmax_ok = std::min(h->ns, 96);
@@ -975,7 +979,7 @@ int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int3
   if (n_lambda < 1) return fail(h, KDQ_ERR_ARG, "n_lambda must be >= 1");
   KDQ_CUDA(h, cudaSetDevice(h->device));
   KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
-  const size_t C = h->nchains, NN2 = (size_t)h->Ns * h->Ns, e = h->esz, pairs = C / 2;
+  const size_t C = h->nchains, NN2 = (size_t)h->Ns * h->Ns, e = h->esz, pairs = dop ? C : C / 2;
   const int nmax = std::max(nA, nB);
   if (!h->scee) {
     KDQ_CUDA(h, h->scee_G0.alloc(C * NN2 * e));
@@ -983,8 +987,8 @@ int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int3
     KDQ_CUDA(h, h->scee_G0t.alloc(C * NN2 * e));
     KDQ_CUDA(h, h->scee_BMs.alloc(C * (h->NN - 1) * NN2 * e));
     KDQ_CUDA(h, h->scee_BMi.alloc(C * (h->NN - 1) * NN2 * e));
-    KDQ_CUDA(h, h->scee_det.alloc(pairs * 4 * sizeof(double)));
   }
+  KDQ_CUDA(h, h->scee_det.alloc(pairs * 4 * sizeof(double)));
   KDQ_CUDA(h, h->scee_inv.alloc(pairs * 2 * (size_t)nmax * nmax * e));
   KDQ_CUDA(h, upload(h->scee_idx, idx));
   SweepParams& P = h->P;
@@ -1002,18 +1006,21 @@ int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int3
   P.scee_nlam = n_lambda;
   P.scee_lam = lambda;
   P.scee_det = h->scee_det.as<double>();
+  P.scee_dop = dop;
+  P.scee_alpha = alpha;
   h->scee_lam = lambda;
   h->scee = true;
   return KDQ_OK;
 }
 
-int kdq_scee_run(kdq_handle* h, int32_t sweeps, double* O, size_t len) {
+int scee_run(kdq_handle* h, int32_t sweeps, double* O, size_t len, int dop) {
   if (!h) return KDQ_ERR_ARG;
-  if (!h->scee) return fail(h, KDQ_ERR_STATE, "kdq_scee_enable must precede kdq_scee_run");
+  if (!h->scee || h->P.scee_dop != dop)
+    return fail(h, KDQ_ERR_STATE, dop ? "kdq_dop_enable must precede kdq_dop_run" : "kdq_scee_enable must precede kdq_scee_run");
   if (sweeps < 0) return fail(h, KDQ_ERR_ARG, "sweeps must be >= 0");
-  const size_t pairs = h->nchains / 2;
+  const size_t pairs = dop ? h->nchains : h->nchains / 2;
   if (!O || len != pairs * (size_t)(sweeps + 1))
-    return fail(h, KDQ_ERR_ARG, "O must hold n_pairs * (sweeps + 1) doubles");
+    return fail(h, KDQ_ERR_ARG, dop ? "O must hold n_chains * (sweeps + 1) doubles" : "O must hold n_pairs * (sweeps + 1) doubles");
   KDQ_CUDA(h, cudaSetDevice(h->device));
   if (h->use_tape) {
     std::vector<ChainCtl> ctl(h->nchains);
@@ -1053,6 +1060,21 @@ int kdq_scee_run(kdq_handle* h, int32_t sweeps, double* O, size_t len) {
   h->initialised = false;   // G and the chains now hold the SCEE state
   return KDQ_OK;
 }
+}  // namespace
+
+int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB,
+                    double lambda, int32_t n_lambda) {
+  return scee_setup(h, indexA, nA, indexB, nB, lambda, n_lambda, 0, 0.0);
+}
+
+int kdq_scee_run(kdq_handle* h, int32_t sweeps, double* O, size_t len) { return scee_run(h, sweeps, O, len, 0); }
+
+int kdq_dop_enable(kdq_handle* h, double alpha, const int32_t* indexA, int32_t nA, const int32_t* indexB,
+                   int32_t nB, double lambda, int32_t n_lambda) {
+  return scee_setup(h, indexA, nA, indexB, nB, lambda, n_lambda, 1, alpha);
+}
+
+int kdq_dop_run(kdq_handle* h, int32_t sweeps, double* O, size_t len) { return scee_run(h, sweeps, O, len, 1); }
 
 int kdq_scee_get_green(kdq_handle* h, int32_t chain, int32_t which, double* G, size_t len) {
   if (!h || !G) return fail(h, KDQ_ERR_ARG, "NULL argument");

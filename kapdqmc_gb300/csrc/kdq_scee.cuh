@@ -250,17 +250,52 @@ __device__ __noinline__ double scee_grover(Ctx<KDQ_TU, T, KT, T, KT>& c, const T
   return exp(2.0 * lg);
 }
 
-// get_ABGM!: four Green's functions of both replicas and both Grover inverses
+// Disorder-operator matrix X = e^{i alpha} I + (1 - e^{i alpha}) G0[R,R] of a
+// region (get_ABX!, src/tU/disorder_operate.jl:202-224): inverse into inv,
+// |det X|^2 returned
+template <int MAXRM, class T, class KT>
+__device__ __noinline__ double scee_xmat(Ctx<KDQ_TU, T, KT, T, KT>& c, const T* G0, const int* idx, int n, T* inv) {
+  const int N = c.P.Ns;
+  double sn, cs;
+  sincos(c.P.scee_alpha, &sn, &cs);
+  const T e = cvt<T>(cd{cs, sn});
+  const T om = one<T>() - e;
+  for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
+    const int i = q % n, j = q / n;
+    T x = om * G0[idx[i] + (size_t)idx[j] * N];
+    if (i == j) x = x + e;
+    inv[q] = x;
+  }
+  __syncthreads();
+  __shared__ int bad;
+  __shared__ T fcol[KDQ_SCEE_MAXR];
+  __shared__ double lg;
+  __shared__ cd ph;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  gj_inverse(n, inv, fcol, c.piv, &bad, &lg, &ph);
+  if (threadIdx.x == 0 && bad) atomicOr(&c.ctl->err, KDQ_FLAG_SINGULAR);
+  return exp(2.0 * lg);
+}
+
+// get_ABGM! (get_ABX! for the disorder operator): four Green's functions of
+// the replicas and the inverses of both region matrices
 template <int MAXRM, class T, class KT>
 __device__ __noinline__ void scee_abgm(Ctx<KDQ_TU, T, KT, T, KT>* c, const SceeChain<T>* q, int idx, bool fwd, int pair) {
   const SweepParams& P = c[0].P;
   scee_g4<MAXRM>(c[0], q[0], idx, fwd);
-  scee_g4<MAXRM>(c[1], q[1], idx, fwd);
+  if (!P.scee_dop) scee_g4<MAXRM>(c[1], q[1], idx, fwd);
   const size_t rs = (size_t)P.scee_nmax * P.scee_nmax;
   T* invA = static_cast<T*>(P.scee_inv) + (size_t)pair * 2 * rs;
   T* invB = invA + rs;
-  const double dA = scee_grover<MAXRM>(c[0], q[0].G0, q[1].G0, P.scee_idxA, P.scee_nA, invA, c[0].W1, c[0].W2);
-  const double dB = scee_grover<MAXRM>(c[0], q[0].G0, q[1].G0, P.scee_idxB, P.scee_nB, invB, c[0].W1, c[0].W2);
+  double dA, dB;
+  if (P.scee_dop) {
+    dA = scee_xmat<MAXRM>(c[0], q[0].G0, P.scee_idxA, P.scee_nA, invA);
+    dB = scee_xmat<MAXRM>(c[0], q[0].G0, P.scee_idxB, P.scee_nB, invB);
+  } else {
+    dA = scee_grover<MAXRM>(c[0], q[0].G0, q[1].G0, P.scee_idxA, P.scee_nA, invA, c[0].W1, c[0].W2);
+    dB = scee_grover<MAXRM>(c[0], q[0].G0, q[1].G0, P.scee_idxB, P.scee_nB, invB, c[0].W1, c[0].W2);
+  }
   if (threadIdx.x == 0) {
     P.scee_det[(size_t)pair * 4 + 0] = dA;
     P.scee_det[(size_t)pair * 4 + 1] = dB;
@@ -332,7 +367,17 @@ __device__ void scee_propose(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q
       T x = 2.0 * qo.G0[ix[l] + (size_t)ix[j] * N];
       return l == j ? x - one<T>() : x;
     };
-    if (r == 0) {   // get_abTau1!: a = G0t[A,i] r, b = Gt0[i,A] X inv
+    if (P.scee_dop) {   // get_abTau! (DOPBuffer_): a = (1 - e^{i alpha}) G0t[R,i] r, b = Gt0[i,R] Xinv
+      double sn, cs;
+      sincos(P.scee_alpha, &sn, &cs);
+      const T om = one<T>() - cvt<T>(cd{cs, sn});
+      for (int l = threadIdx.x; l < n; l += blockDim.x) {
+        ss.a[g][l] = om * (q.G0t[ix[l] + (size_t)i * N] * rr);
+        ss.v[l] = q.Gt0[i + (size_t)ix[l] * N];
+      }
+      __syncthreads();
+      vecmat<T>(n, ss.v, [&](int l, int j) { return iv[l + (size_t)j * n]; }, ss.b[g], ss.part);
+    } else if (r == 0) {   // get_abTau1!: a = G0t[A,i] r, b = Gt0[i,A] X inv
       for (int l = threadIdx.x; l < n; l += blockDim.x) {
         ss.a[g][l] = q.G0t[ix[l] + (size_t)i * N] * rr;
         ss.v[l] = q.Gt0[i + (size_t)ix[l] * N];
@@ -425,22 +470,23 @@ __device__ void scee_layer(Ctx<KDQ_TU, T, KT, T, KT>* c, const SceeChain<T>* q, 
   const SweepParams& P = c[0].P;
   const int N = P.Ns, Nt = P.Nt;
   const uint32_t qs = fwd ? (uint32_t)(lt - 1) * N : (uint32_t)(Nt + (Nt - lt)) * N;
+  const bool two = !P.scee_dop;
   load_tape(c[0], qs, N);
-  load_tape(c[1], qs, N);
+  if (two) load_tape(c[1], qs, N);
   const long long lb0 = c[0].ctl->log_pos, lb1 = c[1].ctl->log_pos;
   for (int i = 0; i < N; ++i) {
     scee_propose<MAXRM>(c[0], q[0], q[1], 0, lt, i, c[0].tk[i], c[0].tu[i], lb0 + i, ss, pair);
-    scee_propose<MAXRM>(c[1], q[1], q[0], 1, lt, i, c[1].tk[i], c[1].tu[i], lb1 + i, ss, pair);
+    if (two) scee_propose<MAXRM>(c[1], q[1], q[0], 1, lt, i, c[1].tk[i], c[1].tu[i], lb1 + i, ss, pair);
   }
   if (threadIdx.x == 0) {
     c[0].ctl->log_pos += N;
-    c[1].ctl->log_pos += N;
+    if (two) c[1].ctl->log_pos += N;
     double* dt = P.scee_det + (size_t)pair * 4;
     dt[2] += pow(dt[0] / dt[1], 1.0 / P.scee_nlam);   // (detg_A / detg_B)^(1/Nlambda)
     dt[3] += 1.0;
   }
   finish_tape(c[0], N);
-  finish_tape(c[1], N);
+  if (two) finish_tape(c[1], N);
   __syncthreads();
 }
 
@@ -454,8 +500,9 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
   SceeSmem<T>& ss = *reinterpret_cast<SceeSmem<T>*>(reinterpret_cast<unsigned char*>(dyn_d) + scee_tape_bytes(N));
   PhaseClock clk;
   clk.start(nullptr);
+  const int nrep = P.scee_dop ? 1 : 2;
   auto mk = [&](int r) {
-    const int chain = 2 * pair + r;
+    const int chain = nrep * pair + (r < nrep ? r : 0);
     const size_t cNN = (size_t)chain * P.sz_NN, cNn = (size_t)chain * P.sz_Nn;
     double* tu = dyn_d + (size_t)r * N;
     uint8_t* tk = reinterpret_cast<uint8_t*>(dyn_d + 2 * (size_t)N) + (size_t)r * N;
@@ -472,11 +519,11 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
                                       static_cast<const KT*>(P.K), clk};
   };
   Ctx<KDQ_TU, T, KT, T, KT> c[2] = {mk(0), mk(1)};
-  const SceeChain<T> q[2] = {scee_chain<T>(P, 2 * pair), scee_chain<T>(P, 2 * pair + 1)};
+  const SceeChain<T> q[2] = {scee_chain<T>(P, nrep * pair), scee_chain<T>(P, nrep * pair + nrep - 1)};
   const int NN = P.NN, Th = NN / 2 + 1;
   if (mode == KDQ_MODE_INIT) {
     // block products, both stabilised chains, then the state at node 1
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < nrep; ++r) {
       for (int b = 1; b < NN; ++b)
         scee_block_mats<MAXRM>(c[r], b, q[r].BMs + (size_t)(b - 1) * N * N, q[r].BMi + (size_t)(b - 1) * N * N);
       for (int i = 1; i < NN; ++i) {
@@ -491,11 +538,11 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
   if (mode == KDQ_MODE_FWD) {   // idx == k while these slices run
     for (int lt = lo + 1; lt <= hi; ++lt) {
       scee_wrap<MAXRM>(c[0], q[0], lt, true);
-      scee_wrap<MAXRM>(c[1], q[1], lt, true);
+      if (nrep == 2) scee_wrap<MAXRM>(c[1], q[1], lt, true);
       scee_layer<MAXRM>(c, q, lt, true, ss, pair);
     }
     const int idx = k + 1;   // lt == nodes[idx]
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < nrep; ++r) {
       scee_block_mats<MAXRM>(c[r], idx - 1, q[r].BMs + (size_t)(idx - 2) * N * N,
                              q[r].BMi + (size_t)(idx - 2) * N * N);
       for (int i = idx; i <= max(Th, idx); ++i) scee_br<MAXRM>(c[r], q[r], i);
@@ -507,7 +554,7 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
       scee_layer<MAXRM>(c, q, lt, false, ss, pair);
       if (lt - 1 == lo) {
         const int idx = k;
-        for (int r = 0; r < 2; ++r) {
+        for (int r = 0; r < nrep; ++r) {
           scee_block_mats<MAXRM>(c[r], idx, q[r].BMs + (size_t)(idx - 1) * N * N, q[r].BMi + (size_t)(idx - 1) * N * N);
           for (int i = idx; i >= min(Th, idx); --i) scee_bl<MAXRM>(c[r], q[r], i);
           for (int i = idx + 1; i <= max(Th, idx); ++i) scee_br<MAXRM>(c[r], q[r], i);
@@ -515,7 +562,7 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
         scee_abgm<MAXRM>(c, q, idx, false, pair);
       } else {
         scee_wrap<MAXRM>(c[0], q[0], lt, false);
-        scee_wrap<MAXRM>(c[1], q[1], lt, false);
+        if (nrep == 2) scee_wrap<MAXRM>(c[1], q[1], lt, false);
       }
     }
     if (k == 1 && threadIdx.x == 0) {   // end of the sweep: one estimator row
@@ -524,7 +571,7 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
       c[0].ctl->obs_slot += 1;
       dt[2] = dt[3] = 0.0;
       c[0].ctl->sweep += 1;
-      c[1].ctl->sweep += 1;
+      if (nrep == 2) c[1].ctl->sweep += 1;
     }
   }
 }

@@ -269,6 +269,20 @@ class Sweeper:
         self._ck(self.lib.kdq_scee_run(self.h, sweeps, out.ctypes.data, out.size))
         return out.reshape(npairs, sweeps + 1)
 
+    def dop_enable(self, alpha: float, indexA, indexB, lam: float, nlam: int):
+        """Angle, regions (1-based sites), lambda and Nlambda of the disorder-operator sweep."""
+        a = np.ascontiguousarray(np.asarray(indexA, dtype=np.int32))
+        b = np.ascontiguousarray(np.asarray(indexB, dtype=np.int32))
+        self._ck(self.lib.kdq_dop_enable(self.h, float(alpha), a.ctypes.data, a.size, b.ctypes.data, b.size,
+                                         float(lam), int(nlam)))
+
+    def dop_run(self, sweeps: int):
+        """Disorder-operator sweeps of every chain; returns (n_chains, sweeps + 1)
+        rows as ctrl_SCDOPicr writes them."""
+        out = np.empty(self.nchains * (sweeps + 1))
+        self._ck(self.lib.kdq_dop_run(self.h, sweeps, out.ctypes.data, out.size))
+        return out.reshape(self.nchains, sweeps + 1)
+
     def scee_green(self, chain: int, which: int):
         """Green's function `which` (0 Gt, 1 G0, 2 Gt0, 3 G0t) of one replica."""
         N = self.model.Ns
@@ -413,6 +427,48 @@ def ctrl_SCEEicr(path, model, indexA, indexB, Sweeps: int, λ: float, Nλ: int, 
     if record:
         if path:
             _append_csv(_scee_csv_name(path, model, Nλ), O)
+        return out, O
+    return out
+
+
+def _dop_csv_name(path, model, nlam):
+    """src/tU/disorder_operate.jl:15-31 (the quench variant keyed on a non-constant alpha profile)."""
+    def f(x):
+        return repr(float(x))
+
+    site = "[" + ", ".join(str(int(v)) for v in model.site) + "]"
+    name = {"SQUARE90": "□90", "SQUARE45": "□45", "HoneyComb60": "HC", "HoneyComb120": "HC120"}[model.Lattice]
+    if len(np.unique(model.α)) == 1:
+        return os.path.join(path, f"tUSCDOP{name}_t{f(model.Ht)}U{f(model.Hu1)}size{site}Δt{f(model.Δt)}"
+                                  f"Θ{f(model.Θrelax)}N{nlam}BS{model.BatchSize}.csv")
+    return os.path.join(path, f"tUSCDOP{name}_t{f(model.Ht)}U{f(model.Hu1)}_{f(model.Hu2)}size{site}Δt{f(model.Δt)}"
+                              f"Θ{f(model.Θrelax)}_{f(model.Θquench)}N{nlam}BS{model.BatchSize}.csv")
+
+
+def ctrl_SCDOPicr(path, model, alpha: float, indexA, indexB, Sweeps: int, λ: float, Nλ: int, s, record: bool, *,
+                  seed=None, tape=None, device: int = 0):
+    """Disorder-operator sweep of the field(s) ``s`` (src/tU/disorder_operate.jl:
+    1-247): returns the updated field(s); with ``record`` one CSV row per chain
+    (lambda, then the per-sweep estimator) is appended under ``path`` and the
+    rows are also returned."""
+    if model.kind != KIND_TU:
+        raise ValueError("ctrl_SCDOPicr is implemented for t-U")
+    s = np.asarray(s, dtype=np.uint8)
+    single = s.shape == tuple(model.field_shape)
+    stack = s[None] if single else s
+    with Sweeper(model, nchains=stack.shape[0], device=device) as sw:
+        sw.set_fields(stack)
+        if tape is not None:
+            sw.set_tape(*tape)
+        else:
+            sw.set_rng(int.from_bytes(os.urandom(8), "little") if seed is None else seed)
+        sw.dop_enable(alpha, indexA, indexB, λ, Nλ)
+        O = sw.dop_run(Sweeps)
+        out = sw.get_fields()
+    out = out[0] if single else out
+    if record:
+        if path:
+            _append_csv(_dop_csv_name(path, model, Nλ), O)
         return out, O
     return out
 

@@ -37,6 +37,7 @@ class SCEE:
         self.I = np.eye(model.Ns, dtype=np.complex128)
         self.accepts: list = []
         self.O: list = []
+        self.nrep = 2
 
     # slice matrices (BM_F!, BMinv_F!: src/tU/GreenMatrix.jl:10-47) --------
     def D(self, r, lt, sign=1.0):
@@ -161,7 +162,7 @@ class SCEE:
         self.BR = [[None] * (NN + 1) for _ in range(2)]
         self.Gt, self.G0, self.Gt0, self.G0t = [None] * 2, [None] * 2, [None] * 2, [None] * 2
         Pt = self.m.Pt.astype(np.complex128)
-        for r in range(2):
+        for r in range(self.nrep):
             for idx in range(1, NN):
                 self.BMs[r][idx] = self.BM(r, idx)
                 self.BMi[r][idx] = self.BMinv(r, idx)
@@ -176,14 +177,14 @@ class SCEE:
 
     def forward_slice(self, lt):
         Θ = self.Θ
-        for r in range(2):
+        for r in range(self.nrep):
             self.wrap(r, lt, True)
         self.layer(lt)
         val = (self.detA / self.detB) ** (1 / self.nlam)
         if lt in self.nodes:
             self.idx += 1
             idx = self.idx
-            for r in range(2):
+            for r in range(self.nrep):
                 self.BMs[r][idx - 1] = self.BM(r, idx - 1)
                 self.BMi[r][idx - 1] = self.BMinv(r, idx - 1)
                 for i in range(idx, max(Θ, idx) + 1):
@@ -200,7 +201,7 @@ class SCEE:
         if (lt - 1) in self.nodes:
             self.idx -= 1
             idx = self.idx
-            for r in range(2):
+            for r in range(self.nrep):
                 self.BMs[r][idx] = self.BM(r, idx)
                 self.BMi[r][idx] = self.BMinv(r, idx)
                 for i in range(idx, min(Θ, idx) - 1, -1):
@@ -209,7 +210,7 @@ class SCEE:
                     self.BR[r][i] = O.orth_cols(self.BMs[r][i - 1] @ self.BR[r][i - 1])
             self.ABGM(idx, False)
         else:
-            for r in range(2):
+            for r in range(self.nrep):
                 self.wrap(r, lt, False)
         return val
 
@@ -228,7 +229,79 @@ def proposals_per_sweep(model) -> int:
     return 4 * model.Ns * model.Nt
 
 
+def ctrl_SCDOPicr(model, alpha, indexA, indexB, sweeps, lam, nlam, s, tape: O.Tape):
+    """Disorder-operator sweep of the field ``s``; returns the DOP object."""
+    return DOP(model, s, alpha, indexA, indexB, lam, nlam, tape).run(sweeps)
+
+
 def ctrl_SCEEicr(model, indexA, indexB, sweeps, lam, nlam, ss, tape: O.Tape):
     """Run ``sweeps`` coupled sweeps of the replica pair ``ss``; returns the
     SCEE object (fields ``s``, ``O`` per sweep, Green's functions, accepts)."""
     return SCEE(model, ss[0], ss[1], indexA, indexB, lam, nlam, tape).run(sweeps)
+
+
+class DOP(SCEE):
+    """ctrl_SCDOPicr (src/tU/disorder_operate.jl:1-247): one replica, its
+    weight reweighted by |det X_A|^(2 λ) |det X_B|^(2 (1 - λ)) with the
+    disorder-operator matrices X = e^{iα} I + (1 - e^{iα}) G0[R,R] (get_ABX!,
+    :202-224); the estimator is (|det X_A|^2 / |det X_B|^2)^(1/Nλ).  Updates
+    follow UpdateSCDOPLayer! (:225-247) with get_abTau! for DOPBuffer_
+    (src/public/Gupdate.jl:60-81): a = (1 - e^{iα}) G0t[R,i] r,
+    b = Gt0[i,R] Xinv, Tau = 1 + b a."""
+
+    def __init__(self, model, s, alpha, indexA, indexB, lam, nlam, tape):
+        super().__init__(model, s, s, indexA, indexB, lam, nlam, tape)
+        self.s = self.s[:1]
+        self.alpha = alpha
+        self.nrep = 1
+
+    def xmat(self, reg):
+        e = np.exp(1j * self.alpha)
+        X = (1 - e) * self.G0[0][np.ix_(reg, reg)] + e * np.eye(len(reg))
+        return abs(np.linalg.det(X)) ** 2, np.linalg.inv(X)
+
+    def ABGM(self, idx, forward):   # get_ABX!
+        self.G4(0, idx, forward)
+        self.detA, self.invA = self.xmat(self.A)
+        self.detB, self.invB = self.xmat(self.B)
+
+    def propose(self, r, lt, i):
+        m, s = self.m, self.s[0]
+        k, u = self.tape.draw()
+        sold = int(s[i, lt - 1])
+        sx = O._sx(sold, k)
+        Δ = np.exp(1j * m.α[lt - 1] * (m.η[sx - 1] - m.η[sold - 1])) - 1
+        Gt, Gt0, G0t = self.Gt[0], self.Gt0[0], self.G0t[0]
+        pc = 1 + Δ * (1 - Gt[i, i])
+        rr = Δ / pc
+        p = abs(pc) ** 2 * m.γ[sx - 1] / m.γ[sold - 1]
+        e = np.exp(1j * self.alpha)
+        taus = []
+        for reg, inv in ((self.A, self.invA), (self.B, self.invB)):
+            a = (1 - e) * (G0t[reg, i] * rr)
+            b = Gt0[i, reg] @ inv
+            taus.append((a, b, 1 + b @ a))
+        dA, dB = abs(taus[0][2]) ** 2, abs(taus[1][2]) ** 2
+        p *= dA ** self.lam * dB ** (1 - self.lam)
+        acc = u < p
+        self.accepts.append(bool(acc))
+        if acc:
+            self.detA *= dA
+            self.detB *= dB
+            for (a, b, tau), name in zip(taus, ("invA", "invB")):
+                inv = getattr(self, name)
+                setattr(self, name, inv - np.outer(inv @ a, b) / tau)
+            G0 = self.G0[0]
+            zN = rr * Gt0[i, :]
+            c0t, ct = G0t[:, i].copy(), Gt[:, i].copy()
+            G0 += np.outer(c0t, zN)
+            Gt0 += np.outer(ct, zN)
+            zN = -rr * Gt[i, :]
+            zN[i] += rr
+            G0t -= np.outer(c0t, zN)
+            Gt -= np.outer(ct, zN)
+            s[i, lt - 1] = sx
+
+    def layer(self, lt):   # UpdateSCDOPLayer!
+        for i in range(self.m.Ns):
+            self.propose(0, lt, i)

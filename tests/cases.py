@@ -61,3 +61,24 @@ def c5():
     """t-U 9x9 honeycomb, U=4, dt=0.1, 2Θ=20 (200 slices), n_wrap=10."""
     return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Δt=0.1, Θrelax=10.0, Θquench=0.0,
                            Lattice="HoneyComb120", site=[9, 9], BatchSize=10, Initial="H0")
+
+
+def tu_square90_flux():
+    # the reference's π-flux test lattice (test/tU/□tU_runtests.jl:44-45), 4x4 instead of 6x6
+    return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Θrelax=1.0, Θquench=0.0, Lattice="SQUARE90",
+                           site=[4, 4], Δt=0.1, BatchSize=5, Initial="H0", flux=3.141592653589793)
+
+
+def tu_honeycomb60():
+    return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Δt=0.1, Θrelax=1.0, Θquench=0.0,
+                           Lattice="HoneyComb60", site=[3, 3], BatchSize=5, Initial="H0")
+
+
+def tv_honeycomb60():
+    return tV_Hubbard_Para(Ht=1.0, Hv1=1.0, Hv2=1.0, Δt=0.1, Θrelax=1.0, Θquench=0.0,
+                           Lattice="HoneyComb60", site=[3, 3], BatchSize=5, Initial="H0")
+
+
+def tuv_honeycomb60():
+    return tUV_Hubbard_Para(Ht=1.0, Hu=4.0, Hv=0.5, Lattice="HoneyComb60", site=[3, 3], Δt=0.1, Θ=1.0,
+                            BatchSize=5, Initial="H0")

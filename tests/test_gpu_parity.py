@@ -77,6 +77,13 @@ def test_tu_flux_complex_kinetic():
     _compare(cases.tu_square(flux=np.pi), record=False)
 
 
+@pytest.mark.parametrize("make", [cases.tu_square90_flux, cases.tu_honeycomb60, cases.tv_honeycomb60,
+                                  cases.tuv_honeycomb60])
+def test_other_lattices(make):
+    # SQUARE90 with pi flux (complex hopping) and the HoneyComb60 geometry
+    _compare(make(), record=False)
+
+
 def test_tv_honeycomb():
     _compare(cases.tv_honeycomb())
 

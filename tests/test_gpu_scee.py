@@ -10,7 +10,7 @@ import dqmc_oracle as O
 import philox
 import scee_oracle as S
 from kapdqmc_gb300 import Initial_s, area_index
-from kapdqmc_gb300.sweep import Sweeper, ctrl_SCEEicr
+from kapdqmc_gb300.sweep import Sweeper, ctrl_SCDOPicr, ctrl_SCEEicr
 
 pytestmark = pytest.mark.gpu
 
@@ -70,3 +70,31 @@ def test_ctrl_scee_reference_shaped_call(tmp_path):
     assert O_.shape == (1, 3) and O_[0, 0] == 0.5
     files = list(tmp_path.iterdir())
     assert len(files) == 1 and files[0].name.startswith("tUSCEEHC120_t1.0U4.0size[3, 3]")
+
+
+@pytest.mark.parametrize("make,alpha", [(cases.tu_honeycomb, 0.7), (cases.tu_quench, 1.9)])
+def test_dop_matches_oracle(make, alpha):
+    m = make()
+    A, B = regions(m)
+    nch, sweeps, seed, lam = 3, 2, 13, 0.4
+    fields = np.stack([Initial_s(m, 90 + c) for c in range(nch)])
+    n_rep = 2 * m.Ns * m.Nt
+    with Sweeper(m, nch) as sw:
+        sw.set_fields(fields)
+        sw.set_rng(seed)
+        sw.enable_accept_log(n_rep * sweeps)
+        sw.dop_enable(alpha, A, B, lam, 2)
+        Orows = sw.dop_run(sweeps)
+        s_gpu = sw.get_fields()
+        acc = sw.accept_log()
+        Gs = [[sw.scee_green(c, w) for w in range(4)] for c in range(nch)]
+    for c in range(nch):
+        ks, us = zip(*(philox.tape(seed, c, w, n_rep) for w in range(sweeps)))
+        ref = S.DOP(m, fields[c], alpha, A, B, lam, 2, O.Tape(np.concatenate(ks), np.concatenate(us))).run(sweeps)
+        np.testing.assert_array_equal(acc[c].astype(bool), np.array(ref.accepts))
+        np.testing.assert_array_equal(s_gpu[c], ref.s[0])
+        for w, G in enumerate((ref.Gt[0], ref.G0[0], ref.Gt0[0], ref.G0t[0])):
+            assert np.linalg.norm(Gs[c][w] - G) / np.linalg.norm(G) < 1e-9
+        np.testing.assert_allclose(Orows[c, 1:], ref.O, rtol=1e-8)
+    out, O_ = ctrl_SCDOPicr("", m, alpha, A, B, 1, lam, 2, fields[0], True, seed=1)
+    assert out.shape == tuple(m.field_shape) and O_.shape == (1, 2)

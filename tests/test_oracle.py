@@ -48,7 +48,8 @@ def test_tape_statistics():
 
 
 @pytest.mark.parametrize("make", [cases.tu_square, cases.tu_honeycomb, cases.tv_honeycomb,
-                                  cases.tuv_honeycomb, cases.tuv_square])
+                                  cases.tuv_honeycomb, cases.tuv_square, cases.tu_square90_flux,
+                                  cases.tu_honeycomb60, cases.tv_honeycomb60, cases.tuv_honeycomb60])
 def test_wrapped_G_matches_brute_force(make):
     model = make()
     sw = _run(model, sweeps=2, record=False)

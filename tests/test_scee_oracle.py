@@ -110,3 +110,55 @@ def test_ratio_is_the_reweighted_weight_change():
     s1n[i, lt - 1] = sx
     dw = total([s1n, sc.s[1]]) - total([sc.s[0], sc.s[1]])
     assert abs(dw - np.log(p)) < 1e-8, (dw, np.log(p))
+
+
+def test_dop_state_and_ratio():
+    # the disorder-operator sweep: state against brute force after updates and
+    # node crossings, the incremental X inverses against fresh ones, and the
+    # ratio against the reweighted weight change
+    m = cases.tu_honeycomb()
+    A, B = regions(m)
+    alpha, lam = 0.7, 0.4
+    n = 2 * m.Ns * m.Nt
+    k, u = philox.tape(4, 0, 0, n)
+    sc = S.DOP(m, Initial_s(m, 5), alpha, A, B, lam, 2, O.Tape(k, u)).init()
+    half = m.Nt // 2
+    for lt in range(1, half + 3):
+        sc.forward_slice(lt)
+    for r_check in (0,):
+        for got, ref in zip((sc.Gt[0], sc.G0[0], sc.Gt0[0], sc.G0t[0]), brute(sc, 0, half + 2)):
+            assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-9
+    for reg, det, inv in ((sc.A, sc.detA, sc.invA), (sc.B, sc.detB, sc.invB)):
+        d, i = sc.xmat(reg)
+        assert abs(det - d) < 1e-9 * d
+        assert np.linalg.norm(inv - i) < 1e-9 * np.linalg.norm(i)
+    assert 0 < sum(sc.accepts) < len(sc.accepts)
+
+    from kapdqmc_gb300.sweep import log_weight
+    sc2 = S.DOP(m, Initial_s(m, 6), alpha, A, B, lam, 1, O.Tape([1], [2.0])).init()
+
+    def total(s):
+        t = log_weight(m, s, O.log_det(m, s)[0])
+        G0 = O.G_tau(m, s, sc2.nodes[sc2.Θ - 1])
+        e = np.exp(1j * alpha)
+        for reg, w in ((sc2.A, lam), (sc2.B, 1 - lam)):
+            X = (1 - e) * G0[np.ix_(reg, reg)] + e * np.eye(len(reg))
+            t += 2 * w * np.log(abs(np.linalg.det(X)))
+        return t
+
+    lt, i = 1, 3
+    sc2.wrap(0, lt, True)
+    sold = int(sc2.s[0][i, lt - 1])
+    sx = O._sx(sold, 1)
+    Δ = np.exp(1j * m.α[lt - 1] * (m.η[sx - 1] - m.η[sold - 1])) - 1
+    pc = 1 + Δ * (1 - sc2.Gt[0][i, i])
+    rr = Δ / pc
+    p = abs(pc) ** 2 * m.γ[sx - 1] / m.γ[sold - 1]
+    e = np.exp(1j * alpha)
+    for reg, inv, w in ((sc2.A, sc2.invA, lam), (sc2.B, sc2.invB, 1 - lam)):
+        a = (1 - e) * (sc2.G0t[0][reg, i] * rr)
+        b = sc2.Gt0[0][i, reg] @ inv
+        p *= abs(1 + b @ a) ** (2 * w)
+    s1 = sc2.s[0].copy()
+    s1[i, lt - 1] = sx
+    assert abs((total(s1) - total(sc2.s[0])) - np.log(p)) < 1e-8
