@@ -650,7 +650,7 @@ __device__ void load_tape(Ctx<KIND, T, KT, TW, KW>& c, uint32_t q0, int n) {
     const bool ok = c.ctl->tape_pos + (size_t)n <= P.tape_len;
     for (int m = threadIdx.x; m < n; m += blockDim.x) {
       c.tk[m] = ok ? P.tape_k[base + m] : 0;
-      c.tu[m] = ok ? P.tape_u[base + m] : 2.0;   // u = 2 rejects
+      c.tu[m] = ok ? P.tape_u[base + m] : HUGE_VAL;   // u = +inf rejects every proposal
     }
     if (!ok && threadIdx.x == 0) atomicOr(&c.ctl->err, KDQ_FLAG_TAPE);
   } else {

@@ -102,14 +102,17 @@ def fit_effective_model(fields, logdet, epochs: int = 20, batch: int = 64, lr: f
 
     The target 2 log|det| is standardised (mean mu, deviation sd) for the fit
     and the scale is folded back into the last layer afterwards, so that the
-    returned parameters give F(s) ~ 2 log|det(P^H B P)| directly.  Returns
-    (params, loss per epoch in standardised units, (mu, sd)).
+    returned parameters give F(s) ~ 2 log|det(P^H B P)| directly.  F sums
+    Nt Ns outputs, so one Adam step moves it by about lr Nt Ns: the step
+    size is lr scaled by min(1, 400 / (Nt Ns)).  Returns (params, loss per
+    epoch in standardised units, (mu, sd)).
     """
     f, (n, Nt, Ns) = _shape(fields)
     t = 2.0 * np.asarray(logdet, dtype=np.float64)
     mu, sd = float(t.mean()), float(t.std()) or 1.0
     p0 = init_params(seed, zero_output=True) if params is None else _params(params).copy()
-    p, loss = cnn_train(f, (t - mu) / sd, p0, epochs, batch, lr, seed, device)
+    lr_eff = lr * min(1.0, 400.0 / (Nt * Ns))
+    p, loss = cnn_train(f, (t - mu) / sd, p0, epochs, batch, lr_eff, seed, device)
     p = p.astype(np.float64)
     p[2912:3056] *= sd                       # W3
     p[3056] = p[3056] * sd + mu / (Nt * Ns)  # b3

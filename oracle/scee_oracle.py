@@ -161,7 +161,7 @@ class SCEE:
         self.BL = [[None] * (NN + 1) for _ in range(2)]
         self.BR = [[None] * (NN + 1) for _ in range(2)]
         self.Gt, self.G0, self.Gt0, self.G0t = [None] * 2, [None] * 2, [None] * 2, [None] * 2
-        Pt = self.m.Pt.astype(np.complex128)
+        Pt = self.m.Pt.astype(self.I.dtype)
         for r in range(self.nrep):
             for idx in range(1, NN):
                 self.BMs[r][idx] = self.BM(r, idx)
@@ -305,3 +305,165 @@ class DOP(SCEE):
     def layer(self, lt):   # UpdateSCDOPLayer!
         for i in range(self.m.Ns):
             self.propose(0, lt, i)
+
+
+class SCEE_TV(SCEE):
+    """ctrl_SCEEicr for t-V (src/tV/SCEE.jl:1-517): real arithmetic, bond
+    fields, rank-2 updates with 2x2 Tau matrices, the Grover determinant
+    itself (not its modulus squared) in the weight, and the bond rotations
+    wrapped direction by direction between the updates of each direction
+    (WrapK! :509-517, WrapV! src/tV/GreenMatrix.jl:99-119)."""
+
+    def __init__(self, model, s1, s2, indexA, indexB, lam, nlam, tape):
+        super().__init__(model, s1, s2, indexA, indexB, lam, nlam, tape)
+        self.I = np.eye(model.Ns)
+        self.tv = []
+        for r in range(2):
+            sw = O._TVSweep(model, self.s[r], O.Tape([], []), False)
+            sw.s = self.s[r]          # share the replica's live field
+            self.tv.append(sw)
+
+    def BM(self, r, idx):   # BM_F!, src/tV/GreenMatrix.jl:12-38
+        M = self.I.copy()
+        for lt in range(self.nodes[idx - 1] + 1, self.nodes[idx] + 1):
+            M = self.tv[r].B_left(lt, M)
+        return M
+
+    def BMinv(self, r, idx):   # BMinv_F!, src/tV/GreenMatrix.jl:40-66
+        sw, M = self.tv[r], self.I.copy()
+        for lt in range(self.nodes[idx - 1] + 1, self.nodes[idx] + 1):
+            M = M @ self.m.eKinv
+            for j in reversed(range(self.m.z)):
+                M = sw.uvR(j, sw.uvR(j, M) * sw.Dj(lt, j, -1.0)[None, :])
+        return M
+
+    def grover(self, reg):   # get_ABGM!, src/tV/SCEE.jl:433-445: det, not its modulus squared
+        a = self.G0[0][np.ix_(reg, reg)]
+        b = self.G0[1][np.ix_(reg, reg)]
+        g = 2 * a @ b - a - b + np.eye(len(reg))
+        return float(np.linalg.det(g)), np.linalg.inv(g)
+
+    def wrapK(self, r, forward):   # WrapK!
+        m = self.m
+        A, Ai = (m.eK, m.eKinv) if forward else (m.eKinv, m.eK)
+        self.Gt[r] = A @ self.Gt[r] @ Ai
+        self.Gt0[r] = A @ self.Gt0[r]
+        self.G0t[r] = self.G0t[r] @ Ai
+
+    def wrapV(self, r, lt, j, forward):   # WrapV! "L", "B", "R" of direction j
+        sw = self.tv[r]
+        d = sw.Dj(lt, j, 1.0 if forward else -1.0)
+        self.Gt0[r] = sw.uvL(j, d[:, None] * sw.uvL(j, self.Gt0[r]))
+        self.Gt[r] = sw.wrapV(self.Gt[r], j, d)
+        self.G0t[r] = sw.uvR(j, sw.uvR(j, self.G0t[r]) / d[None, :])
+
+    def propose_bond(self, r, lt, j, i):   # UpdateSCEELayer!, src/tV/SCEE.jl:447-508
+        m, s, sw = self.m, self.s[r], self.tv[r]
+        x, y = int(sw.X[j][i]), int(sw.Y[j][i])
+        S = [x, y]
+        k, u = self.tape.draw()
+        sold = int(s[i, j, lt - 1])
+        sx = O._sx(sold, k)
+        Δs = m.α[lt - 1] * (m.η[sx - 1] - m.η[sold - 1])                    # get_r!
+        t2 = np.exp(Δs * np.array([1.0, -1.0])) - 1
+        Δ = (sw.uv * t2[None, :]) @ sw.uv
+        Gt, Gt0, G0t = self.Gt[r], self.Gt0[r], self.G0t[r]
+        rm = Δ - Δ @ Gt[np.ix_(S, S)]
+        rm[0, 0] += 1
+        rm[1, 1] += 1
+        p = O.det22(rm)
+        rr = O.inv22(rm) @ Δ
+        p *= m.γ[sx - 1] / m.γ[sold - 1]
+        other = self.G0[1 - r]
+        taus = []
+        for reg, inv in ((self.A, self.invA), (self.B, self.invB)):
+            X = 2 * other[np.ix_(reg, reg)] - np.eye(len(reg))
+            if r == 0:   # get_abTau1!
+                a = G0t[np.ix_(reg, S)] @ rr
+                b = (Gt0[np.ix_(S, reg)] @ X) @ inv
+            else:        # get_abTau2!
+                a = X @ G0t[np.ix_(reg, S)]
+                b = (rr @ Gt0[np.ix_(S, reg)]) @ inv
+            tau = b @ a + np.eye(2)
+            taus.append((a, b, tau, O.det22(tau)))
+        dA, dB = taus[0][3], taus[1][3]
+        p *= np.power(dA, self.lam) * np.power(dB, 1 - self.lam)
+        self.last_p = p
+        acc = u < p
+        self.accepts.append(bool(acc))
+        if acc:
+            self.detA *= dA
+            self.detB *= dB
+            for (a, b, tau, _), name in zip(taus, ("invA", "invB")):   # GMupdate!
+                inv = getattr(self, name)
+                setattr(self, name, inv - (inv @ a) @ O.inv22(tau) @ b)
+            G0 = self.G0[r]                                             # G4update!
+            zN = rr @ Gt0[S, :]
+            c0t, ct = G0t[:, S].copy(), Gt[:, S].copy()
+            G0 += c0t @ zN
+            Gt0 += ct @ zN
+            zN = -rr @ Gt[S, :]
+            zN[:, S] += rr
+            G0t -= c0t @ zN
+            Gt -= ct @ zN
+            s[i, j, lt - 1] = sx
+
+    def layer_dir(self, lt, j):
+        for i in range(self.m.Ns // 2):
+            self.propose_bond(0, lt, j, i)
+            self.propose_bond(1, lt, j, i)
+
+    def estimator(self):
+        return np.power(self.detA / self.detB, 1 / self.nlam)
+
+    def forward_slice(self, lt):   # src/tV/SCEE.jl:87-152
+        for r in range(2):
+            self.wrapK(r, True)
+        for j in reversed(range(self.m.z)):
+            for r in range(2):
+                self.wrapV(r, lt, j, True)
+            self.layer_dir(lt, j)
+        val = self.estimator()
+        if lt in self.nodes:
+            self.node_step(forward=True)
+        return val
+
+    def backward_slice(self, lt):   # src/tV/SCEE.jl:258-330
+        for j in range(self.m.z):
+            self.layer_dir(lt, j)
+            for r in range(2):
+                self.wrapV(r, lt, j, False)
+        for r in range(2):
+            self.wrapK(r, False)
+        val = self.estimator()
+        if (lt - 1) in self.nodes:
+            self.node_step(forward=False)
+        return val
+
+    def node_step(self, forward):
+        Θ = self.Θ
+        if forward:
+            self.idx += 1
+            idx = self.idx
+            for r in range(2):
+                self.BMs[r][idx - 1] = self.BM(r, idx - 1)
+                self.BMi[r][idx - 1] = self.BMinv(r, idx - 1)
+                for i in range(idx, max(Θ, idx) + 1):
+                    self.BR[r][i] = O.orth_cols(self.BMs[r][i - 1] @ self.BR[r][i - 1])
+                for i in range(idx - 1, min(Θ, idx) - 1, -1):
+                    self.BL[r][i] = O.orth_rows(self.BL[r][i + 1] @ self.BMs[r][i])
+        else:
+            self.idx -= 1
+            idx = self.idx
+            for r in range(2):
+                self.BMs[r][idx] = self.BM(r, idx)
+                self.BMi[r][idx] = self.BMinv(r, idx)
+                for i in range(idx, min(Θ, idx) - 1, -1):
+                    self.BL[r][i] = O.orth_rows(self.BL[r][i + 1] @ self.BMs[r][i])
+                for i in range(idx + 1, max(Θ, idx) + 1):
+                    self.BR[r][i] = O.orth_cols(self.BMs[r][i - 1] @ self.BR[r][i - 1])
+        self.ABGM(self.idx, forward)
+
+
+def proposals_per_sweep_tv(model) -> int:
+    return 2 * 2 * (model.Ns // 2) * model.z * model.Nt

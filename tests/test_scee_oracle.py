@@ -77,7 +77,7 @@ def test_ratio_is_the_reweighted_weight_change():
     A, B = regions(m)
     lam = 0.3
     s1, s2 = Initial_s(m, 3), Initial_s(m, 4)
-    sc = S.SCEE(m, s1, s2, A, B, lam, 1, O.Tape([1], [2.0])).init()   # u = 2: rejected, ratio only
+    sc = S.SCEE(m, s1, s2, A, B, lam, 1, O.Tape([1], [float("inf")])).init()   # u = inf: rejected, ratio only
     from kapdqmc_gb300.sweep import log_weight
 
     def total(ss):
@@ -135,7 +135,7 @@ def test_dop_state_and_ratio():
     assert 0 < sum(sc.accepts) < len(sc.accepts)
 
     from kapdqmc_gb300.sweep import log_weight
-    sc2 = S.DOP(m, Initial_s(m, 6), alpha, A, B, lam, 1, O.Tape([1], [2.0])).init()
+    sc2 = S.DOP(m, Initial_s(m, 6), alpha, A, B, lam, 1, O.Tape([1], [float("inf")])).init()
 
     def total(s):
         t = log_weight(m, s, O.log_det(m, s)[0])
@@ -162,3 +162,65 @@ def test_dop_state_and_ratio():
     s1 = sc2.s[0].copy()
     s1[i, lt - 1] = sx
     assert abs((total(s1) - total(sc2.s[0])) - np.log(p)) < 1e-8
+
+
+def brute_tv(sc, r, tau):
+    m, s = sc.m, sc.s[r]
+    sw = O._TVSweep(m, s, O.Tape([], []), False)
+
+    def prod(t2, t1):
+        M = np.eye(m.Ns)
+        for lt in range(t1 + 1, t2 + 1):
+            M = sw.B_left(lt, M)
+        return M
+
+    t0 = sc.nodes[sc.Θ - 1]
+    Gt, G0 = O.G_tau(m, s, tau), O.G_tau(m, s, t0)
+    I = np.eye(m.Ns)
+    if tau <= t0:
+        return Gt, G0, -(I - Gt) @ np.linalg.inv(prod(t0, tau)), prod(t0, tau) @ Gt
+    return Gt, G0, prod(tau, t0) @ G0, -(I - G0) @ np.linalg.inv(prod(tau, t0))
+
+
+def test_scee_tv_state_and_ratio():
+    m = cases.tv_honeycomb()
+    A, B = regions(m)
+    n = S.proposals_per_sweep_tv(m)
+    k, u = philox.tape(9, 0, 0, n)
+    sc = S.SCEE_TV(m, Initial_s(m, 1), Initial_s(m, 2), A, B, 0.5, 2, O.Tape(k, u)).init()
+    half = m.Nt // 2
+    for lt in range(1, m.Nt + 1):
+        sc.forward_slice(lt)
+        if lt in (3, half + 2):
+            for r in range(2):
+                for got, ref in zip((sc.Gt[r], sc.G0[r], sc.Gt0[r], sc.G0t[r]), brute_tv(sc, r, lt)):
+                    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-8
+            for reg, det, inv in ((sc.A, sc.detA, sc.invA), (sc.B, sc.detB, sc.invB)):
+                d, i = sc.grover(reg)
+                assert abs(det - d) < 1e-8 * abs(d)
+                assert np.linalg.norm(inv - i) < 1e-8 * np.linalg.norm(i)
+    assert 0 < sum(sc.accepts) < len(sc.accepts)
+    # ratio of a replica-1 proposal against the reweighted weight change
+    lam = 0.3
+    sc2 = S.SCEE_TV(m, Initial_s(m, 3), Initial_s(m, 4), A, B, lam, 1, O.Tape([1], [float("inf")])).init()
+    from kapdqmc_gb300.sweep import log_weight
+
+    def total(ss):
+        t = sum(log_weight(m, s, O.log_det(m, s)[0]) for s in ss)
+        G0s = [O.G_tau(m, s, sc2.nodes[sc2.Θ - 1]) for s in ss]
+        for reg, w in ((sc2.A, lam), (sc2.B, 1 - lam)):
+            a, b = G0s[0][np.ix_(reg, reg)], G0s[1][np.ix_(reg, reg)]
+            t += w * np.log(abs(np.linalg.det(2 * a @ b - a - b + np.eye(len(reg)))))
+        return t
+
+    lt, j, i = 1, m.z - 1, 2
+    for r in range(2):
+        sc2.wrapK(r, True)
+        sc2.wrapV(r, lt, j, True)
+    sc2.propose_bond(0, lt, j, i)      # u = inf: rejected, the ratio is kept
+    p = sc2.last_p
+    s1 = sc2.s[0].copy()
+    sold = int(s1[i, j, lt - 1])
+    s1[i, j, lt - 1] = O._sx(sold, 1)
+    dw = total([s1, sc2.s[1]]) - total(sc2.s)
+    assert p > 0 and abs(dw - np.log(p)) < 1e-8, (dw, np.log(p))
