@@ -294,7 +294,8 @@ int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice,
                     int32_t eff_steps);
 
 /* Coupled incremental SCEE sweep, ctrl_SCEEicr(path, model, indexA, indexB,
- * Sweeps, lambda, Nlambda, ss, record) (src/tU/SCEE.jl:1-211), t-U in FP64.
+ * Sweeps, lambda, Nlambda, ss, record) (src/tU/SCEE.jl:1-211,
+ * src/tV/SCEE.jl:1-431), t-U and t-V in FP64.
  * Chains 2p and 2p+1 of the handle are the two replicas ss[1], ss[2] of pair
  * p (fields through kdq_set_fields, random stream through kdq_set_rng or
  * kdq_set_tape, replica r of pair p drawing from chain 2p+r's stream in the
@@ -303,12 +304,16 @@ int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice,
  * builds every replica's block products and stabilised chains and runs
  * `sweeps` coupled sweeps: each site proposal of either replica is accepted
  * with its local ratio times |det g_A'/det g_A|^(2 lambda) |det g_B'/det g_B|^(2 (1-lambda))
- * (UpdateSCEELayer!, src/tU/SCEE.jl:230-287).  O receives per pair the
- * reference's CSV row: O[p (sweeps+1)] = lambda, then per sweep the mean over
- * slices of (|det g_A|^2 / |det g_B|^2)^(1/Nlambda); len counts doubles.
- * kdq_scee_get_green copies one replica's Green's function `which`
- * (0: G(tau,tau), 1: G(tau0,tau0) at the middle node, 2: G(tau,tau0),
- * 3: G(tau0,tau); complex, 2 Ns^2 doubles) at the end of the run (tau = 0).
+ * (t-U, UpdateSCEELayer!, src/tU/SCEE.jl:230-287; t-V: each bond proposal
+ * with (det g_A'/det g_A)^lambda (det g_B'/det g_B)^(1-lambda), the bond
+ * rotations of each direction wrapped between that direction's updates,
+ * src/tV/SCEE.jl:87-330,447-508).  O receives per pair the reference's CSV
+ * row: O[p (sweeps+1)] = lambda, then per sweep the mean over slices of
+ * (detg_A / detg_B)^(1/Nlambda), detg = |det g|^2 (t-U) or det g (t-V);
+ * len counts doubles.  kdq_scee_get_green copies one replica's Green's
+ * function `which` (0: G(tau,tau), 1: G(tau0,tau0) at the middle node,
+ * 2: G(tau,tau0), 3: G(tau0,tau); Ns^2 values, complex for t-U as 2 doubles
+ * each) at the end of the run (tau = 0).
  * After kdq_scee_run, kdq_init must precede a plain sweep. */
 int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB,
                     double lambda, int32_t n_lambda);

@@ -962,7 +962,8 @@ namespace {
 int scee_setup(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB, double lambda,
                int32_t n_lambda, int dop, double alpha) {
   if (!h) return KDQ_ERR_ARG;
-  if (h->kind != KDQ_TU) return fail(h, KDQ_ERR_ARG, "the SCEE and disorder-operator sweeps are implemented for t-U only");
+  if (h->kind != KDQ_TU && !(h->kind == KDQ_TV && !dop))
+    return fail(h, KDQ_ERR_ARG, "the SCEE sweep is implemented for t-U and t-V, the disorder-operator sweep for t-U");
   if (!dop && h->nchains % 2) return fail(h, KDQ_ERR_ARG, "the SCEE sweep needs an even number of chains (replica pairs)");
   if (!std::isfinite(alpha)) return fail(h, KDQ_ERR_ARG, "alpha must be finite");
   if (h->precision != KDQ_PREC_FP64) return fail(h, KDQ_ERR_ARG, "the SCEE sweep runs in FP64 only");
@@ -1081,7 +1082,7 @@ int kdq_scee_get_green(kdq_handle* h, int32_t chain, int32_t which, double* G, s
   if (!h->scee) return fail(h, KDQ_ERR_STATE, "kdq_scee_enable must precede kdq_scee_get_green");
   if (chain < 0 || chain >= h->nchains || which < 0 || which > 3) return fail(h, KDQ_ERR_ARG, "chain or which out of range");
   const size_t NN2 = (size_t)h->Ns * h->Ns;
-  if (len != NN2 * 2) return fail(h, KDQ_ERR_ARG, "G must hold 2 Ns^2 doubles (complex)");
+  if (len != NN2 * (h->esz / 8)) return fail(h, KDQ_ERR_ARG, "G must hold Ns^2 values (2 doubles each if complex)");
   KDQ_CUDA(h, cudaSetDevice(h->device));
   KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
   const DevBuf* src[4] = {&h->G, &h->scee_G0, &h->scee_Gt0, &h->scee_G0t};

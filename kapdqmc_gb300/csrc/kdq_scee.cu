@@ -5,16 +5,21 @@
 #include "kdq_scee.cuh"
 
 namespace kdq {
-cudaError_t launch_scee_rm1(const SweepParams& P, int mode, int k, bool kc, int npairs, size_t dyn, cudaStream_t st);
-cudaError_t launch_scee_rm3(const SweepParams& P, int mode, int k, bool kc, int npairs, size_t dyn, cudaStream_t st);
-cudaError_t launch_scee_rm6(const SweepParams& P, int mode, int k, bool kc, int npairs, size_t dyn, cudaStream_t st);
+cudaError_t launch_scee_rm1(const SweepParams& P, int mode, int k, int kind, bool kc, int npairs, size_t dyn,
+                            cudaStream_t st);
+cudaError_t launch_scee_rm3(const SweepParams& P, int mode, int k, int kind, bool kc, int npairs, size_t dyn,
+                            cudaStream_t st);
+cudaError_t launch_scee_rm6(const SweepParams& P, int mode, int k, int kind, bool kc, int npairs, size_t dyn,
+                            cudaStream_t st);
 
-size_t scee_dyn_bytes(int Ns) { return scee_tape_bytes(Ns) + sizeof(SceeSmem<cd>); }
+size_t scee_dyn_bytes(int Ns, int kind) {
+  return scee_tape_bytes(Ns) + (kind == KDQ_TV ? sizeof(SceeSmemTV) : sizeof(SceeSmem<cd>));
+}
 
 cudaError_t launch_scee(const SweepParams& P, int mode, int k, int maxrm, bool kc, int npairs, cudaStream_t st) {
-  const size_t dyn = scee_dyn_bytes(P.Ns);
-  if (maxrm == 1) return launch_scee_rm1(P, mode, k, kc, npairs, dyn, st);
-  if (maxrm == 3) return launch_scee_rm3(P, mode, k, kc, npairs, dyn, st);
-  return launch_scee_rm6(P, mode, k, kc, npairs, dyn, st);
+  const size_t dyn = scee_dyn_bytes(P.Ns, P.kind);
+  if (maxrm == 1) return launch_scee_rm1(P, mode, k, P.kind, kc, npairs, dyn, st);
+  if (maxrm == 3) return launch_scee_rm3(P, mode, k, P.kind, kc, npairs, dyn, st);
+  return launch_scee_rm6(P, mode, k, P.kind, kc, npairs, dyn, st);
 }
 }  // namespace kdq

@@ -37,6 +37,20 @@ struct SceeSmem {
   int bad;
 };
 
+// the same for the rank-2 (bond) updates of the t-V sweep (real)
+struct SceeSmemTV {
+  double a[2][2][KDQ_SCEE_MAXR];   // [region][column of S][site]
+  double b[2][2][KDQ_SCEE_MAXR];   // [region][row of S][site]
+  double y[2][2][KDQ_SCEE_MAXR];
+  double v[2][KDQ_SCEE_MAXR];
+  double w[2][KDQ_SCEE_MAXR];
+  double part[8][KDQ_SCEE_MAXR];
+  double g4[8][KDQ_MAX_NS];         // staged columns and rows of the rank-2 Green's-function update
+  double tau[2][4];
+  double rr[4];
+  int acc;
+};
+
 // out[j] = sum_l v[l] M(l, j), j < n (M given as an accessor); all threads
 template <class T, class MF>
 __device__ void vecmat(int n, const T* v, MF M, T* out, T (*part)[KDQ_SCEE_MAXR]) {
@@ -92,10 +106,51 @@ __device__ void mcopy(int n, const T* src, T* dst) {
   __syncthreads();
 }
 
+// One-sided bond rotations of direction j of slice lt on an N x N matrix
+// (WrapV! "L" and "R", src/tV/GreenMatrix.jl:99-119): tv_left applies V_j
+// (sign +1) or V_j^-1 (sign -1) from the left, tv_right V_j^-1 (sign +1) or
+// V_j (sign -1) from the right, each as the 2x2 blocks on the bond's rows or
+// columns.
+template <int KIND, class T, class KT>
+__device__ void tv_left(Ctx<KIND, T, KT, T, KT>& c, T* M, int lt, int j, int sign) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, nb = N / 2;
+  tv_coeffs(c, lt, j, sign);
+  const T* L = c.sm.dvec;
+  const int* bx = P.bx + (size_t)j * nb;
+  const int* by = P.by + (size_t)j * nb;
+  for (Walk w(nb, N); w.ok(); w.next()) {
+    const int x = bx[w.i], y = by[w.i];
+    const T lp = L[2 * w.i], lm = L[2 * w.i + 1];
+    const T gx = M[x + (size_t)w.j * N], gy = M[y + (size_t)w.j * N];
+    M[x + (size_t)w.j * N] = lp * gx + lm * gy;
+    M[y + (size_t)w.j * N] = lm * gx + lp * gy;
+  }
+  __syncthreads();
+}
+
+template <int KIND, class T, class KT>
+__device__ void tv_right(Ctx<KIND, T, KT, T, KT>& c, T* M, int lt, int j, int sign) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, nb = N / 2;
+  tv_coeffs(c, lt, j, sign);
+  const T* R = c.sm.dinv;
+  const int* bx = P.bx + (size_t)j * nb;
+  const int* by = P.by + (size_t)j * nb;
+  for (Walk w(N, nb); w.ok(); w.next()) {
+    const int xp = bx[w.j], yp = by[w.j];
+    const T rp = R[2 * w.j], rm = R[2 * w.j + 1];
+    const T a = M[w.i + (size_t)xp * N], b = M[w.i + (size_t)yp * N];
+    M[w.i + (size_t)xp * N] = a * rp + b * rm;
+    M[w.i + (size_t)yp * N] = a * rm + b * rp;
+  }
+  __syncthreads();
+}
+
 // Block product of block k and its inverse (BM_F!, BMinv_F!,
 // src/tU/GreenMatrix.jl:10-47): BM = prod D eK, BMinv = prod eKinv D^-1.
-template <int MAXRM, class T, class KT>
-__device__ __noinline__ void scee_block_mats(Ctx<KDQ_TU, T, KT, T, KT>& c, int k, T* BM, T* BMi) {
+template <int MAXRM, int KIND, class T, class KT>
+__device__ __noinline__ void scee_block_mats(Ctx<KIND, T, KT, T, KT>& c, int k, T* BM, T* BMi) {
   const SweepParams& P = c.P;
   const int N = P.Ns;
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
@@ -104,17 +159,28 @@ __device__ __noinline__ void scee_block_mats(Ctx<KDQ_TU, T, KT, T, KT>& c, int k
   }
   __syncthreads();
   for (int lt = (int)P.nodes[k - 1] + 1; lt <= (int)P.nodes[k]; ++lt) {
-    slice_diag(c, lt, +1);
-    gemm_sq<MAXRM, T>(N, N, N, c.eK, N, BM, N, c.W1, N, c.sm.dvec, (const T*)nullptr);
-    mcopy(N * N, c.W1, BM);
-    gemm_sq<MAXRM, T>(N, N, N, BMi, N, c.eKinv, N, c.W1, N, (const T*)nullptr, c.sm.dinv);
-    mcopy(N * N, c.W1, BMi);
+    if constexpr (KIND == KDQ_TV) {   // B = V_1 .. V_z eK, B^-1 = eKinv V_z^-1 .. V_1^-1
+      gemm_sq<MAXRM, T>(N, N, N, c.eK, N, BM, N, c.W1, N);
+      mcopy(N * N, c.W1, BM);
+      gemm_sq<MAXRM, T>(N, N, N, BMi, N, c.eKinv, N, c.W1, N);
+      mcopy(N * N, c.W1, BMi);
+      for (int j = P.z - 1; j >= 0; --j) {
+        tv_left(c, BM, lt, j, +1);
+        tv_right(c, BMi, lt, j, +1);
+      }
+    } else {
+      slice_diag(c, lt, +1);
+      gemm_sq<MAXRM, T>(N, N, N, c.eK, N, BM, N, c.W1, N, c.sm.dvec, (const T*)nullptr);
+      mcopy(N * N, c.W1, BM);
+      gemm_sq<MAXRM, T>(N, N, N, BMi, N, c.eKinv, N, c.W1, N, (const T*)nullptr, c.sm.dinv);
+      mcopy(N * N, c.W1, BMi);
+    }
   }
 }
 
 // BR[i] = orth_cols(BMs[i-1] BR[i-1])
-template <int MAXRM, class T, class KT>
-__device__ __noinline__ void scee_br(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int i) {
+template <int MAXRM, int KIND, class T, class KT>
+__device__ __noinline__ void scee_br(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, int i) {
   const int N = c.P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
   const SweepParams& P = c.P;
@@ -124,8 +190,8 @@ __device__ __noinline__ void scee_br(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeCha
 }
 
 // BL[i] = orth_rows(BL[i+1] BMs[i])
-template <int MAXRM, class T, class KT>
-__device__ __noinline__ void scee_bl(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int i) {
+template <int MAXRM, int KIND, class T, class KT>
+__device__ __noinline__ void scee_bl(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, int i) {
   const int N = c.P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
   const SweepParams& P = c.P;
@@ -146,8 +212,8 @@ __device__ __noinline__ void scee_bl(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeCha
 }
 
 // out = I - BR (BL BR)^-1 BL at node i (get_G!, src/public/Gupdate.jl:139-157)
-template <int MAXRM, class T, class KT>
-__device__ __noinline__ void scee_green(Ctx<KDQ_TU, T, KT, T, KT>& c, int i, T* out) {
+template <int MAXRM, int KIND, class T, class KT>
+__device__ __noinline__ void scee_green(Ctx<KIND, T, KT, T, KT>& c, int i, T* out) {
   const int N = c.P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
   const SweepParams& P = c.P;
@@ -171,8 +237,8 @@ __device__ __noinline__ void scee_green(Ctx<KDQ_TU, T, KT, T, KT>& c, int i, T* 
 }
 
 // G4!: the four Green's functions of one replica at node idx
-template <int MAXRM, class T, class KT>
-__device__ __noinline__ void scee_g4(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int idx, bool fwd) {
+template <int MAXRM, int KIND, class T, class KT>
+__device__ __noinline__ void scee_g4(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, int idx, bool fwd) {
   const SweepParams& P = c.P;
   const int N = P.Ns, NN2 = N * N, Th = P.NN / 2 + 1;
   T* Gt = c.G;
@@ -222,8 +288,8 @@ __device__ __noinline__ void scee_g4(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeCha
 
 // Grover matrix g = 2 a b - a - b + I of the replicas' G0 on a region; its
 // inverse into inv and |det g|^2 (returned to thread 0)
-template <int MAXRM, class T, class KT>
-__device__ __noinline__ double scee_grover(Ctx<KDQ_TU, T, KT, T, KT>& c, const T* G0a, const T* G0b, const int* idx, int n,
+template <int MAXRM, int KIND, class T, class KT>
+__device__ __noinline__ double scee_grover(Ctx<KIND, T, KT, T, KT>& c, const T* G0a, const T* G0b, const int* idx, int n,
                               T* inv, T* wa, T* wb) {
   const int N = c.P.Ns;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
@@ -247,14 +313,15 @@ __device__ __noinline__ double scee_grover(Ctx<KDQ_TU, T, KT, T, KT>& c, const T
   __syncthreads();
   gj_inverse(n, inv, fcol, c.piv, &bad, &lg, &ph);
   if (threadIdx.x == 0 && bad) atomicOr(&c.ctl->err, KDQ_FLAG_SINGULAR);
-  return exp(2.0 * lg);
+  if constexpr (KIND == KDQ_TV) return ph.x * exp(lg);   // det g itself (src/tV/SCEE.jl:437)
+  return exp(2.0 * lg);                                   // |det g|^2 (src/tU/SCEE.jl:267)
 }
 
 // Disorder-operator matrix X = e^{i alpha} I + (1 - e^{i alpha}) G0[R,R] of a
 // region (get_ABX!, src/tU/disorder_operate.jl:202-224): inverse into inv,
 // |det X|^2 returned
-template <int MAXRM, class T, class KT>
-__device__ __noinline__ double scee_xmat(Ctx<KDQ_TU, T, KT, T, KT>& c, const T* G0, const int* idx, int n, T* inv) {
+template <int MAXRM, int KIND, class T, class KT>
+__device__ __noinline__ double scee_xmat(Ctx<KIND, T, KT, T, KT>& c, const T* G0, const int* idx, int n, T* inv) {
   const int N = c.P.Ns;
   double sn, cs;
   sincos(c.P.scee_alpha, &sn, &cs);
@@ -280,18 +347,20 @@ __device__ __noinline__ double scee_xmat(Ctx<KDQ_TU, T, KT, T, KT>& c, const T* 
 
 // get_ABGM! (get_ABX! for the disorder operator): four Green's functions of
 // the replicas and the inverses of both region matrices
-template <int MAXRM, class T, class KT>
-__device__ __noinline__ void scee_abgm(Ctx<KDQ_TU, T, KT, T, KT>* c, const SceeChain<T>* q, int idx, bool fwd, int pair) {
+template <int MAXRM, int KIND, class T, class KT>
+__device__ __noinline__ void scee_abgm(Ctx<KIND, T, KT, T, KT>* c, const SceeChain<T>* q, int idx, bool fwd, int pair) {
   const SweepParams& P = c[0].P;
   scee_g4<MAXRM>(c[0], q[0], idx, fwd);
   if (!P.scee_dop) scee_g4<MAXRM>(c[1], q[1], idx, fwd);
   const size_t rs = (size_t)P.scee_nmax * P.scee_nmax;
   T* invA = static_cast<T*>(P.scee_inv) + (size_t)pair * 2 * rs;
   T* invB = invA + rs;
-  double dA, dB;
+  double dA = 0.0, dB = 0.0;
   if (P.scee_dop) {
-    dA = scee_xmat<MAXRM>(c[0], q[0].G0, P.scee_idxA, P.scee_nA, invA);
-    dB = scee_xmat<MAXRM>(c[0], q[0].G0, P.scee_idxB, P.scee_nB, invB);
+    if constexpr (KIND == KDQ_TU) {
+      dA = scee_xmat<MAXRM>(c[0], q[0].G0, P.scee_idxA, P.scee_nA, invA);
+      dB = scee_xmat<MAXRM>(c[0], q[0].G0, P.scee_idxB, P.scee_nB, invB);
+    }
   } else {
     dA = scee_grover<MAXRM>(c[0], q[0].G0, q[1].G0, P.scee_idxA, P.scee_nA, invA, c[0].W1, c[0].W2);
     dB = scee_grover<MAXRM>(c[0], q[0].G0, q[1].G0, P.scee_idxB, P.scee_nB, invB, c[0].W1, c[0].W2);
@@ -306,8 +375,8 @@ __device__ __noinline__ void scee_abgm(Ctx<KDQ_TU, T, KT, T, KT>* c, const SceeC
 // WrapKV! "L", "B", "R" of one replica (src/tU/GreenMatrix.jl:56-86; the
 // backward "R" uses cis(+alpha eta) as the reference's in-place inversion of
 // its diagonal in the preceding "B" call leaves it)
-template <int MAXRM, class T, class KT>
-__device__ void scee_wrap(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, int lt, bool fwd) {
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void scee_wrap(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, int lt, bool fwd) {
   const int N = c.P.Ns, NN2 = N * N;
   slice_diag(c, lt, +1);
   const T* d = c.sm.dvec;
@@ -337,8 +406,8 @@ __device__ void scee_wrap(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, i
 
 // One proposal of replica r (0 or 1) at site i of slice lt (UpdateSCEELayer!,
 // src/tU/SCEE.jl:230-287); co / qo: the other replica.
-template <int MAXRM, class T, class KT>
-__device__ void scee_propose(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q, const SceeChain<T>& qo, int r,
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void scee_propose(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, const SceeChain<T>& qo, int r,
                              int lt, int i, int kk, double u, long long logpos, SceeSmem<T>& ss, int pair) {
   const SweepParams& P = c.P;
   const int N = P.Ns;
@@ -464,8 +533,17 @@ __device__ void scee_propose(Ctx<KDQ_TU, T, KT, T, KT>& c, const SceeChain<T>& q
   __syncthreads();
 }
 
-template <int MAXRM, class T, class KT>
-__device__ void scee_layer(Ctx<KDQ_TU, T, KT, T, KT>* c, const SceeChain<T>* q, int lt, bool fwd, SceeSmem<T>& ss,
+// the estimator (detg_A / detg_B)^(1/Nlambda) after every slice's updates
+__device__ inline void scee_accumulate(const SweepParams& P, int pair) {
+  if (threadIdx.x == 0) {
+    double* dt = P.scee_det + (size_t)pair * 4;
+    dt[2] += pow(dt[0] / dt[1], 1.0 / P.scee_nlam);
+    dt[3] += 1.0;
+  }
+}
+
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void scee_layer(Ctx<KIND, T, KT, T, KT>* c, const SceeChain<T>* q, int lt, bool fwd, SceeSmem<T>& ss,
                            int pair) {
   const SweepParams& P = c[0].P;
   const int N = P.Ns, Nt = P.Nt;
@@ -481,23 +559,248 @@ __device__ void scee_layer(Ctx<KDQ_TU, T, KT, T, KT>* c, const SceeChain<T>* q, 
   if (threadIdx.x == 0) {
     c[0].ctl->log_pos += N;
     if (two) c[1].ctl->log_pos += N;
-    double* dt = P.scee_det + (size_t)pair * 4;
-    dt[2] += pow(dt[0] / dt[1], 1.0 / P.scee_nlam);   // (detg_A / detg_B)^(1/Nlambda)
-    dt[3] += 1.0;
   }
+  scee_accumulate(P, pair);
   finish_tape(c[0], N);
   if (two) finish_tape(c[1], N);
   __syncthreads();
 }
 
-template <int MAXRM, class T, class KT>
+// ------------------------------------------------------------------ t-V
+// WrapK! (src/tV/SCEE.jl:509-517): Gt <- A Gt A^-1, Gt0 <- A Gt0, G0t <- G0t A^-1
+// with A = eK (forward) or eKinv (backward)
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void scee_wrapk(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, bool fwd) {
+  const int N = c.P.Ns, NN2 = N * N;
+  const KT* A = fwd ? c.eK : c.eKinv;
+  const KT* Ai = fwd ? c.eKinv : c.eK;
+  gemm_sq<MAXRM, T>(N, N, N, c.G, N, Ai, N, c.W1, N);
+  gemm_sq<MAXRM, T>(N, N, N, A, N, c.W1, N, c.G, N);
+  gemm_sq<MAXRM, T>(N, N, N, A, N, q.Gt0, N, c.W1, N);
+  mcopy(NN2, c.W1, q.Gt0);
+  gemm_sq<MAXRM, T>(N, N, N, q.G0t, N, Ai, N, c.W1, N);
+  mcopy(NN2, c.W1, q.G0t);
+}
+
+// WrapV! "L", "B", "R" of direction j: V_j (forward) or V_j^-1 (backward)
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void scee_wrapv(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, int lt, int j, bool fwd) {
+  const int sign = fwd ? +1 : -1;
+  tv_left(c, q.Gt0, lt, j, sign);
+  tv_rotate(c, c.G, lt, j, sign);
+  tv_right(c, q.G0t, lt, j, sign);
+}
+
+// One bond proposal of replica r (UpdateSCEELayer!, src/tV/SCEE.jl:447-508):
+// rank-2 versions of get_abTau1!/get_abTau2!, GMupdate! and G4update!.
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void scee_propose_tv(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, const SceeChain<T>& qo, int r,
+                                int lt, int j, int bi, int kk, double u, long long logpos, SceeSmemTV& ss, int pair) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns, nb = N / 2;
+  const size_t rs = (size_t)P.scee_nmax * P.scee_nmax;
+  double* inv[2] = {static_cast<double*>(P.scee_inv) + (size_t)pair * 2 * rs, nullptr};
+  inv[1] = inv[0] + rs;
+  const int* ridx[2] = {P.scee_idxA, P.scee_idxB};
+  const int rn[2] = {P.scee_nA, P.scee_nB};
+  const int S[2] = {P.bx[j * nb + bi], P.by[j * nb + bi]};
+  uint8_t* sf = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * nb + bi;
+  const int sold = *sf;
+  const int sx = kk + (kk + 1 >= sold ? 2 : 1);
+  const double* G = c.G;
+  __shared__ double p0;
+  if (threadIdx.x == 0) {   // get_r!, src/tV/GreenMatrix.jl:76-89
+    const double h = 0.70710678118654752440;
+    const double* t2 = P.rtab + ((size_t)(lt - 1) * 16 + (sold - 1) * 4 + sx - 1) * 2;
+    const double q00 = -h * t2[0], q01 = -h * t2[1], q10 = -h * t2[0], q11 = h * t2[1];
+    const double d00 = q00 * -h + q01 * -h, d01 = q00 * -h + q01 * h;
+    const double d10 = q10 * -h + q11 * -h, d11 = q10 * -h + q11 * h;
+    const double g00 = G[S[0] + (size_t)S[0] * N], g01 = G[S[0] + (size_t)S[1] * N];
+    const double g10 = G[S[1] + (size_t)S[0] * N], g11 = G[S[1] + (size_t)S[1] * N];
+    double a00 = d00 - (d00 * g00 + d01 * g10), a01 = d01 - (d00 * g01 + d01 * g11);
+    double a10 = d10 - (d10 * g00 + d11 * g10), a11 = d11 - (d10 * g01 + d11 * g11);
+    a00 += 1.0;
+    a11 += 1.0;
+    const double det = a00 * a11 - a01 * a10;
+    p0 = det * P.gratio[(sold - 1) * 4 + sx - 1];
+    const double rd = 1.0 / det;
+    const double i00 = a11 * rd, i01 = -a01 * rd, i10 = -a10 * rd, i11 = a00 * rd;
+    ss.rr[0] = i00 * d00 + i01 * d10;   // r = (I + Delta (I - G_SS))^-1 Delta, row-major 2x2
+    ss.rr[1] = i00 * d01 + i01 * d11;
+    ss.rr[2] = i10 * d00 + i11 * d10;
+    ss.rr[3] = i10 * d01 + i11 * d11;
+  }
+  __syncthreads();
+  const double r00 = ss.rr[0], r01 = ss.rr[1], r10 = ss.rr[2], r11 = ss.rr[3];
+  for (int g = 0; g < 2; ++g) {
+    const int n = rn[g];
+    const int* ix = ridx[g];
+    const double* iv = inv[g];
+    auto X = [&](int l, int m) {   // 2 G0_other[A,A] - I
+      const double x = 2.0 * qo.G0[ix[l] + (size_t)ix[m] * N];
+      return l == m ? x - 1.0 : x;
+    };
+    auto IV = [&](int l, int m) { return iv[l + (size_t)m * n]; };
+    if (r == 0) {   // a = G0t[A,S] r, b = Gt0[S,A] X inv
+      for (int l = threadIdx.x; l < n; l += blockDim.x) {
+        const double g0 = q.G0t[ix[l] + (size_t)S[0] * N], g1 = q.G0t[ix[l] + (size_t)S[1] * N];
+        ss.a[g][0][l] = g0 * r00 + g1 * r10;
+        ss.a[g][1][l] = g0 * r01 + g1 * r11;
+        ss.v[0][l] = q.Gt0[S[0] + (size_t)ix[l] * N];
+        ss.v[1][l] = q.Gt0[S[1] + (size_t)ix[l] * N];
+      }
+      __syncthreads();
+      for (int qr = 0; qr < 2; ++qr) {
+        vecmat<double>(n, ss.v[qr], X, ss.y[g][qr], ss.part);
+        vecmat<double>(n, ss.y[g][qr], IV, ss.b[g][qr], ss.part);
+      }
+    } else {        // a = X G0t[A,S], b = r Gt0[S,A] inv
+      for (int l = threadIdx.x; l < n; l += blockDim.x) {
+        ss.y[g][0][l] = q.G0t[ix[l] + (size_t)S[0] * N];
+        ss.y[g][1][l] = q.G0t[ix[l] + (size_t)S[1] * N];
+        const double t0 = q.Gt0[S[0] + (size_t)ix[l] * N], t1 = q.Gt0[S[1] + (size_t)ix[l] * N];
+        ss.v[0][l] = r00 * t0 + r01 * t1;
+        ss.v[1][l] = r10 * t0 + r11 * t1;
+      }
+      __syncthreads();
+      for (int qc = 0; qc < 2; ++qc) {
+        matvec<double>(n, X, ss.y[g][qc], ss.a[g][qc], ss.part);
+        vecmat<double>(n, ss.v[qc], IV, ss.b[g][qc], ss.part);
+      }
+    }
+    // Tau = I + b a (2 x 2, row-major)
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int l = threadIdx.x; l < n; l += blockDim.x)
+      for (int e = 0; e < 4; ++e) t[e] = fma(ss.b[g][e >> 1][l], ss.a[g][e & 1][l], t[e]);
+    for (int e = 0; e < 4; ++e) {
+      t[e] = warp_sum(t[e]);
+      if ((threadIdx.x & 31) == 0) ss.part[threadIdx.x >> 5][e] = t[e];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int e = 0; e < 4; ++e) {
+        double tt = (e == 0 || e == 3) ? 1.0 : 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tt += ss.part[w][e];
+        ss.tau[g][e] = tt;
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double dA = ss.tau[0][0] * ss.tau[0][3] - ss.tau[0][1] * ss.tau[0][2];
+    const double dB = ss.tau[1][0] * ss.tau[1][3] - ss.tau[1][1] * ss.tau[1][2];
+    const double p = p0 * (pow(dA, P.scee_lam) * pow(dB, 1.0 - P.scee_lam));
+    int acc = u < p;
+    if (isnan(p)) {
+      acc = 0;
+      atomicOr(&c.ctl->err, KDQ_FLAG_NAN);
+    }
+    ss.acc = acc;
+    if (acc) {
+      P.scee_det[(size_t)pair * 4 + 0] *= dA;
+      P.scee_det[(size_t)pair * 4 + 1] *= dB;
+    }
+    if (P.acc_log && logpos < P.acc_log_cap) P.acc_log[(size_t)c.chain * P.acc_log_cap + logpos] = (uint8_t)acc;
+    c.ctl->n_prop += 1;
+    c.ctl->n_acc += acc;
+  }
+  __syncthreads();
+  if (!ss.acc) return;
+  // GMupdate!: inv <- inv - (inv a) Tau^-1 b
+  for (int g = 0; g < 2; ++g) {
+    const int n = rn[g];
+    double* iv = inv[g];
+    auto IV = [&](int l, int m) { return iv[l + (size_t)m * n]; };
+    for (int qc = 0; qc < 2; ++qc) matvec<double>(n, IV, ss.a[g][qc], ss.y[g][qc], ss.part);
+    const double* tg = ss.tau[g];
+    const double td = 1.0 / (tg[0] * tg[3] - tg[1] * tg[2]);
+    const double t00 = tg[3] * td, t01 = -tg[1] * td, t10 = -tg[2] * td, t11 = tg[0] * td;
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+      const double b0 = ss.b[g][0][m], b1 = ss.b[g][1][m];
+      ss.w[0][m] = t00 * b0 + t01 * b1;
+      ss.w[1][m] = t10 * b0 + t11 * b1;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int l = e % n, m = e / n;
+      iv[e] -= ss.y[g][0][l] * ss.w[0][m] + ss.y[g][1][l] * ss.w[1][m];
+    }
+    __syncthreads();
+  }
+  // G4update!: z1 = r Gt0[S,:], z2 = E_S r - r Gt[S,:]
+  double* c0t0 = ss.g4[0];
+  double* c0t1 = ss.g4[1];
+  double* ct0 = ss.g4[2];
+  double* ct1 = ss.g4[3];
+  double* z10 = ss.g4[4];
+  double* z11 = ss.g4[5];
+  double* z20 = ss.g4[6];
+  double* z21 = ss.g4[7];
+  for (int b = threadIdx.x; b < N; b += blockDim.x) {
+    c0t0[b] = q.G0t[b + (size_t)S[0] * N];
+    c0t1[b] = q.G0t[b + (size_t)S[1] * N];
+    ct0[b] = G[b + (size_t)S[0] * N];
+    ct1[b] = G[b + (size_t)S[1] * N];
+    const double t0 = q.Gt0[S[0] + (size_t)b * N], t1 = q.Gt0[S[1] + (size_t)b * N];
+    z10[b] = r00 * t0 + r01 * t1;
+    z11[b] = r10 * t0 + r11 * t1;
+    const double g0 = G[S[0] + (size_t)b * N], g1 = G[S[1] + (size_t)b * N];
+    double w0 = -(r00 * g0 + r01 * g1), w1 = -(r10 * g0 + r11 * g1);
+    if (b == S[0]) { w0 += r00; w1 += r10; }
+    if (b == S[1]) { w0 += r01; w1 += r11; }
+    z20[b] = w0;
+    z21[b] = w1;
+  }
+  __syncthreads();
+  for (Walk w(N, N); w.ok(); w.next()) {
+    const double a0 = c0t0[w.i], a1 = c0t1[w.i], e0 = ct0[w.i], e1 = ct1[w.i];
+    const double y0 = z10[w.j], y1 = z11[w.j], x0 = z20[w.j], x1 = z21[w.j];
+    q.G0[w.e] += a0 * y0 + a1 * y1;
+    q.Gt0[w.e] += e0 * y0 + e1 * y1;
+    q.G0t[w.e] -= a0 * x0 + a1 * x1;
+    c.G[w.e] -= e0 * x0 + e1 * x1;
+  }
+  if (threadIdx.x == 0) *sf = (uint8_t)sx;
+  __syncthreads();
+}
+
+// The bonds of direction j of slice lt, both replicas alternating per bond
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void scee_layer_tv(Ctx<KIND, T, KT, T, KT>* c, const SceeChain<T>* q, int lt, int j, bool fwd,
+                              SceeSmemTV& ss, int pair) {
+  const SweepParams& P = c[0].P;
+  const int nb = P.Ns / 2, Nt = P.Nt, pf = P.n_field;
+  const uint32_t qs = fwd ? (uint32_t)(lt - 1) * pf : (uint32_t)(Nt + (Nt - lt)) * pf;
+  const int off = (fwd ? (P.z - 1 - j) : j) * nb;
+  load_tape(c[0], qs + off, nb);
+  load_tape(c[1], qs + off, nb);
+  const long long lb0 = c[0].ctl->log_pos, lb1 = c[1].ctl->log_pos;
+  for (int i = 0; i < nb; ++i) {
+    scee_propose_tv<MAXRM>(c[0], q[0], q[1], 0, lt, j, i, c[0].tk[i], c[0].tu[i], lb0 + i, ss, pair);
+    scee_propose_tv<MAXRM>(c[1], q[1], q[0], 1, lt, j, i, c[1].tk[i], c[1].tu[i], lb1 + i, ss, pair);
+  }
+  if (threadIdx.x == 0) {
+    c[0].ctl->log_pos += nb;
+    c[1].ctl->log_pos += nb;
+  }
+  finish_tape(c[0], nb);
+  finish_tape(c[1], nb);
+  __syncthreads();
+}
+
+template <int KIND, class T>
+struct SceeSmemOf { using type = SceeSmem<T>; };
+template <class T>
+struct SceeSmemOf<KDQ_TV, T> { using type = SceeSmemTV; };
+
+template <int MAXRM, int KIND, class T, class KT>
 __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, int mode, int k) {
   extern __shared__ double dyn_d[];
   __shared__ Smem<T> sm;
   const int pair = blockIdx.x;
   const int N = P.Ns;
   // dynamic shared memory: the two replicas' tape slices, then SceeSmem
-  SceeSmem<T>& ss = *reinterpret_cast<SceeSmem<T>*>(reinterpret_cast<unsigned char*>(dyn_d) + scee_tape_bytes(N));
+  using SS = typename SceeSmemOf<KIND, T>::type;
+  SS& ss = *reinterpret_cast<SS*>(reinterpret_cast<unsigned char*>(dyn_d) + scee_tape_bytes(N));
   PhaseClock clk;
   clk.start(nullptr);
   const int nrep = P.scee_dop ? 1 : 2;
@@ -506,7 +809,7 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
     const size_t cNN = (size_t)chain * P.sz_NN, cNn = (size_t)chain * P.sz_Nn;
     double* tu = dyn_d + (size_t)r * N;
     uint8_t* tk = reinterpret_cast<uint8_t*>(dyn_d + 2 * (size_t)N) + (size_t)r * N;
-    return Ctx<KDQ_TU, T, KT, T, KT>{P, sm, tk, tu, chain, P.ctl + chain,
+    return Ctx<KIND, T, KT, T, KT>{P, sm, tk, tu, chain, P.ctl + chain,
                                       static_cast<T*>(P.G) + cNN, static_cast<T*>(P.W1) + cNN,
                                       static_cast<T*>(P.W2) + cNN, static_cast<T*>(P.Yw) + cNn,
                                       static_cast<T*>(P.Y2w) + cNn, static_cast<T*>(P.Y) + cNn,
@@ -518,7 +821,7 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
                                       static_cast<const KT*>(P.HalfeK), static_cast<const KT*>(P.HalfeKinv),
                                       static_cast<const KT*>(P.K), clk};
   };
-  Ctx<KDQ_TU, T, KT, T, KT> c[2] = {mk(0), mk(1)};
+  Ctx<KIND, T, KT, T, KT> c[2] = {mk(0), mk(1)};
   const SceeChain<T> q[2] = {scee_chain<T>(P, nrep * pair), scee_chain<T>(P, nrep * pair + nrep - 1)};
   const int NN = P.NN, Th = NN / 2 + 1;
   if (mode == KDQ_MODE_INIT) {
@@ -537,9 +840,20 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
   const int lo = (int)P.nodes[k - 1], hi = (int)P.nodes[k];
   if (mode == KDQ_MODE_FWD) {   // idx == k while these slices run
     for (int lt = lo + 1; lt <= hi; ++lt) {
-      scee_wrap<MAXRM>(c[0], q[0], lt, true);
-      if (nrep == 2) scee_wrap<MAXRM>(c[1], q[1], lt, true);
-      scee_layer<MAXRM>(c, q, lt, true, ss, pair);
+      if constexpr (KIND == KDQ_TV) {   // src/tV/SCEE.jl:87-135
+        scee_wrapk<MAXRM>(c[0], q[0], true);
+        scee_wrapk<MAXRM>(c[1], q[1], true);
+        for (int j = P.z - 1; j >= 0; --j) {
+          scee_wrapv<MAXRM>(c[0], q[0], lt, j, true);
+          scee_wrapv<MAXRM>(c[1], q[1], lt, j, true);
+          scee_layer_tv<MAXRM>(c, q, lt, j, true, ss, pair);
+        }
+        scee_accumulate(P, pair);
+      } else {
+        scee_wrap<MAXRM>(c[0], q[0], lt, true);
+        if (nrep == 2) scee_wrap<MAXRM>(c[1], q[1], lt, true);
+        scee_layer<MAXRM>(c, q, lt, true, ss, pair);
+      }
     }
     const int idx = k + 1;   // lt == nodes[idx]
     for (int r = 0; r < nrep; ++r) {
@@ -551,7 +865,18 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
     scee_abgm<MAXRM>(c, q, idx, true, pair);
   } else {                      // idx == k+1 while these slices run
     for (int lt = hi; lt > lo; --lt) {
-      scee_layer<MAXRM>(c, q, lt, false, ss, pair);
+      if constexpr (KIND == KDQ_TV) {   // src/tV/SCEE.jl:258-282: the wraps come before the node step
+        for (int j = 0; j < P.z; ++j) {
+          scee_layer_tv<MAXRM>(c, q, lt, j, false, ss, pair);
+          scee_wrapv<MAXRM>(c[0], q[0], lt, j, false);
+          scee_wrapv<MAXRM>(c[1], q[1], lt, j, false);
+        }
+        scee_wrapk<MAXRM>(c[0], q[0], false);
+        scee_wrapk<MAXRM>(c[1], q[1], false);
+        scee_accumulate(P, pair);
+      } else {
+        scee_layer<MAXRM>(c, q, lt, false, ss, pair);
+      }
       if (lt - 1 == lo) {
         const int idx = k;
         for (int r = 0; r < nrep; ++r) {
@@ -560,7 +885,7 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
           for (int i = idx + 1; i <= max(Th, idx); ++i) scee_br<MAXRM>(c[r], q[r], i);
         }
         scee_abgm<MAXRM>(c, q, idx, false, pair);
-      } else {
+      } else if constexpr (KIND != KDQ_TV) {
         scee_wrap<MAXRM>(c[0], q[0], lt, false);
         if (nrep == 2) scee_wrap<MAXRM>(c[1], q[1], lt, false);
       }

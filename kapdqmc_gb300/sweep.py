@@ -286,9 +286,10 @@ class Sweeper:
     def scee_green(self, chain: int, which: int):
         """Green's function `which` (0 Gt, 1 G0, 2 Gt0, 3 G0t) of one replica."""
         N = self.model.Ns
-        out = np.empty(2 * N * N)
+        cplx = self.model.kind != KIND_TV
+        out = np.empty((2 if cplx else 1) * N * N)
         self._ck(self.lib.kdq_scee_get_green(self.h, chain, which, out.ctypes.data, out.size))
-        return out.view(np.complex128).reshape(N, N, order="F")
+        return (out.view(np.complex128) if cplx else out).reshape(N, N, order="F")
 
     def slmc_stats(self):
         """(proposed, accepted, no-change) cluster moves of the last call."""
@@ -388,11 +389,18 @@ def _append_csv(file, rows):
 
 
 def _scee_csv_name(path, model, nlam):
-    """src/tU/SCEE.jl:16-32."""
+    """src/tU/SCEE.jl:16-32, src/tV/SCEE.jl:16-32."""
     def f(x):
         return repr(float(x))
 
     site = "[" + ", ".join(str(int(v)) for v in model.site) + "]"
+    if model.kind == KIND_TV:
+        name = {"SQUARE45": "□", "SQUARE90": "□", "HoneyComb60": "HC", "HoneyComb120": "HC120"}[model.Lattice]
+        if len(np.unique(model.α)) == 1:
+            return os.path.join(path, f"tVSCEE{name}_t{f(model.Ht)}V{f(model.Hv1)}size{site}Δt{f(model.Δt)}"
+                                      f"Θ{f(model.Θrelax)}N{nlam}BS{model.BatchSize}.csv")
+        return os.path.join(path, f"tVSCEE{name}_t{f(model.Ht)}V{f(model.Hv1)}_{f(model.Hv2)}size{site}Δt{f(model.Δt)}"
+                                  f"Θ{f(model.Θrelax)}_{f(model.Θquench)}N{nlam}BS{model.BatchSize}.csv")
     name = {"SQUARE90": "□90", "SQUARE45": "□45", "HoneyComb60": "HC", "HoneyComb120": "HC120"}[model.Lattice]
     if model.Θquench == 0.0:
         return os.path.join(path, f"tUSCEE{name}_t{f(model.Ht)}U{f(model.Hu1)}size{site}Δt{f(model.Δt)}"
@@ -404,14 +412,14 @@ def _scee_csv_name(path, model, nlam):
 def ctrl_SCEEicr(path, model, indexA, indexB, Sweeps: int, λ: float, Nλ: int, ss, record: bool, *,
                  seed=None, tape=None, device: int = 0):
     """Coupled incremental SCEE sweep of the replica pair(s) ``ss``
-    (src/tU/SCEE.jl:1-211): returns the updated fields.  ``ss`` is a pair
+    (src/tU/SCEE.jl:1-211, src/tV/SCEE.jl:1-431): returns the updated fields.  ``ss`` is a pair
     [s1, s2] or a stack of pairs (n_pairs, 2, ...); with ``record`` one CSV row
     per pair (lambda, then the per-sweep estimator) is appended to the
     reference's file name under ``path`` and the rows are also returned."""
-    if model.kind != KIND_TU:
-        raise ValueError("ctrl_SCEEicr is implemented for t-U")
+    if model.kind not in (KIND_TU, KIND_TV):
+        raise ValueError("ctrl_SCEEicr is implemented for t-U and t-V")
     ss = np.asarray(ss, dtype=np.uint8)
-    single = ss.ndim == 3
+    single = ss.ndim == len(model.field_shape) + 1
     pairs = ss[None] if single else ss
     stack = pairs.reshape((-1,) + tuple(model.field_shape))
     with Sweeper(model, nchains=stack.shape[0], device=device) as sw:
