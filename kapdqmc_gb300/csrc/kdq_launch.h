@@ -24,10 +24,10 @@ cudaError_t launch_tuv_mixed(const SweepParams& P, int mode, int k, int maxrm, b
 // (the self-learning cluster moves need more than the default 48 KB).
 cudaError_t prepare_tu(size_t dyn);
 cudaError_t prepare_tu_mixed(size_t dyn);
-// Coupled SCEE sweep (t-U, t-V): one CTA per replica pair (chains 2p, 2p+1),
+// Coupled SCEE sweep (t-U, t-V, t-UV): one CTA per replica pair (chains 2p, 2p+1),
 // or per chain for the disorder-operator sweep (t-U).
-cudaError_t launch_scee(const SweepParams& P, int mode, int k, int maxrm, bool k_complex, int npairs,
-                        cudaStream_t st);
+cudaError_t launch_scee(const SweepParams& P, int mode, int k, int maxrm, bool k_complex, bool g_complex,
+                        int npairs, cudaStream_t st);
 size_t scee_dyn_bytes(int Ns, int kind);
 // Grover determinants of npairs replica pairs (matrices 2p, 2p+1 of G).
 // scratch: npairs * 3 * nA^2 elements of the G type; pivs: npairs * nA.

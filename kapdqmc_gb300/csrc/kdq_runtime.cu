@@ -962,8 +962,7 @@ namespace {
 int scee_setup(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB, double lambda,
                int32_t n_lambda, int dop, double alpha) {
   if (!h) return KDQ_ERR_ARG;
-  if (h->kind != KDQ_TU && !(h->kind == KDQ_TV && !dop))
-    return fail(h, KDQ_ERR_ARG, "the SCEE sweep is implemented for t-U and t-V, the disorder-operator sweep for t-U");
+  if (dop && h->kind != KDQ_TU) return fail(h, KDQ_ERR_ARG, "the disorder-operator sweep is implemented for t-U");
   if (!dop && h->nchains % 2) return fail(h, KDQ_ERR_ARG, "the SCEE sweep needs an even number of chains (replica pairs)");
   if (!std::isfinite(alpha)) return fail(h, KDQ_ERR_ARG, "alpha must be finite");
   if (h->precision != KDQ_PREC_FP64) return fail(h, KDQ_ERR_ARG, "the SCEE sweep runs in FP64 only");
@@ -1044,10 +1043,10 @@ int scee_run(kdq_handle* h, int32_t sweeps, double* O, size_t len, int dop) {
   P.record = 0;
   const bool kc = h->kc;
   auto t0 = std::chrono::steady_clock::now();
-  KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_INIT, 0, h->maxrm, kc, (int)pairs, h->stream));
+  KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_INIT, 0, h->maxrm, kc, h->gc, (int)pairs, h->stream));
   for (int w = 0; w < sweeps; ++w) {
-    for (int k = 1; k <= h->NN - 1; ++k) KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_FWD, k, h->maxrm, kc, (int)pairs, h->stream));
-    for (int k = h->NN - 1; k >= 1; --k) KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_BWD, k, h->maxrm, kc, (int)pairs, h->stream));
+    for (int k = 1; k <= h->NN - 1; ++k) KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_FWD, k, h->maxrm, kc, h->gc, (int)pairs, h->stream));
+    for (int k = h->NN - 1; k >= 1; --k) KDQ_CUDA(h, kdq::launch_scee(P, KDQ_MODE_BWD, k, h->maxrm, kc, h->gc, (int)pairs, h->stream));
   }
   if (int rc = kdq_synchronize(h)) return rc;
   h->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -37,17 +37,18 @@ struct SceeSmem {
   int bad;
 };
 
-// the same for the rank-2 (bond) updates of the t-V sweep (real)
-struct SceeSmemTV {
-  double a[2][2][KDQ_SCEE_MAXR];   // [region][column of S][site]
-  double b[2][2][KDQ_SCEE_MAXR];   // [region][row of S][site]
-  double y[2][2][KDQ_SCEE_MAXR];
-  double v[2][KDQ_SCEE_MAXR];
-  double w[2][KDQ_SCEE_MAXR];
-  double part[8][KDQ_SCEE_MAXR];
-  double g4[8][KDQ_MAX_NS];         // staged columns and rows of the rank-2 Green's-function update
-  double tau[2][4];
-  double rr[4];
+// the same for the rank-2 (bond) updates of the t-V and t-UV sweeps
+template <class T>
+struct SceeSmem2 {
+  T a[2][2][KDQ_SCEE_MAXR];   // [region][column of S][site]
+  T b[2][2][KDQ_SCEE_MAXR];   // [region][row of S][site]
+  T y[2][2][KDQ_SCEE_MAXR];
+  T v[2][KDQ_SCEE_MAXR];
+  T w[2][KDQ_SCEE_MAXR];
+  T part[8][KDQ_SCEE_MAXR];
+  T g4[8][KDQ_MAX_NS];        // staged columns and rows of the rank-2 Green's-function update
+  T tau[2][4];
+  T rr[4];
   int acc;
 };
 
@@ -591,59 +592,78 @@ __device__ void scee_wrapv(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, in
   tv_right(c, q.G0t, lt, j, sign);
 }
 
-// One bond proposal of replica r (UpdateSCEELayer!, src/tV/SCEE.jl:447-508):
-// rank-2 versions of get_abTau1!/get_abTau2!, GMupdate! and G4update!.
+// One bond proposal of replica r at sites S = (x, y) (UpdateSCEELayer!,
+// t-V src/tV/SCEE.jl:447-508, t-UV src/tUV/SCEE.jl:355-402): rank-2
+// versions of get_abTau1!/get_abTau2!, GMupdate! and G4update!.  t-V weighs
+// with det Tau (real), t-UV with |det Tau|^2; t-UV's local ratio is |det r|^2
+// times the gamma ratio only (the reference's SCEE update leaves out the
+// plain sweep's real-type factor).
 template <int MAXRM, int KIND, class T, class KT>
-__device__ void scee_propose_tv(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, const SceeChain<T>& qo, int r,
-                                int lt, int j, int bi, int kk, double u, long long logpos, SceeSmemTV& ss, int pair) {
+__device__ void scee_propose2(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, const SceeChain<T>& qo, int r,
+                              int lt, int x, int y, uint8_t* sf, int kk, double u, long long logpos,
+                              SceeSmem2<T>& ss, int pair) {
   const SweepParams& P = c.P;
-  const int N = P.Ns, nb = N / 2;
+  const int N = P.Ns;
   const size_t rs = (size_t)P.scee_nmax * P.scee_nmax;
-  double* inv[2] = {static_cast<double*>(P.scee_inv) + (size_t)pair * 2 * rs, nullptr};
+  T* inv[2] = {static_cast<T*>(P.scee_inv) + (size_t)pair * 2 * rs, nullptr};
   inv[1] = inv[0] + rs;
   const int* ridx[2] = {P.scee_idxA, P.scee_idxB};
   const int rn[2] = {P.scee_nA, P.scee_nB};
-  const int S[2] = {P.bx[j * nb + bi], P.by[j * nb + bi]};
-  uint8_t* sf = c.s + (size_t)(lt - 1) * P.n_field + (size_t)j * nb + bi;
+  const int S[2] = {x, y};
   const int sold = *sf;
   const int sx = kk + (kk + 1 >= sold ? 2 : 1);
-  const double* G = c.G;
+  const T* G = c.G;
   __shared__ double p0;
-  if (threadIdx.x == 0) {   // get_r!, src/tV/GreenMatrix.jl:76-89
-    const double h = 0.70710678118654752440;
-    const double* t2 = P.rtab + ((size_t)(lt - 1) * 16 + (sold - 1) * 4 + sx - 1) * 2;
-    const double q00 = -h * t2[0], q01 = -h * t2[1], q10 = -h * t2[0], q11 = h * t2[1];
-    const double d00 = q00 * -h + q01 * -h, d01 = q00 * -h + q01 * h;
-    const double d10 = q10 * -h + q11 * -h, d11 = q10 * -h + q11 * h;
-    const double g00 = G[S[0] + (size_t)S[0] * N], g01 = G[S[0] + (size_t)S[1] * N];
-    const double g10 = G[S[1] + (size_t)S[0] * N], g11 = G[S[1] + (size_t)S[1] * N];
-    double a00 = d00 - (d00 * g00 + d01 * g10), a01 = d01 - (d00 * g01 + d01 * g11);
-    double a10 = d10 - (d10 * g00 + d11 * g10), a11 = d11 - (d10 * g01 + d11 * g11);
-    a00 += 1.0;
-    a11 += 1.0;
-    const double det = a00 * a11 - a01 * a10;
-    p0 = det * P.gratio[(sold - 1) * 4 + sx - 1];
-    const double rd = 1.0 / det;
-    const double i00 = a11 * rd, i01 = -a01 * rd, i10 = -a10 * rd, i11 = a00 * rd;
-    ss.rr[0] = i00 * d00 + i01 * d10;   // r = (I + Delta (I - G_SS))^-1 Delta, row-major 2x2
-    ss.rr[1] = i00 * d01 + i01 * d11;
-    ss.rr[2] = i10 * d00 + i11 * d10;
-    ss.rr[3] = i10 * d01 + i11 * d11;
+  if (threadIdx.x == 0) {
+    const T g00 = G[S[0] + (size_t)S[0] * N], g01 = G[S[0] + (size_t)S[1] * N];
+    const T g10 = G[S[1] + (size_t)S[0] * N], g11 = G[S[1] + (size_t)S[1] * N];
+    if constexpr (KIND == KDQ_TV) {   // get_r!, src/tV/GreenMatrix.jl:76-89
+      const double h = 0.70710678118654752440;
+      const double* t2 = P.rtab + ((size_t)(lt - 1) * 16 + (sold - 1) * 4 + sx - 1) * 2;
+      const double q00 = -h * t2[0], q01 = -h * t2[1], q10 = -h * t2[0], q11 = h * t2[1];
+      const double d00 = q00 * -h + q01 * -h, d01 = q00 * -h + q01 * h;
+      const double d10 = q10 * -h + q11 * -h, d11 = q10 * -h + q11 * h;
+      double a00 = d00 - (d00 * g00 + d01 * g10), a01 = d01 - (d00 * g01 + d01 * g11);
+      double a10 = d10 - (d10 * g00 + d11 * g10), a11 = d11 - (d10 * g01 + d11 * g11);
+      a00 += 1.0;
+      a11 += 1.0;
+      const double det = a00 * a11 - a01 * a10;
+      p0 = det * P.gratio[(sold - 1) * 4 + sx - 1];
+      const double rd = 1.0 / det;
+      const double i00 = a11 * rd, i01 = -a01 * rd, i10 = -a10 * rd, i11 = a00 * rd;
+      ss.rr[0] = i00 * d00 + i01 * d10;   // r = (I + Delta (I - G_SS))^-1 Delta, row-major 2x2
+      ss.rr[1] = i00 * d01 + i01 * d11;
+      ss.rr[2] = i10 * d00 + i11 * d10;
+      ss.rr[3] = i10 * d01 + i11 * d11;
+    } else {                          // get_r!, src/tUV/GreenMatrix.jl:73-89
+      const T* t2 = reinterpret_cast<const T*>(P.rtab) + (size_t)((sold - 1) * 4 + sx - 1) * 2;
+      T a00 = t2[0] - t2[0] * g00, a01 = zero<T>() - t2[0] * g01;
+      T a10 = zero<T>() - t2[1] * g10, a11 = t2[1] - t2[1] * g11;
+      a00 = a00 + one<T>();
+      a11 = a11 + one<T>();
+      const T det = a00 * a11 - a01 * a10;
+      p0 = abs2(det) * P.gratio[(sold - 1) * 4 + sx - 1];
+      const T rd = one<T>() / det;
+      ss.rr[0] = (a11 * rd) * t2[0];
+      ss.rr[1] = ((zero<T>() - a01) * rd) * t2[1];
+      ss.rr[2] = ((zero<T>() - a10) * rd) * t2[0];
+      ss.rr[3] = (a00 * rd) * t2[1];
+    }
   }
   __syncthreads();
-  const double r00 = ss.rr[0], r01 = ss.rr[1], r10 = ss.rr[2], r11 = ss.rr[3];
+  const T r00 = ss.rr[0], r01 = ss.rr[1], r10 = ss.rr[2], r11 = ss.rr[3];
   for (int g = 0; g < 2; ++g) {
     const int n = rn[g];
     const int* ix = ridx[g];
-    const double* iv = inv[g];
+    const T* iv = inv[g];
     auto X = [&](int l, int m) {   // 2 G0_other[A,A] - I
-      const double x = 2.0 * qo.G0[ix[l] + (size_t)ix[m] * N];
-      return l == m ? x - 1.0 : x;
+      const T xv = 2.0 * qo.G0[ix[l] + (size_t)ix[m] * N];
+      return l == m ? xv - one<T>() : xv;
     };
     auto IV = [&](int l, int m) { return iv[l + (size_t)m * n]; };
     if (r == 0) {   // a = G0t[A,S] r, b = Gt0[S,A] X inv
       for (int l = threadIdx.x; l < n; l += blockDim.x) {
-        const double g0 = q.G0t[ix[l] + (size_t)S[0] * N], g1 = q.G0t[ix[l] + (size_t)S[1] * N];
+        const T g0 = q.G0t[ix[l] + (size_t)S[0] * N], g1 = q.G0t[ix[l] + (size_t)S[1] * N];
         ss.a[g][0][l] = g0 * r00 + g1 * r10;
         ss.a[g][1][l] = g0 * r01 + g1 * r11;
         ss.v[0][l] = q.Gt0[S[0] + (size_t)ix[l] * N];
@@ -651,27 +671,27 @@ __device__ void scee_propose_tv(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& 
       }
       __syncthreads();
       for (int qr = 0; qr < 2; ++qr) {
-        vecmat<double>(n, ss.v[qr], X, ss.y[g][qr], ss.part);
-        vecmat<double>(n, ss.y[g][qr], IV, ss.b[g][qr], ss.part);
+        vecmat<T>(n, ss.v[qr], X, ss.y[g][qr], ss.part);
+        vecmat<T>(n, ss.y[g][qr], IV, ss.b[g][qr], ss.part);
       }
     } else {        // a = X G0t[A,S], b = r Gt0[S,A] inv
       for (int l = threadIdx.x; l < n; l += blockDim.x) {
         ss.y[g][0][l] = q.G0t[ix[l] + (size_t)S[0] * N];
         ss.y[g][1][l] = q.G0t[ix[l] + (size_t)S[1] * N];
-        const double t0 = q.Gt0[S[0] + (size_t)ix[l] * N], t1 = q.Gt0[S[1] + (size_t)ix[l] * N];
+        const T t0 = q.Gt0[S[0] + (size_t)ix[l] * N], t1 = q.Gt0[S[1] + (size_t)ix[l] * N];
         ss.v[0][l] = r00 * t0 + r01 * t1;
         ss.v[1][l] = r10 * t0 + r11 * t1;
       }
       __syncthreads();
       for (int qc = 0; qc < 2; ++qc) {
-        matvec<double>(n, X, ss.y[g][qc], ss.a[g][qc], ss.part);
-        vecmat<double>(n, ss.v[qc], IV, ss.b[g][qc], ss.part);
+        matvec<T>(n, X, ss.y[g][qc], ss.a[g][qc], ss.part);
+        vecmat<T>(n, ss.v[qc], IV, ss.b[g][qc], ss.part);
       }
     }
     // Tau = I + b a (2 x 2, row-major)
-    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    T t[4] = {zero<T>(), zero<T>(), zero<T>(), zero<T>()};
     for (int l = threadIdx.x; l < n; l += blockDim.x)
-      for (int e = 0; e < 4; ++e) t[e] = fma(ss.b[g][e >> 1][l], ss.a[g][e & 1][l], t[e]);
+      for (int e = 0; e < 4; ++e) madd(t[e], ss.b[g][e >> 1][l], ss.a[g][e & 1][l]);
     for (int e = 0; e < 4; ++e) {
       t[e] = warp_sum(t[e]);
       if ((threadIdx.x & 31) == 0) ss.part[threadIdx.x >> 5][e] = t[e];
@@ -679,15 +699,23 @@ __device__ void scee_propose_tv(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& 
     __syncthreads();
     if (threadIdx.x == 0)
       for (int e = 0; e < 4; ++e) {
-        double tt = (e == 0 || e == 3) ? 1.0 : 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tt += ss.part[w][e];
+        T tt = (e == 0 || e == 3) ? one<T>() : zero<T>();
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tt = tt + ss.part[w][e];
         ss.tau[g][e] = tt;
       }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double dA = ss.tau[0][0] * ss.tau[0][3] - ss.tau[0][1] * ss.tau[0][2];
-    const double dB = ss.tau[1][0] * ss.tau[1][3] - ss.tau[1][1] * ss.tau[1][2];
+    const T tA = ss.tau[0][0] * ss.tau[0][3] - ss.tau[0][1] * ss.tau[0][2];
+    const T tB = ss.tau[1][0] * ss.tau[1][3] - ss.tau[1][1] * ss.tau[1][2];
+    double dA, dB;
+    if constexpr (KIND == KDQ_TV) {   // det Tau (src/tV/SCEE.jl:458-459)
+      dA = re(tA);
+      dB = re(tB);
+    } else {                          // |det Tau|^2 (src/tUV/SCEE.jl:366-367)
+      dA = abs2(tA);
+      dB = abs2(tB);
+    }
     const double p = p0 * (pow(dA, P.scee_lam) * pow(dB, 1.0 - P.scee_lam));
     int acc = u < p;
     if (isnan(p)) {
@@ -708,56 +736,56 @@ __device__ void scee_propose_tv(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& 
   // GMupdate!: inv <- inv - (inv a) Tau^-1 b
   for (int g = 0; g < 2; ++g) {
     const int n = rn[g];
-    double* iv = inv[g];
+    T* iv = inv[g];
     auto IV = [&](int l, int m) { return iv[l + (size_t)m * n]; };
-    for (int qc = 0; qc < 2; ++qc) matvec<double>(n, IV, ss.a[g][qc], ss.y[g][qc], ss.part);
-    const double* tg = ss.tau[g];
-    const double td = 1.0 / (tg[0] * tg[3] - tg[1] * tg[2]);
-    const double t00 = tg[3] * td, t01 = -tg[1] * td, t10 = -tg[2] * td, t11 = tg[0] * td;
+    for (int qc = 0; qc < 2; ++qc) matvec<T>(n, IV, ss.a[g][qc], ss.y[g][qc], ss.part);
+    const T* tg = ss.tau[g];
+    const T td = one<T>() / (tg[0] * tg[3] - tg[1] * tg[2]);
+    const T t00 = tg[3] * td, t01 = (zero<T>() - tg[1]) * td, t10 = (zero<T>() - tg[2]) * td, t11 = tg[0] * td;
     for (int m = threadIdx.x; m < n; m += blockDim.x) {
-      const double b0 = ss.b[g][0][m], b1 = ss.b[g][1][m];
+      const T b0 = ss.b[g][0][m], b1 = ss.b[g][1][m];
       ss.w[0][m] = t00 * b0 + t01 * b1;
       ss.w[1][m] = t10 * b0 + t11 * b1;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
       const int l = e % n, m = e / n;
-      iv[e] -= ss.y[g][0][l] * ss.w[0][m] + ss.y[g][1][l] * ss.w[1][m];
+      iv[e] = iv[e] - (ss.y[g][0][l] * ss.w[0][m] + ss.y[g][1][l] * ss.w[1][m]);
     }
     __syncthreads();
   }
   // G4update!: z1 = r Gt0[S,:], z2 = E_S r - r Gt[S,:]
-  double* c0t0 = ss.g4[0];
-  double* c0t1 = ss.g4[1];
-  double* ct0 = ss.g4[2];
-  double* ct1 = ss.g4[3];
-  double* z10 = ss.g4[4];
-  double* z11 = ss.g4[5];
-  double* z20 = ss.g4[6];
-  double* z21 = ss.g4[7];
+  T* c0t0 = ss.g4[0];
+  T* c0t1 = ss.g4[1];
+  T* ct0 = ss.g4[2];
+  T* ct1 = ss.g4[3];
+  T* z10 = ss.g4[4];
+  T* z11 = ss.g4[5];
+  T* z20 = ss.g4[6];
+  T* z21 = ss.g4[7];
   for (int b = threadIdx.x; b < N; b += blockDim.x) {
     c0t0[b] = q.G0t[b + (size_t)S[0] * N];
     c0t1[b] = q.G0t[b + (size_t)S[1] * N];
     ct0[b] = G[b + (size_t)S[0] * N];
     ct1[b] = G[b + (size_t)S[1] * N];
-    const double t0 = q.Gt0[S[0] + (size_t)b * N], t1 = q.Gt0[S[1] + (size_t)b * N];
+    const T t0 = q.Gt0[S[0] + (size_t)b * N], t1 = q.Gt0[S[1] + (size_t)b * N];
     z10[b] = r00 * t0 + r01 * t1;
     z11[b] = r10 * t0 + r11 * t1;
-    const double g0 = G[S[0] + (size_t)b * N], g1 = G[S[1] + (size_t)b * N];
-    double w0 = -(r00 * g0 + r01 * g1), w1 = -(r10 * g0 + r11 * g1);
-    if (b == S[0]) { w0 += r00; w1 += r10; }
-    if (b == S[1]) { w0 += r01; w1 += r11; }
+    const T g0 = G[S[0] + (size_t)b * N], g1 = G[S[1] + (size_t)b * N];
+    T w0 = zero<T>() - (r00 * g0 + r01 * g1), w1 = zero<T>() - (r10 * g0 + r11 * g1);
+    if (b == S[0]) { w0 = w0 + r00; w1 = w1 + r10; }
+    if (b == S[1]) { w0 = w0 + r01; w1 = w1 + r11; }
     z20[b] = w0;
     z21[b] = w1;
   }
   __syncthreads();
   for (Walk w(N, N); w.ok(); w.next()) {
-    const double a0 = c0t0[w.i], a1 = c0t1[w.i], e0 = ct0[w.i], e1 = ct1[w.i];
-    const double y0 = z10[w.j], y1 = z11[w.j], x0 = z20[w.j], x1 = z21[w.j];
-    q.G0[w.e] += a0 * y0 + a1 * y1;
-    q.Gt0[w.e] += e0 * y0 + e1 * y1;
-    q.G0t[w.e] -= a0 * x0 + a1 * x1;
-    c.G[w.e] -= e0 * x0 + e1 * x1;
+    const T a0 = c0t0[w.i], a1 = c0t1[w.i], e0 = ct0[w.i], e1 = ct1[w.i];
+    const T y0 = z10[w.j], y1 = z11[w.j], x0 = z20[w.j], x1 = z21[w.j];
+    q.G0[w.e] = q.G0[w.e] + (a0 * y0 + a1 * y1);
+    q.Gt0[w.e] = q.Gt0[w.e] + (e0 * y0 + e1 * y1);
+    q.G0t[w.e] = q.G0t[w.e] - (a0 * x0 + a1 * x1);
+    c.G[w.e] = c.G[w.e] - (e0 * x0 + e1 * x1);
   }
   if (threadIdx.x == 0) *sf = (uint8_t)sx;
   __syncthreads();
@@ -766,7 +794,7 @@ __device__ void scee_propose_tv(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& 
 // The bonds of direction j of slice lt, both replicas alternating per bond
 template <int MAXRM, int KIND, class T, class KT>
 __device__ void scee_layer_tv(Ctx<KIND, T, KT, T, KT>* c, const SceeChain<T>* q, int lt, int j, bool fwd,
-                              SceeSmemTV& ss, int pair) {
+                              SceeSmem2<T>& ss, int pair) {
   const SweepParams& P = c[0].P;
   const int nb = P.Ns / 2, Nt = P.Nt, pf = P.n_field;
   const uint32_t qs = fwd ? (uint32_t)(lt - 1) * pf : (uint32_t)(Nt + (Nt - lt)) * pf;
@@ -775,8 +803,11 @@ __device__ void scee_layer_tv(Ctx<KIND, T, KT, T, KT>* c, const SceeChain<T>* q,
   load_tape(c[1], qs + off, nb);
   const long long lb0 = c[0].ctl->log_pos, lb1 = c[1].ctl->log_pos;
   for (int i = 0; i < nb; ++i) {
-    scee_propose_tv<MAXRM>(c[0], q[0], q[1], 0, lt, j, i, c[0].tk[i], c[0].tu[i], lb0 + i, ss, pair);
-    scee_propose_tv<MAXRM>(c[1], q[1], q[0], 1, lt, j, i, c[1].tk[i], c[1].tu[i], lb1 + i, ss, pair);
+    const int x = P.bx[j * nb + i], y = P.by[j * nb + i];
+    uint8_t* f0 = c[0].s + (size_t)(lt - 1) * pf + (size_t)j * nb + i;
+    uint8_t* f1 = c[1].s + (size_t)(lt - 1) * pf + (size_t)j * nb + i;
+    scee_propose2<MAXRM>(c[0], q[0], q[1], 0, lt, x, y, f0, c[0].tk[i], c[0].tu[i], lb0 + i, ss, pair);
+    scee_propose2<MAXRM>(c[1], q[1], q[0], 1, lt, x, y, f1, c[1].tk[i], c[1].tu[i], lb1 + i, ss, pair);
   }
   if (threadIdx.x == 0) {
     c[0].ctl->log_pos += nb;
@@ -787,10 +818,42 @@ __device__ void scee_layer_tv(Ctx<KIND, T, KT, T, KT>* c, const SceeChain<T>* q,
   __syncthreads();
 }
 
+// All bonds of slice lt (t-UV), both replicas alternating per bond, the tape
+// slices loaded in chunks of Ns proposals
+template <int MAXRM, int KIND, class T, class KT>
+__device__ void scee_layer_tuv(Ctx<KIND, T, KT, T, KT>* c, const SceeChain<T>* q, int lt, bool fwd,
+                               SceeSmem2<T>& ss, int pair) {
+  const SweepParams& P = c[0].P;
+  const int N = P.Ns, Nt = P.Nt, pf = P.n_field;
+  const uint32_t qs = fwd ? (uint32_t)(lt - 1) * pf : (uint32_t)(Nt + (Nt - lt)) * pf;
+  for (int c0 = 0; c0 < pf; c0 += N) {
+    const int n = min(N, pf - c0);
+    load_tape(c[0], qs + c0, n);
+    load_tape(c[1], qs + c0, n);
+    const long long lb0 = c[0].ctl->log_pos, lb1 = c[1].ctl->log_pos;
+    for (int i = 0; i < n; ++i) {
+      const int b = c0 + i, x = P.bx[b], y = P.by[b];
+      uint8_t* f0 = c[0].s + (size_t)(lt - 1) * pf + b;
+      uint8_t* f1 = c[1].s + (size_t)(lt - 1) * pf + b;
+      scee_propose2<MAXRM>(c[0], q[0], q[1], 0, lt, x, y, f0, c[0].tk[i], c[0].tu[i], lb0 + i, ss, pair);
+      scee_propose2<MAXRM>(c[1], q[1], q[0], 1, lt, x, y, f1, c[1].tk[i], c[1].tu[i], lb1 + i, ss, pair);
+    }
+    if (threadIdx.x == 0) {
+      c[0].ctl->log_pos += n;
+      c[1].ctl->log_pos += n;
+    }
+    finish_tape(c[0], n);
+    finish_tape(c[1], n);
+    __syncthreads();
+  }
+}
+
 template <int KIND, class T>
 struct SceeSmemOf { using type = SceeSmem<T>; };
 template <class T>
-struct SceeSmemOf<KDQ_TV, T> { using type = SceeSmemTV; };
+struct SceeSmemOf<KDQ_TV, T> { using type = SceeSmem2<T>; };
+template <class T>
+struct SceeSmemOf<KDQ_TUV, T> { using type = SceeSmem2<T>; };
 
 template <int MAXRM, int KIND, class T, class KT>
 __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, int mode, int k) {
@@ -849,6 +912,11 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
           scee_layer_tv<MAXRM>(c, q, lt, j, true, ss, pair);
         }
         scee_accumulate(P, pair);
+      } else if constexpr (KIND == KDQ_TUV) {   // src/tUV/SCEE.jl:108-140
+        scee_wrap<MAXRM>(c[0], q[0], lt, true);
+        scee_wrap<MAXRM>(c[1], q[1], lt, true);
+        scee_layer_tuv<MAXRM>(c, q, lt, true, ss, pair);
+        scee_accumulate(P, pair);
       } else {
         scee_wrap<MAXRM>(c[0], q[0], lt, true);
         if (nrep == 2) scee_wrap<MAXRM>(c[1], q[1], lt, true);
@@ -874,6 +942,11 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
         scee_wrapk<MAXRM>(c[0], q[0], false);
         scee_wrapk<MAXRM>(c[1], q[1], false);
         scee_accumulate(P, pair);
+      } else if constexpr (KIND == KDQ_TUV) {   // src/tUV/SCEE.jl:228-258: the wraps come before the node step
+        scee_layer_tuv<MAXRM>(c, q, lt, false, ss, pair);
+        scee_accumulate(P, pair);
+        scee_wrap<MAXRM>(c[0], q[0], lt, false);
+        scee_wrap<MAXRM>(c[1], q[1], lt, false);
       } else {
         scee_layer<MAXRM>(c, q, lt, false, ss, pair);
       }
@@ -885,7 +958,7 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_scee(const SweepParams P, in
           for (int i = idx + 1; i <= max(Th, idx); ++i) scee_br<MAXRM>(c[r], q[r], i);
         }
         scee_abgm<MAXRM>(c, q, idx, false, pair);
-      } else if constexpr (KIND != KDQ_TV) {
+      } else if constexpr (KIND == KDQ_TU) {
         scee_wrap<MAXRM>(c[0], q[0], lt, false);
         if (nrep == 2) scee_wrap<MAXRM>(c[1], q[1], lt, false);
       }

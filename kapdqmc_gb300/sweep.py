@@ -286,7 +286,7 @@ class Sweeper:
     def scee_green(self, chain: int, which: int):
         """Green's function `which` (0 Gt, 1 G0, 2 Gt0, 3 G0t) of one replica."""
         N = self.model.Ns
-        cplx = self.model.kind != KIND_TV
+        cplx = self.model.is_complex
         out = np.empty((2 if cplx else 1) * N * N)
         self._ck(self.lib.kdq_scee_get_green(self.h, chain, which, out.ctypes.data, out.size))
         return (out.view(np.complex128) if cplx else out).reshape(N, N, order="F")
@@ -394,6 +394,10 @@ def _scee_csv_name(path, model, nlam):
         return repr(float(x))
 
     site = "[" + ", ".join(str(int(v)) for v in model.site) + "]"
+    if model.kind == KIND_TUV:   # src/tUV/SCEE.jl:16-26
+        name = {"SQUARE45": "□", "SQUARE90": "□", "HoneyComb60": "HC60", "HoneyComb120": "HC120"}[model.Lattice]
+        return os.path.join(path, f"tUVSCEE{name}_t{f(model.Ht)}U{f(model.U)}V{f(model.V)}size{site}Δt{f(model.Δt)}"
+                                  f"Θ{f(model.Θ)}N{nlam}BS{model.BatchSize}.csv")
     if model.kind == KIND_TV:
         name = {"SQUARE45": "□", "SQUARE90": "□", "HoneyComb60": "HC", "HoneyComb120": "HC120"}[model.Lattice]
         if len(np.unique(model.α)) == 1:
@@ -412,12 +416,12 @@ def _scee_csv_name(path, model, nlam):
 def ctrl_SCEEicr(path, model, indexA, indexB, Sweeps: int, λ: float, Nλ: int, ss, record: bool, *,
                  seed=None, tape=None, device: int = 0):
     """Coupled incremental SCEE sweep of the replica pair(s) ``ss``
-    (src/tU/SCEE.jl:1-211, src/tV/SCEE.jl:1-431): returns the updated fields.  ``ss`` is a pair
+    (src/tU/SCEE.jl:1-211, src/tV/SCEE.jl:1-431, src/tUV/SCEE.jl:1-339):
+    returns the updated fields.  ``ss`` is a pair
     [s1, s2] or a stack of pairs (n_pairs, 2, ...); with ``record`` one CSV row
     per pair (lambda, then the per-sweep estimator) is appended to the
     reference's file name under ``path`` and the rows are also returned."""
-    if model.kind not in (KIND_TU, KIND_TV):
-        raise ValueError("ctrl_SCEEicr is implemented for t-U and t-V")
+
     ss = np.asarray(ss, dtype=np.uint8)
     single = ss.ndim == len(model.field_shape) + 1
     pairs = ss[None] if single else ss

@@ -467,3 +467,91 @@ class SCEE_TV(SCEE):
 
 def proposals_per_sweep_tv(model) -> int:
     return 2 * 2 * (model.Ns // 2) * model.z * model.Nt
+
+
+class SCEE_TUV(SCEE):
+    """ctrl_SCEEicr for t-UV (src/tUV/SCEE.jl:1-402): site phases summed over
+    the bonds (eta on the bond's first site, a eta on its second), the same
+    one- and two-sided slice wraps as t-U, rank-2 bond proposals with
+    |det Tau|^2 factors and |det g|^2 Grover weights.  As in the reference's
+    UpdateSCEELayer! (:355-402) the real-type extra weight
+    exp((eta - eta')(a + 1)) of the plain sweep is not applied, and the
+    backward sweep wraps every slice before the node step (:225-275)."""
+
+    def __init__(self, model, s1, s2, indexA, indexB, lam, nlam, tape):
+        super().__init__(model, s1, s2, indexA, indexB, lam, nlam, tape)
+        dt = np.complex128 if model.is_complex else np.float64
+        self.I = np.eye(model.Ns, dtype=dt)
+        self.uv = []
+        for r in range(2):
+            sw = O._TUVSweep(model, self.s[r], O.Tape([], []), False)
+            sw.s = self.s[r]
+            self.uv.append(sw)
+
+    def D(self, r, lt, sign=1.0):
+        return self.uv[r].phase(lt, sign)
+
+    def propose_bond(self, r, lt, b):
+        m, s, sw = self.m, self.s[r], self.uv[r]
+        x, y = int(sw.X[b]), int(sw.Y[b])
+        S = [x, y]
+        k, u = self.tape.draw()
+        sold = int(s[b, lt - 1])
+        sx = O._sx(sold, k)
+        Δs = m.η[sx - 1] - m.η[sold - 1]                                     # get_r!
+        t2 = np.array([Δs, m.a * Δs])
+        t2 = np.exp(1j * t2) - 1 if m.is_complex else np.exp(t2) - 1
+        Gt, Gt0, G0t = self.Gt[r], self.Gt0[r], self.G0t[r]
+        rm = -(t2[:, None] * Gt[np.ix_(S, S)])
+        rm[0, 0] = (t2[0] + rm[0, 0]) + 1
+        rm[1, 1] = (t2[1] + rm[1, 1]) + 1
+        p = abs(O.det22(rm)) ** 2
+        rr = O.inv22(rm) * t2[None, :]
+        p *= m.γ[sx - 1] / m.γ[sold - 1]
+        other = self.G0[1 - r]
+        taus = []
+        for reg, inv in ((self.A, self.invA), (self.B, self.invB)):
+            X = 2 * other[np.ix_(reg, reg)] - np.eye(len(reg))
+            if r == 0:
+                a = G0t[np.ix_(reg, S)] @ rr
+                b_ = (Gt0[np.ix_(S, reg)] @ X) @ inv
+            else:
+                a = X @ G0t[np.ix_(reg, S)]
+                b_ = (rr @ Gt0[np.ix_(S, reg)]) @ inv
+            tau = b_ @ a + np.eye(2)
+            taus.append((a, b_, tau, abs(O.det22(tau)) ** 2))
+        dA, dB = taus[0][3], taus[1][3]
+        p *= dA ** self.lam * dB ** (1 - self.lam)
+        self.last_p = p
+        acc = u < p
+        self.accepts.append(bool(acc))
+        if acc:
+            self.detA *= dA
+            self.detB *= dB
+            for (a, b_, tau, _), name in zip(taus, ("invA", "invB")):
+                inv = getattr(self, name)
+                setattr(self, name, inv - (inv @ a) @ O.inv22(tau) @ b_)
+            G0 = self.G0[r]
+            zN = rr @ Gt0[S, :]
+            c0t, ct = G0t[:, S].copy(), Gt[:, S].copy()
+            G0 += c0t @ zN
+            Gt0 += ct @ zN
+            zN = -rr @ Gt[S, :]
+            zN[:, S] += rr
+            G0t -= c0t @ zN
+            Gt -= ct @ zN
+            s[b, lt - 1] = sx
+
+    def layer(self, lt):
+        for b in range(len(self.uv[0].X)):
+            self.propose_bond(0, lt, b)
+            self.propose_bond(1, lt, b)
+
+    def backward_slice(self, lt):   # wraps before the node step
+        self.layer(lt)
+        val = (self.detA / self.detB) ** (1 / self.nlam)
+        for r in range(2):
+            self.wrap(r, lt, False)
+        if (lt - 1) in self.nodes:
+            SCEE_TV.node_step(self, forward=False)
+        return val

@@ -140,3 +140,42 @@ def test_scee_tv_matches_oracle(make):
                 rel = np.linalg.norm(Gs[2 * p + r][w] - G) / np.linalg.norm(G)
                 assert rel < 1e-8, (p, r, w, rel)
         np.testing.assert_allclose(Orows[p, 1:], ref.O, rtol=1e-8)
+
+
+def _tape_tuv(seed, pair, sweeps, m):
+    n_rep = 2 * m.Ns * m.z * m.Nt
+    ks, us = [], []
+    for w in range(sweeps):
+        k0, u0 = philox.tape(seed, 2 * pair, w, n_rep)
+        k1, u1 = philox.tape(seed, 2 * pair + 1, w, n_rep)
+        ks.append(np.stack([k0, k1], axis=1).ravel())
+        us.append(np.stack([u0, u1], axis=1).ravel())
+    return O.Tape(np.concatenate(ks), np.concatenate(us))
+
+
+@pytest.mark.parametrize("make", [cases.tuv_honeycomb, lambda: cases.tuv_honeycomb(U=-4.0), cases.tuv_square])
+def test_scee_tuv_matches_oracle(make):
+    m = make()
+    A, B = regions(m) if "HoneyComb" in m.Lattice else ([1, 2, 3, 4, 5, 6], [1, 2, 3])
+    npairs, sweeps, seed, lam, nlam = 2, 2, 23, 0.5, 2
+    fields = np.stack([Initial_s(m, 30 + c) for c in range(2 * npairs)])
+    n_rep = 2 * m.Ns * m.z * m.Nt
+    with Sweeper(m, 2 * npairs) as sw:
+        sw.set_fields(fields)
+        sw.set_rng(seed)
+        sw.enable_accept_log(n_rep * sweeps)
+        sw.scee_enable(A, B, lam, nlam)
+        Orows = sw.scee_run(sweeps)
+        s_gpu = sw.get_fields()
+        acc = sw.accept_log()
+        Gs = [[sw.scee_green(c, w) for w in range(4)] for c in range(2 * npairs)]
+    for p in range(npairs):
+        ref = S.SCEE_TUV(m, fields[2 * p], fields[2 * p + 1], A, B, lam, nlam, _tape_tuv(seed, p, sweeps, m)).run(sweeps)
+        ra = np.array(ref.accepts).reshape(-1, 2)
+        for r in range(2):
+            np.testing.assert_array_equal(acc[2 * p + r].astype(bool), ra[:, r], err_msg=f"pair {p} replica {r}")
+            np.testing.assert_array_equal(s_gpu[2 * p + r], ref.s[r])
+            for w, G in enumerate((ref.Gt[r], ref.G0[r], ref.Gt0[r], ref.G0t[r])):
+                rel = np.linalg.norm(Gs[2 * p + r][w] - G) / np.linalg.norm(G)
+                assert rel < 1e-9, (p, r, w, rel)
+        np.testing.assert_allclose(Orows[p, 1:], ref.O, rtol=1e-8)

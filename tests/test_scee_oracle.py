@@ -224,3 +224,29 @@ def test_scee_tv_state_and_ratio():
     s1[i, j, lt - 1] = O._sx(sold, 1)
     dw = total([s1, sc2.s[1]]) - total(sc2.s)
     assert p > 0 and abs(dw - np.log(p)) < 1e-8, (dw, np.log(p))
+
+
+@pytest.mark.parametrize("U", [4.0, -4.0])
+def test_scee_tuv_state_matches_brute_force(U):
+    m = cases.tuv_honeycomb(U=U)
+    A, B = regions(m)
+    n = 4 * m.Ns * m.z * m.Nt
+    k, u = philox.tape(9, 0, 0, n)
+    sc = S.SCEE_TUV(m, Initial_s(m, 1), Initial_s(m, 2), A, B, 0.5, 2, O.Tape(k, u)).init()
+    for lt in range(1, m.Nt + 1):
+        sc.forward_slice(lt)
+    for lt in range(m.Nt, 7, -1):
+        sc.backward_slice(lt)
+    for r in range(2):
+        s, sw = sc.s[r], O._TUVSweep(m, sc.s[r], O.Tape([], []), False)
+        t0, tau = sc.nodes[sc.Θ - 1], 7
+        Gt, G0 = O.G_tau(m, s, tau), O.G_tau(m, s, t0)
+        M = np.eye(m.Ns, dtype=sc.I.dtype)
+        for lt in range(tau + 1, t0 + 1):
+            M = sw.B_left(lt, M)
+        ref = (Gt, G0, -(np.eye(m.Ns) - Gt) @ np.linalg.inv(M), M @ Gt)
+        for got, want in zip((sc.Gt[r], sc.G0[r], sc.Gt0[r], sc.G0t[r]), ref):
+            assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-9
+    d, i = sc.grover(sc.A)
+    assert abs(sc.detA - d) < 1e-9 * d
+    assert 0 < sum(sc.accepts) < len(sc.accepts)
