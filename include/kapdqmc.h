@@ -295,7 +295,7 @@ int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice,
 
 /* Coupled incremental SCEE sweep, ctrl_SCEEicr(path, model, indexA, indexB,
  * Sweeps, lambda, Nlambda, ss, record) (src/tU/SCEE.jl:1-211,
- * src/tV/SCEE.jl:1-431), t-U and t-V in FP64.
+ * src/tV/SCEE.jl:1-431, src/tUV/SCEE.jl:1-339), t-U, t-V and t-UV in FP64.
  * Chains 2p and 2p+1 of the handle are the two replicas ss[1], ss[2] of pair
  * p (fields through kdq_set_fields, random stream through kdq_set_rng or
  * kdq_set_tape, replica r of pair p drawing from chain 2p+r's stream in the
@@ -307,12 +307,14 @@ int kdq_slmc_enable(kdq_handle* h, const float* params, int32_t moves_per_slice,
  * (t-U, UpdateSCEELayer!, src/tU/SCEE.jl:230-287; t-V: each bond proposal
  * with (det g_A'/det g_A)^lambda (det g_B'/det g_B)^(1-lambda), the bond
  * rotations of each direction wrapped between that direction's updates,
- * src/tV/SCEE.jl:87-330,447-508).  O receives per pair the reference's CSV
+ * src/tV/SCEE.jl:87-330,447-508; t-UV: bond proposals with
+ * |det Tau|^2 factors and without the plain sweep's real-type factor,
+ * src/tUV/SCEE.jl:355-402).  O receives per pair the reference's CSV
  * row: O[p (sweeps+1)] = lambda, then per sweep the mean over slices of
- * (detg_A / detg_B)^(1/Nlambda), detg = |det g|^2 (t-U) or det g (t-V);
+ * (detg_A / detg_B)^(1/Nlambda), detg = |det g|^2 (t-U, t-UV) or det g (t-V);
  * len counts doubles.  kdq_scee_get_green copies one replica's Green's
  * function `which` (0: G(tau,tau), 1: G(tau0,tau0) at the middle node,
- * 2: G(tau,tau0), 3: G(tau0,tau); Ns^2 values, complex for t-U as 2 doubles
+ * 2: G(tau,tau0), 3: G(tau0,tau); Ns^2 values, complex sweeps as 2 doubles
  * each) at the end of the run (tau = 0).
  * After kdq_scee_run, kdq_init must precede a plain sweep. */
 int kdq_scee_enable(kdq_handle* h, const int32_t* indexA, int32_t nA, const int32_t* indexB, int32_t nB,
