@@ -42,6 +42,7 @@ _SIGS = {
     "kdq_dop_enable": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
                                  C.c_double, C.c_int32]),
     "kdq_dop_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]),
+    "kdq_set_measure_full": (C.c_int, [C.c_void_p, C.c_int32]),
     "kdq_cnn_forward": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
     "kdq_cnn_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                C.c_int32]),

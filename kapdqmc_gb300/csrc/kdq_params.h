@@ -40,6 +40,7 @@ struct ChainCtl {
 struct SweepParams {
   // model
   int kind, Ns, Nt, z, n_field, NN, n_obs, record;
+  int meas_full;                // t-U: 4 more columns, the structure factors with all terms
   int lattice, L1, L2;
   int site_nb;                  // tUV: entries per site in site_bonds
   const int64_t* nodes;         // NN

@@ -1078,6 +1078,18 @@ __device__ void observables(Ctx<KIND, T, KT, TW, KW>& c, const TW* G0) {
                re((o - g(a1, a1)) * (o - g(b2, b2)) - g(a1, b2) * g(b2, a1));
           t2 = re((o - g(a1, a1)) * conjg(g(a2, a2))) + re((o - g(b1, b1)) * conjg(g(b2, b2))) -
                re((o - g(a1, a1)) * conjg(g(b2, b2))) - re((o - g(b1, b1)) * conjg(g(a2, a2)));
+          if (P.meas_full) {   // the discarded adjoint (opposite-spin) terms restored
+            const double u1 = t1 + re(conjg(g(a1, a1) * g(a2, a2) + g(a1, a2) * (del - g(a2, a1)))) +
+                              re(conjg(g(b1, b1) * g(b2, b2) + g(b1, b2) * (del - g(b2, b1)))) -
+                              re(conjg(g(b1, b1) * g(a2, a2) - g(b1, a2) * g(a2, b1))) -
+                              re(conjg(g(a1, a1) * g(b2, b2) - g(a1, b2) * g(b2, a1)));
+            const double u2 = t2 + re(conjg(g(a1, a1)) * (o - g(a2, a2))) + re(conjg(g(b1, b1)) * (o - g(b2, b2))) -
+                              re(conjg(g(a1, a1)) * (o - g(b2, b2))) - re(conjg(g(b1, b1)) * (o - g(a2, a2)));
+            sf[4] += u1 + u2;
+            sf[5] += ph * (u1 + u2);
+            sf[6] += u1 - u2;
+            sf[7] += ph * (u1 - u2);
+          }
         }
         sf[0] += t1 + t2;
         sf[1] += ph * (t1 + t2);
@@ -1089,13 +1101,15 @@ __device__ void observables(Ctx<KIND, T, KT, TW, KW>& c, const TW* G0) {
   ek = block_sum(ek, c.sm.red);
   eu = block_sum(eu, c.sm.red);
   ev = block_sum(ev, c.sm.red);
-  const int nsf = KIND == KDQ_TV ? 8 : 4;
+  const int nsf = (KIND == KDQ_TV || P.meas_full) ? 8 : 4;
   for (int q = 0; q < nsf; ++q) sf[q] = block_sum(sf[q], c.sm.red);
   const double n2 = (double)N * N;
   if constexpr (KIND == KDQ_TU) {
     acc[0] = -2.0 * P.Ht * ek;
     acc[1] = eu;
     for (int q = 0; q < 4; ++q) acc[2 + q] = sf[q] / n2;
+    if (P.meas_full)
+      for (int q = 0; q < 4; ++q) acc[6 + q] = sf[4 + q] / n2;
   } else if constexpr (KIND == KDQ_TV) {
     acc[0] = P.Ht * ek;
     acc[1] = ev;

@@ -291,6 +291,12 @@ class Sweeper:
         self._ck(self.lib.kdq_scee_get_green(self.h, chain, which, out.ctypes.data, out.size))
         return (out.view(np.complex128) if cplx else out).reshape(N, N, order="F")
 
+    def set_measure_full(self, enable: bool = True):
+        """t-U: also measure the honeycomb structure factors with all terms
+        (columns 6-9 of every measurement row)."""
+        self._ck(self.lib.kdq_set_measure_full(self.h, int(bool(enable))))
+        self.n_obs = self.lib.kdq_n_obs(self.h)
+
     def slmc_stats(self):
         """(proposed, accepted, no-change) cluster moves of the last call."""
         out = np.zeros(3, dtype=np.int64)
@@ -516,7 +522,7 @@ def phy_update(path, model, s, Sweeps: int, record: bool = False, *, seed=None, 
             sw.close()
     out = out[0] if single else out
     if record:
-        if path:
-            _append_csv(_csv_name(path, model), obs.mean(axis=0))
+        if path:   # the reference's columns; further columns are returned only
+            _append_csv(_csv_name(path, model), obs.mean(axis=0)[..., :6 if model.kind == KIND_TU else None])
         return out, obs
     return out

@@ -128,6 +128,7 @@ class _Sweep:
         self.sweep_no = 0          # Philox sweep counter of the cluster moves
         self.slmc = None           # cluster-move configuration (t-U), see phy_update
         self.slmc_log: list = []   # (u, p) of every cluster-move decision
+        self.full_sf = False       # t-U: append the structure factors with all terms
 
     def node(self, k):  # 1-based access to nodes
         return self.nodes[k - 1]
@@ -292,13 +293,15 @@ class _TUSweep(_Sweep):
         out = [Ek, Eu.real, 0.0, 0.0, 0.0, 0.0]
         if "HoneyComb" in m.Lattice:
             out[2:] = _honeycomb_sf_quirk(m.site, G0, m.Ns, spinful_real=False)
+        if self.full_sf:
+            out += _honeycomb_sf_full(m.site, G0, m.Ns) if "HoneyComb" in m.Lattice else [0.0] * 4
         return np.array(out)
 
     def run(self, sweeps):
         m = self.m
         self.init_chain()
         for _ in range(sweeps):
-            acc, cnt = np.zeros(6), 0
+            acc, cnt = np.zeros(10 if self.full_sf else 6), 0
             for lt in range(1, m.Nt + 1):
                 self.G = self.wrap_forward(self.G, lt)
                 self.update_layer(lt)
@@ -612,6 +615,42 @@ def _honeycomb_sf_quirk(site, G0, Ns, spinful_real):
     return [float(np.real(v)) / n2 for v in (CDW0, CDW1, SDW0, SDW1)]
 
 
+def _honeycomb_sf_full(site, G0, Ns):
+    """CDW0, CDW1, SDW0, SDW1 of the complex branch with every term: each
+    correlator of src/tU/phy_update.jl:194-235 plus its ``+adjoint(...)``
+    continuation (the opposite-spin part), which the reference discards."""
+    L1, L2 = site
+    cells = _cells(site)
+    CDW0 = CDW1 = SDW0 = SDW1 = 0.0
+    g, c = G0, np.conj
+    for rx in range(1, L1 + 1):
+        for ry in range(1, L2 + 1):
+            t1 = t2 = 0.0
+            for (ix, iy), a1 in cells.items():
+                a2 = cells[((ix + rx - 1) % L1 + 1, (iy + ry - 1) % L2 + 1)]
+                b1, b2 = a1 + 1, a2 + 1
+                δ = 1.0 if a1 == a2 else 0.0
+                t1 += (1 - g[a1, a1]) * (1 - g[a2, a2]) + (δ - g[a1, a2]) * g[a2, a1] \
+                    + c(g[a1, a1] * g[a2, a2] + g[a1, a2] * (δ - g[a2, a1]))
+                t1 += (1 - g[b1, b1]) * (1 - g[b2, b2]) + (δ - g[b1, b2]) * g[b2, b1] \
+                    + c(g[b1, b1] * g[b2, b2] + g[b1, b2] * (δ - g[b2, b1]))
+                t1 -= (1 - g[b1, b1]) * (1 - g[a2, a2]) - g[b1, a2] * g[a2, b1] \
+                    + c(g[b1, b1] * g[a2, a2] - g[b1, a2] * g[a2, b1])
+                t1 -= (1 - g[a1, a1]) * (1 - g[b2, b2]) - g[a1, b2] * g[b2, a1] \
+                    + c(g[a1, a1] * g[b2, b2] - g[a1, b2] * g[b2, a1])
+                t2 += (1 - g[a1, a1]) * c(g[a2, a2]) + c(g[a1, a1]) * (1 - g[a2, a2])
+                t2 += (1 - g[b1, b1]) * c(g[b2, b2]) + c(g[b1, b1]) * (1 - g[b2, b2])
+                t2 -= (1 - g[a1, a1]) * c(g[b2, b2]) + c(g[a1, a1]) * (1 - g[b2, b2])
+                t2 -= (1 - g[b1, b1]) * c(g[a2, a2]) + c(g[b1, b1]) * (1 - g[a2, a2])
+            ph = math.cos(2 * math.pi / L1 * rx + 2 * math.pi / L2 * ry)
+            CDW0 += t1 + t2
+            CDW1 += ph * (t1 + t2)
+            SDW0 += t1 - t2
+            SDW1 += ph * (t1 - t2)
+    n2 = Ns ** 2
+    return [float(np.real(v)) / n2 for v in (CDW0, CDW1, SDW0, SDW1)]
+
+
 def _tv_density_sf(site, G0, Ns):
     """R0, R1 (4 sublattice components each).  src/tV/phy_update.jl:268-294."""
     L1, L2 = site
@@ -647,7 +686,7 @@ def proposals_per_sweep(model) -> int:
     return 2 * model.Nt * model.n_field
 
 
-def phy_update(model, s, sweeps: int, tape: Tape, record: bool = False, slmc=None):
+def phy_update(model, s, sweeps: int, tape: Tape, record: bool = False, slmc=None, full_sf: bool = False):
     """Run ``sweeps`` sweeps; returns the sweep object (s, G, accepts, drift, obs_rows).
 
     Mirrors ``phy_update(path, model, s, Sweeps, record)`` without the CSV side
@@ -656,6 +695,7 @@ def phy_update(model, s, sweeps: int, tape: Tape, record: bool = False, slmc=Non
     a dict with params, moves, cluster_len, steps, seed and chain.
     """
     sw = _SWEEPS[model.kind](model, s, tape, record)
+    sw.full_sf = full_sf
     if slmc is not None:
         if model.kind != KIND_TU:
             raise ValueError("cluster moves are restated for t-U only")

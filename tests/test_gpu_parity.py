@@ -254,3 +254,29 @@ def test_grover_det_at_middle_slice():
         mids.append(held["G"])
     want = [O.grover_det(mids[0], mids[1], index), O.grover_det(mids[2], mids[3], index)]
     np.testing.assert_allclose(dets, want, rtol=1e-8, atol=1e-12)
+
+
+@pytest.mark.parametrize("record", [1, 2])
+def test_full_structure_factors(record):
+    # t-U honeycomb with the structure factors' discarded adjoint terms restored
+    # (columns 6-9) next to the reference's columns
+    model = cases.tu_honeycomb()
+    nch, sweeps, seed = 2, 2, 77
+    fields = np.stack([Initial_s(model, 300 + c) for c in range(nch)])
+    with Sweeper(model, nch) as sw:
+        sw.set_measure_full(True)
+        sw.set_fields(fields)
+        sw.set_rng(seed)
+        obs = sw.phy_update(sweeps, record)
+    assert obs.shape == (nch, sweeps, 10)
+    for c in range(nch):
+        ref = _oracle_full(model, fields[c], seed, c, sweeps)
+        ro = np.array(ref.obs_rows)
+        err = np.abs(obs[c] - ro).max() / max(1.0, np.abs(ro).max())
+        assert err < (1e-8 if record == 2 else 1e-9), err
+
+
+def _oracle_full(model, s, seed, chain, sweeps):
+    n = O.proposals_per_sweep(model)
+    ks, us = zip(*(philox.tape(seed, chain, w, n) for w in range(sweeps)))
+    return O.phy_update(model, s, sweeps, O.Tape(np.concatenate(ks), np.concatenate(us)), True, full_sf=True)
