@@ -165,6 +165,96 @@ function phy_update(path::String, model, s, Sweeps::Int64, record::Bool=false;
     return s
 end
 
+"""
+    ctrl_SCEEicr(path, model, indexA, indexB, Sweeps, λ, Nλ, ss, record; seed, device)
+
+GPU replacement of the reference's coupled incremental SCEE sweep
+(src/tU/SCEE.jl:1-211, src/tV/SCEE.jl:1-431, src/tUV/SCEE.jl:1-339).  `ss` is
+the replica pair [s1, s2] (updated in place and returned); with `record` the
+row λ, O_1, ..., O_Sweeps is appended to the reference's file name under `path`.
+"""
+function ctrl_SCEEicr(path::String, model, indexA::Vector{Int64}, indexB::Vector{Int64}, Sweeps::Int64,
+                      λ::Float64, Nλ::Int64, ss, record; seed::Union{Nothing,Integer}=nothing, device::Integer=0)
+    h, _ = create(model, 2; device=device)
+    try
+        buf = vcat(vec(UInt8.(ss[1])), vec(UInt8.(ss[2])))
+        check(ccall((:kdq_set_fields, libkdq), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), h, buf, length(buf)), h)
+        sd = seed === nothing ? time_ns() : UInt64(seed)
+        check(ccall((:kdq_set_rng, libkdq), Cint, (Ptr{Cvoid}, UInt64, UInt64), h, sd, 0), h)
+        check(ccall((:kdq_scee_enable, libkdq), Cint, (Ptr{Cvoid}, Ptr{Int32}, Int32, Ptr{Int32}, Int32, Float64, Int32),
+                    h, Int32.(indexA), length(indexA), Int32.(indexB), length(indexB), λ, Nλ), h)
+        O = zeros(Float64, Sweeps + 1)
+        check(ccall((:kdq_scee_run, libkdq), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Csize_t), h, Sweeps, O, length(O)), h)
+        check(ccall((:kdq_get_fields, libkdq), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), h, buf, length(buf)), h)
+        n = length(ss[1])
+        copyto!(ss[1], reshape(buf[1:n], size(ss[1])))
+        copyto!(ss[2], reshape(buf[n+1:2n], size(ss[2])))
+        if record
+            open(scee_name(path, model, Nλ), "a") do io
+                writedlm(io, O', ',')
+            end
+        end
+    finally
+        destroy(h)
+    end
+    return ss
+end
+
+"""
+    ctrl_SCDOPicr(path, model, alpha, indexA, indexB, Sweeps, λ, Nλ, s, record; seed, device)
+
+GPU replacement of the reference's disorder-operator sweep
+(src/tU/disorder_operate.jl:1-247), t-U.
+"""
+function ctrl_SCDOPicr(path::String, model, alpha::Float64, indexA::Vector{Int64}, indexB::Vector{Int64},
+                       Sweeps::Int64, λ::Float64, Nλ::Int64, s, record; seed::Union{Nothing,Integer}=nothing,
+                       device::Integer=0)
+    h, _ = create(model, 1; device=device)
+    try
+        buf = vec(UInt8.(s))
+        check(ccall((:kdq_set_fields, libkdq), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), h, buf, length(buf)), h)
+        sd = seed === nothing ? time_ns() : UInt64(seed)
+        check(ccall((:kdq_set_rng, libkdq), Cint, (Ptr{Cvoid}, UInt64, UInt64), h, sd, 0), h)
+        check(ccall((:kdq_dop_enable, libkdq), Cint,
+                    (Ptr{Cvoid}, Float64, Ptr{Int32}, Int32, Ptr{Int32}, Int32, Float64, Int32),
+                    h, alpha, Int32.(indexA), length(indexA), Int32.(indexB), length(indexB), λ, Nλ), h)
+        O = zeros(Float64, Sweeps + 1)
+        check(ccall((:kdq_dop_run, libkdq), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Csize_t), h, Sweeps, O, length(O)), h)
+        check(ccall((:kdq_get_fields, libkdq), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), h, buf, length(buf)), h)
+        copyto!(s, reshape(buf, size(s)))
+        if record
+            name = Dict("SQUARE90" => "□90", "SQUARE45" => "□45", "HoneyComb60" => "HC", "HoneyComb120" => "HC120")[model.Lattice]
+            file = length(unique(model.α)) == 1 ?
+                "$(path)/tUSCDOP$(name)_t$(model.Ht)U$(model.Hu1)size$(model.site)Δt$(model.Δt)Θ$(model.Θrelax)N$(Nλ)BS$(model.BatchSize).csv" :
+                "$(path)/tUSCDOP$(name)_t$(model.Ht)U$(model.Hu1)_$(model.Hu2)size$(model.site)Δt$(model.Δt)Θ$(model.Θrelax)_$(model.Θquench)N$(Nλ)BS$(model.BatchSize).csv"
+            open(file, "a") do io
+                writedlm(io, O', ',')
+            end
+        end
+    finally
+        destroy(h)
+    end
+    return s
+end
+
+# SCEE CSV names (src/tU/SCEE.jl:16-32, src/tV/SCEE.jl:16-32, src/tUV/SCEE.jl:16-26)
+function scee_name(path, model::KAPDQMC.tUDQMC.tU_Hubbard_Para_, Nλ)
+    name = Dict("SQUARE90" => "□90", "SQUARE45" => "□45", "HoneyComb60" => "HC", "HoneyComb120" => "HC120")[model.Lattice]
+    model.Θquench == 0.0 ?
+        "$(path)/tUSCEE$(name)_t$(model.Ht)U$(model.Hu1)size$(model.site)Δt$(model.Δt)Θ$(model.Θrelax)N$(Nλ)BS$(model.BatchSize).csv" :
+        "$(path)/tUSCEE$(name)_t$(model.Ht)U$(model.Hu1)_$(model.Hu2)size$(model.site)Δt$(model.Δt)Θ$(model.Θrelax)_$(model.Θquench)N$(Nλ)BS$(model.BatchSize).csv"
+end
+function scee_name(path, model::KAPDQMC.tVDQMC.tV_Hubbard_Para_, Nλ)
+    name = occursin("SQUARE", model.Lattice) ? "□" : (model.Lattice == "HoneyComb60" ? "HC" : "HC120")
+    length(unique(model.α)) == 1 ?
+        "$(path)/tVSCEE$(name)_t$(model.Ht)V$(model.Hv1)size$(model.site)Δt$(model.Δt)Θ$(model.Θrelax)N$(Nλ)BS$(model.BatchSize).csv" :
+        "$(path)/tVSCEE$(name)_t$(model.Ht)V$(model.Hv1)_$(model.Hv2)size$(model.site)Δt$(model.Δt)Θ$(model.Θrelax)_$(model.Θquench)N$(Nλ)BS$(model.BatchSize).csv"
+end
+function scee_name(path, model::KAPDQMC.tUVDQMC.tUV_Hubbard_Para_, Nλ)
+    name = occursin("SQUARE", model.Lattice) ? "□" : (model.Lattice == "HoneyComb60" ? "HC60" : "HC120")
+    "$(path)/tUVSCEE$(name)_t$(model.Ht)U$(model.U)V$(model.V)size$(model.site)Δt$(model.Δt)Θ$(model.Θ)N$(Nλ)BS$(model.BatchSize).csv"
+end
+
 # CSV names of the reference (src/tU/phy_update.jl:12-27, src/tV/phy_update.jl:10-23,
 # src/tUV/phy_update.jl:13-22)
 function csv_name(path, model::KAPDQMC.tUDQMC.tU_Hubbard_Para_)
