@@ -622,13 +622,22 @@ def run_scee(args):
     secs = e0.elapsed_time(e1) * 1e-3
     sw.close()
     est = O[:, 1:]
+    # algorithmic FP64 work of the slice wraps alone (a lower bound of the
+    # sweep's work): per slice and replica Gt two N^3 products, Gt0 and G0t one
+    # each, complex (8 flops per multiply-add), both directions
+    wrap_flops = 2 * model.Nt * 2 * 4 * model.Ns ** 3 * 8
+    peak = fp64_peak_tflops(torch, dev)
+    achieved = wrap_flops * pairs * args.steps / secs / 1e12
     out = {"metric": "SCEE pair-sweeps/s (ctrl_SCEEicr)", "value": pairs * args.steps / secs,
            "unit": "pair-sweeps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": secs * 1e3 / args.steps, "higher_is_better": True, "dtype": "c128",
            "data": "synthetic (seeded HS fields and Philox stream)",
            "config": dict(config(), pairs=pairs, nA=len(A), nB=len(B), lam=0.5, nlam=2,
                           timed="one kdq_scee_run call: block products and chains rebuilt, then the sweeps"),
-           "estimator_mean": float(est.mean()), "estimator_err": float(est.mean(axis=1).std() / math.sqrt(pairs))}
+           "estimator_mean": float(est.mean()), "estimator_err": float(est.mean(axis=1).std() / math.sqrt(pairs)),
+           "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                        "counted": "slice wraps only (8 N^3 complex multiply-adds per slice and pair)",
+                        "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}}
     if not args.no_cpu:
         sys.path.insert(0, str(ROOT / "oracle"))
         import dqmc_oracle as O_
