@@ -37,12 +37,18 @@ __device__ __forceinline__ int wrap1(int v, int n) {  // v in [-n, 2n)
 
 __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
+// Activation rows in shared memory are padded to an odd stride, so that the
+// 16 channels of one site fall into 16 different banks.
+__host__ __device__ inline int pad_stride(int Ns) { return Ns | 1; }
+
 size_t fwd_smem(int R, int Ns) {
-  return align16(sizeof(CnnW)) + align16((size_t)(R + 2) * CH * Ns * sizeof(float)) + align16((size_t)(R + 4) * Ns);
+  const int Sp = pad_stride(Ns);
+  return align16(sizeof(CnnW)) + align16((size_t)(R + 2) * CH * Sp * sizeof(float)) + align16((size_t)(R + 4) * Ns);
 }
 size_t bwd_smem(int R, int Ns) {
-  return align16(sizeof(CnnW)) + align16((size_t)(R + 4) * CH * Ns * sizeof(float)) +
-         align16((size_t)(R + 2) * CH * Ns * sizeof(float)) + align16((size_t)R * CH * Ns * sizeof(float)) +
+  const int Sp = pad_stride(Ns);
+  return align16(sizeof(CnnW)) + align16((size_t)(R + 4) * CH * Sp * sizeof(float)) +
+         align16((size_t)(R + 2) * CH * Sp * sizeof(float)) + align16((size_t)R * CH * Sp * sizeof(float)) +
          align16((size_t)(R + 6) * Ns) + 64 * sizeof(float);
 }
 
@@ -52,8 +58,9 @@ __global__ void __launch_bounds__(256) k_cnn_fwd(const uint8_t* __restrict__ fie
                                                  double* __restrict__ F) {
   extern __shared__ __align__(16) unsigned char smem[];
   CnnW& w = *reinterpret_cast<CnnW*>(smem);
+  const int Sp = pad_stride(Ns);
   float* a1 = reinterpret_cast<float*>(smem + align16(sizeof(CnnW)));
-  uint8_t* x = reinterpret_cast<uint8_t*>(a1) + align16((size_t)(R + 2) * CH * Ns * sizeof(float));
+  uint8_t* x = reinterpret_cast<uint8_t*>(a1) + align16((size_t)(R + 2) * CH * Sp * sizeof(float));
   __shared__ double red[32];
   const int b = blockIdx.y, r0 = blockIdx.x * R;
   const uint8_t* s = fields + (size_t)(idx ? idx[b] : b) * Nt * Ns;
@@ -65,7 +72,7 @@ __global__ void __launch_bounds__(256) k_cnn_fwd(const uint8_t* __restrict__ fie
   __syncthreads();
   for (int e = threadIdx.x; e < (R + 2) * CH * Ns; e += blockDim.x) {
     const int j = e % Ns, o = (e / Ns) % CH, rr = e / (Ns * CH);
-    a1[e] = cnn_a1(w, o, [&](int dt, int dj) { return (int)x[(rr + 1 + dt) * Ns + wrap1(j + dj, Ns)]; });
+    a1[(rr * CH + o) * Sp + j] = cnn_a1(w, o, [&](int dt, int dj) { return (int)x[(rr + 1 + dt) * Ns + wrap1(j + dj, Ns)]; });
   }
   __syncthreads();
   double part = 0.0;
@@ -73,7 +80,7 @@ __global__ void __launch_bounds__(256) k_cnn_fwd(const uint8_t* __restrict__ fie
     const int rr = p / Ns, j = p - rr * Ns;
     if (r0 + rr >= Nt) continue;
     float z[CH];
-    cnn_z2(w, z, [&](int c, int dt, int dj) { return a1[((rr + 1 + dt) * CH + c) * Ns + wrap1(j + dj, Ns)]; });
+    cnn_z2(w, z, [&](int c, int dt, int dj) { return a1[((rr + 1 + dt) * CH + c) * Sp + wrap1(j + dj, Ns)]; });
     float v = w.b3;
 #pragma unroll
     for (int o = 0; o < CH; ++o) v = fmaf(w.w3s[o], tanhf(z[o]), v);
@@ -96,10 +103,11 @@ __global__ void __launch_bounds__(256, 1) k_cnn_bwd(const uint8_t* __restrict__ 
                                                     const double* __restrict__ dF, float* __restrict__ grad) {
   extern __shared__ __align__(16) unsigned char smem[];
   CnnW& w = *reinterpret_cast<CnnW*>(smem);
+  const int Sp = pad_stride(Ns);
   float* a1 = reinterpret_cast<float*>(smem + align16(sizeof(CnnW)));            // rows r0-2 .. r0+R+1
-  float* dz2 = a1 + align16((size_t)(R + 4) * CH * Ns * sizeof(float)) / sizeof(float);  // rows r0-1 .. r0+R
-  float* dz1 = dz2 + align16((size_t)(R + 2) * CH * Ns * sizeof(float)) / sizeof(float);  // rows r0 .. r0+R-1
-  uint8_t* x = reinterpret_cast<uint8_t*>(dz1 + align16((size_t)R * CH * Ns * sizeof(float)) / sizeof(float));
+  float* dz2 = a1 + align16((size_t)(R + 4) * CH * Sp * sizeof(float)) / sizeof(float);  // rows r0-1 .. r0+R
+  float* dz1 = dz2 + align16((size_t)(R + 2) * CH * Sp * sizeof(float)) / sizeof(float);  // rows r0 .. r0+R-1
+  uint8_t* x = reinterpret_cast<uint8_t*>(dz1 + align16((size_t)R * CH * Sp * sizeof(float)) / sizeof(float));
   float* acc = reinterpret_cast<float*>(x + align16((size_t)(R + 6) * Ns));     // 64 floats: S2 (g a2), db2, db1
   load_cnn_weights(w, prm);
   const int tid = threadIdx.x;
@@ -125,19 +133,19 @@ __global__ void __launch_bounds__(256, 1) k_cnn_bwd(const uint8_t* __restrict__ 
     __syncthreads();
     for (int e = tid; e < (R + 4) * CH * Ns; e += blockDim.x) {
       const int j = e % Ns, o = (e / Ns) % CH, rr = e / (Ns * CH);
-      a1[e] = cnn_a1(w, o, [&](int dt, int dj) { return (int)x[(rr + 1 + dt) * Ns + wrap1(j + dj, Ns)]; });
+      a1[(rr * CH + o) * Sp + j] = cnn_a1(w, o, [&](int dt, int dj) { return (int)x[(rr + 1 + dt) * Ns + wrap1(j + dj, Ns)]; });
     }
     __syncthreads();
     for (int p = tid; p < (R + 2) * Ns; p += blockDim.x) {
       const int rr = p / Ns, j = p - rr * Ns;          // t = r0 - 1 + rr
       const bool own = rr >= 1 && rr <= R && r0 + rr - 1 < Nt;
       float z[CH];
-      cnn_z2(w, z, [&](int c, int dt, int dj) { return a1[((rr + 1 + dt) * CH + c) * Ns + wrap1(j + dj, Ns)]; });
+      cnn_z2(w, z, [&](int c, int dt, int dj) { return a1[((rr + 1 + dt) * CH + c) * Sp + wrap1(j + dj, Ns)]; });
 #pragma unroll
       for (int o = 0; o < CH; ++o) {
         const float a = tanhf(z[o]);
         const float d = g * w.w3s[o] * (1.0f - a * a);
-        dz2[(rr * CH + o) * Ns + j] = d;
+        dz2[(rr * CH + o) * Sp + j] = d;
         if (own) {
           s2[o] = fmaf(g, a, s2[o]);
           gb2[o] += d;
@@ -148,11 +156,11 @@ __global__ void __launch_bounds__(256, 1) k_cnn_bwd(const uint8_t* __restrict__ 
     // dW2[o][c][tap] += sum over the tile's positions of dz2[o] a1[c] (shifted)
     for (int rr = 0; rr < R && r0 + rr < Nt; ++rr)
       for (int j = 0; j < Ns; ++j) {
-        const float d = dz2[((rr + 1) * CH + o2) * Ns + j];
+        const float d = dz2[((rr + 1) * CH + o2) * Sp + j];
 #pragma unroll
         for (int tap = 0; tap < 9; ++tap) {
           const int dy = tap / 3, dx = tap % 3;
-          gw2[tap] = fmaf(d, a1[((rr + 1 + dy) * CH + c2) * Ns + wrap1(j + dx - 1, Ns)], gw2[tap]);
+          gw2[tap] = fmaf(d, a1[((rr + 1 + dy) * CH + c2) * Sp + wrap1(j + dx - 1, Ns)], gw2[tap]);
         }
       }
     // da1 at the tile's positions, then dz1 = da1 (1 - a1^2)
@@ -166,7 +174,7 @@ __global__ void __launch_bounds__(256, 1) k_cnn_bwd(const uint8_t* __restrict__ 
 #pragma unroll
         for (int tap = 0; tap < 9; ++tap) {
           const int dy = tap / 3, dx = tap % 3;
-          const float v = dz2[((rr + 2 - dy) * CH + o) * Ns + wrap1(j + 1 - dx, Ns)];
+          const float v = dz2[((rr + 2 - dy) * CH + o) * Sp + wrap1(j + 1 - dx, Ns)];
           const float4* wv = reinterpret_cast<const float4*>(&w.w2b[(o * 9 + tap) * 16]);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
@@ -179,8 +187,8 @@ __global__ void __launch_bounds__(256, 1) k_cnn_bwd(const uint8_t* __restrict__ 
         }
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
-        const float a = a1[((rr + 2) * CH + c) * Ns + j];
-        dz1[(rr * CH + c) * Ns + j] = da[c] * (1.0f - a * a);
+        const float a = a1[((rr + 2) * CH + c) * Sp + j];
+        dz1[(rr * CH + c) * Sp + j] = da[c] * (1.0f - a * a);
       }
     }
     __syncthreads();
@@ -189,7 +197,7 @@ __global__ void __launch_bounds__(256, 1) k_cnn_bwd(const uint8_t* __restrict__ 
       const int dy = tap1 / 3, dx = tap1 % 3;
       for (int rr = 0; rr < R && r0 + rr < Nt; ++rr)
         for (int j = 0; j < Ns; ++j) {
-          const float d = dz1[(rr * CH + o1) * Ns + j];
+          const float d = dz1[(rr * CH + o1) * Sp + j];
           const int v = x[(rr + 2 + dy) * Ns + wrap1(j + dx - 1, Ns)] - 1;
           gw1[0] += v == 0 ? d : 0.0f;
           gw1[1] += v == 1 ? d : 0.0f;
@@ -199,7 +207,7 @@ __global__ void __launch_bounds__(256, 1) k_cnn_bwd(const uint8_t* __restrict__ 
     } else if (tid < 160) {
       const int o = tid - 144;
       for (int rr = 0; rr < R && r0 + rr < Nt; ++rr)
-        for (int j = 0; j < Ns; ++j) gb1 += dz1[(rr * CH + o) * Ns + j];
+        for (int j = 0; j < Ns; ++j) gb1 += dz1[(rr * CH + o) * Sp + j];
     }
   }
   // flush the partials
