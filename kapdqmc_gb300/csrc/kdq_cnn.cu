@@ -1,7 +1,8 @@
 // Training and inference kernels of the self-learning effective model
 // (kdq_cnn.cuh) and their handle-free C entry points.
 //
-// A work item is one tile of R slices (rows) of one configuration.  The
+// A work item is one tile of R slices (rows) of one configuration (R picked
+// per lattice and batch by timing, see autotune).  The
 // forward kernel stages the tile's field window and layer-1 activations in
 // shared memory and adds its share of F to the configuration's total.  The
 // backward kernel is persistent (one CTA per SM): it recomputes the
@@ -11,7 +12,10 @@
 // atomic add per parameter per CTA.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <numeric>
+#include <tuple>
 #include <random>
 #include <string>
 #include <vector>
@@ -344,6 +348,67 @@ struct Net {
   }
 };
 
+// Tile autotuner: the slices per work item (R) of the forward and of the
+// backward kernel are timed on the first batch for every R that fits the
+// shared memory, and the fastest pair is kept per (Nt, Ns, batch, device).
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, std::pair<int, int>> g_tuned;
+
+template <class F>
+float time_ms(cudaStream_t st, F&& launch) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  launch();   // warm-up
+  cudaEventRecord(a, st);
+  for (int q = 0; q < 3; ++q) launch();
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms;
+}
+
+int autotune(Net& n, const uint8_t* f, const int* idx, int B, const __nv_bfloat16* pb, double* F, double* dF,
+             float* g, int device) {
+  const auto key = std::make_tuple(n.Nt, n.Ns, B, device);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      n.Rf = it->second.first;
+      n.Rb = it->second.second;
+      return KDQ_OK;
+    }
+  }
+  const int rf0 = n.Rf, rb0 = n.Rb;   // the largest feasible heights (shared memory opened to these)
+  std::vector<double> ones(B, 1.0 / B);
+  CNN_CUDA(cudaMemcpy(dF, ones.data(), B * sizeof(double), cudaMemcpyHostToDevice));
+  float best_f = 1e30f, best_b = 1e30f;
+  int rf = rf0, rb = rb0;
+  for (int R : {4, 2, 1}) {
+    if (R <= rf0) {
+      n.Rf = R;
+      const float t = time_ms(n.st, [&] { n.fwd(f, idx, B, pb, F); });
+      if (t < best_f) { best_f = t; rf = R; }
+    }
+    if (R <= rb0) {
+      n.Rb = R;
+      const float t = time_ms(n.st, [&] { n.bwd(f, idx, B, pb, dF, g); });
+      if (t < best_b) { best_b = t; rb = R; }
+    }
+  }
+  CNN_CUDA(cudaGetLastError());
+  CNN_CUDA(cudaMemset(g, 0, KDQ_CNN_NPARAM * sizeof(float)));
+  n.Rf = rf;
+  n.Rb = rb;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[key] = {rf, rb};
+  return KDQ_OK;
+}
+
 int net_setup(Net& n, int Nt, int Ns, int device) {
   n.Nt = Nt;
   n.Ns = Ns;
@@ -435,6 +500,9 @@ extern "C" int kdq_cnn_train(const uint8_t* fields, const double* target, int32_
   CNN_CUDA(cudaMemset(dloss.p, 0, std::max(epochs, 1) * sizeof(double)));
   k_to_bf16<<<4, 1024>>>(dp.as<float>(), dpb.as<__nv_bfloat16>(), KDQ_CNN_NPARAM);
   CNN_CUDA(cudaGetLastError());
+  if (int rc = autotune(n, dfld.as<uint8_t>(), nullptr, batch, dpb.as<__nv_bfloat16>(), dF.as<double>(),
+                        ddF.as<double>(), dg.as<float>(), device))
+    return rc;
   std::vector<int> perm(n_cfg);
   std::iota(perm.begin(), perm.end(), 0);
   std::mt19937_64 rng(seed);
