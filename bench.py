@@ -26,6 +26,7 @@ import math
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -362,8 +363,9 @@ def run_gpu(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clk_path = str(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv") if (ROOT / "gpurun_out").is_dir() \
-        else f"/tmp/kdq_clocks_{os.getpid()}.csv"
+    clk_dir = os.environ.get("KDQ_CLOCKS_DIR")   # keep the raw clock samples there when set
+    clk_path = os.path.join(clk_dir, f"clocks_rank{rank}.csv") if clk_dir else \
+        os.path.join(tempfile.gettempdir(), f"kdq_clocks_{os.getpid()}.csv")
     cproc, cfile = clocks_start(clk_path)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
