@@ -140,3 +140,29 @@ def test_trained_model_predicts_local_moves_better_than_none():
     mse_trained = float(np.mean((exact - pred) ** 2))
     mse_none = float(np.mean(exact ** 2))
     assert mse_trained < 0.9 * mse_none, (mse_trained, mse_none)
+
+
+def test_cluster_moves_in_mixed_precision():
+    # FP32 working precision: the cluster moves' rank-|S| update runs in FP32
+    # like the local ones; the FP64 recompute bounds the drift and the carried
+    # log|det| still matches a chain rebuilt (in FP64) from the final fields
+    m = cases.tu_honeycomb()
+    nch = 4
+    fields = np.stack([Initial_s(m, 500 + c) for c in range(nch)])
+    with Sweeper(m, nch) as sw:
+        sw.set_precision("mixed")
+        sw.set_fields(fields)
+        sw.set_rng(12)
+        sw.slmc_enable(slmc.init_params(3) * 0.05, 1, 6, 16)
+        sw.phy_update(2, False)
+        st = sw.slmc_stats()
+        drift = sw.drift(2)
+        ld, _ = sw.log_det()
+        s1 = sw.get_fields()
+    assert st["accepted"] > 0
+    assert drift.max() < 1e-3
+    with Sweeper(m, nch) as sw2:
+        sw2.set_fields(s1)
+        sw2.init()
+        ld2, _ = sw2.log_det()
+    assert np.all(np.abs(ld - ld2) < 1e-3 * np.maximum(1.0, np.abs(ld2)))
