@@ -36,3 +36,9 @@ def test_create_rejects_bad_model_without_gpu_work():
     rc = lib.kdq_create(ctypes.byref(h), ctypes.byref(d), 1, 0)
     assert rc == _lib.KDQ_ERR_ARG
     assert b"kind" in lib.kdq_last_error(None)
+
+
+def test_every_entry_point_is_mapped_in_the_integration_guide():
+    guide = (HEADER.parent.parent / "INTEGRATION.md").read_text()
+    missing = [n for n in declared() if f"`{n}`" not in guide and n not in guide]
+    assert not missing, missing
