@@ -51,6 +51,12 @@ def reference_tau_int():
         return None
 
 
+def _tu_4x4():
+    from kapdqmc_gb300 import tU_Hubbard_Para
+    return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Δt=0.1, Θrelax=5.0, Θquench=0.0,
+                           Lattice="SQUARE45", site=[2, 4], BatchSize=10, Initial="H0")
+
+
 def _tv_6x6():
     from kapdqmc_gb300 import tV_Hubbard_Para
     return tV_Hubbard_Para(Ht=1.0, Hv1=1.0, Hv2=1.0, Δt=0.05, Θrelax=10.0, Θquench=0.0,
@@ -78,6 +84,10 @@ def _tu_hc_9x9():
 # The bench line is c2 (the metric's configuration: batched plain FP64 sweep);
 # the others are the remaining single-GPU configurations, for `--workload`.
 WORKLOADS = {
+    "c1": dict(make=_tu_4x4, chains=1, Ns=16, Nt=100, n_wrap=10,
+               desc="t-U 4x4 square (N=16), 100 slices, n_wrap=10, U/t=4, dt=0.1, one chain, "
+                    "energy + double occupancy per sweep",
+               model="tU_Hubbard_Para(SQUARE45, site=[2,4])"),
     "c2": dict(make=_tv_6x6, chains=256, Ns=72, Nt=400, n_wrap=10,
                desc="t-V 6x6 honeycomb (N=72), 400 slices, n_wrap=10, V/t=1, dt=0.05, 256 independent "
                     "chains, energy + density structure factor per sweep",
