@@ -82,3 +82,29 @@ def tv_honeycomb60():
 def tuv_honeycomb60():
     return tUV_Hubbard_Para(Ht=1.0, Hu=4.0, Hv=0.5, Lattice="HoneyComb60", site=[3, 3], Δt=0.1, Θ=1.0,
                             BatchSize=5, Initial="H0")
+
+
+# Lattices small enough for the exact Fock-space sum (Ns <= 12)
+def tu_hc8(U=4.0):
+    return tU_Hubbard_Para(Ht=1.0, Hu1=U, Hu2=U, Δt=0.1, Θrelax=1.0, Θquench=0.0,
+                           Lattice="HoneyComb120", site=[2, 2], BatchSize=5, Initial="H0")
+
+
+def tu_hc8_quench():
+    return tU_Hubbard_Para(Ht=1.0, Hu1=0.0, Hu2=3.8, Θrelax=0.4, Θquench=0.4, Lattice="HoneyComb120",
+                           site=[2, 2], Δt=0.1, BatchSize=4, Initial="H0")
+
+
+def tu_sq8():
+    return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Θrelax=1.0, Θquench=0.0, Lattice="SQUARE45",
+                           site=[2, 2], Δt=0.1, BatchSize=5, Initial="H0")
+
+
+def tu_sq8_flux():
+    return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Θrelax=1.0, Θquench=0.0, Lattice="SQUARE90",
+                           site=[2, 2], Δt=0.1, BatchSize=5, Initial="H0", flux=3.141592653589793)
+
+
+def tu_hc12():
+    return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Θrelax=1.0, Θquench=0.0, Lattice="HoneyComb120",
+                           site=[2, 3], Δt=0.1, BatchSize=5, Initial="H0")

@@ -1,0 +1,72 @@
+"""Write the golden fixtures of the sweep (``sweep_*.json``) from the CPU oracle.
+
+The reference ships no stored outputs (its tests run sweeps without
+assertions), so these fixtures pin the oracle's own results on small models:
+the initial fields, the Philox proposal stream (seed, chain 0), the
+accept/reject sequence, the final fields, every measurement row, the final
+Green's function and log|det(BL BR)|.  The CPU tests check that the oracle
+still reproduces them; the GPU tests check the CUDA sweep against them
+without running the oracle.
+
+    python tests/golden/make_golden.py          # rewrites tests/golden/sweep_*.json
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+for p in (ROOT, ROOT / "oracle", HERE.parent):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+import cases                     # noqa: E402
+import dqmc_oracle as O          # noqa: E402
+import philox                    # noqa: E402
+from kapdqmc_gb300 import Initial_s   # noqa: E402
+
+CASES = ["tu_square", "tu_honeycomb", "tu_quench", "tu_square90_flux", "tu_honeycomb60",
+         "tv_honeycomb", "tv_honeycomb60", "tuv_honeycomb", "tuv_square", "tuv_honeycomb60"]
+SEED = 1234
+FIELD_SEED = 100
+SWEEPS = 2
+
+
+def make(case: str) -> dict:
+    model = getattr(cases, case)()
+    s = Initial_s(model, FIELD_SEED)
+    n = O.proposals_per_sweep(model)
+    ks, us = zip(*(philox.tape(SEED, 0, w, n) for w in range(SWEEPS)))
+    sw = O.phy_update(model, s, SWEEPS, O.Tape(np.concatenate(ks), np.concatenate(us)), True)
+    G = np.asarray(sw.G)
+    acc = np.packbits(np.array(sw.accepts, dtype=bool)).tobytes().hex()
+    return {
+        "case": case, "seed": SEED, "chain": 0, "sweeps": SWEEPS, "field_seed": FIELD_SEED,
+        "proposals": n * SWEEPS,
+        "s": np.ravel(s, order="F").tolist(),
+        "s_out": np.ravel(sw.s, order="F").tolist(),
+        "n_accept": int(sum(sw.accepts)),
+        "accepts_hex": acc,
+        "obs": np.array(sw.obs_rows).tolist(),
+        "G_re": np.ravel(G.real, order="F").tolist(),
+        "G_im": np.ravel(G.imag, order="F").tolist() if np.iscomplexobj(G) else None,
+        "log_det": O.log_det(model, sw.s)[0],
+        "log_weight": O.log_weight(model, sw.s),
+    }
+
+
+def main() -> None:
+    for case in CASES:
+        spec = make(case)
+        path = HERE / f"sweep_{case}.json"
+        path.write_text(json.dumps(spec, separators=(",", ":")) + "\n")
+        print(f"{path.name}: {spec['proposals']} proposals, {spec['n_accept']} accepted, "
+              f"{path.stat().st_size} bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -88,22 +88,32 @@ def test_grover_identity():
 
 
 def _golden_cases():
-    return sorted(GOLDEN.glob("*.json"))
+    return sorted(GOLDEN.glob("sweep_*.json"))
+
+
+def test_golden_fixtures_present():
+    # tests/golden/make_golden.py writes one fixture per small model
+    assert len(_golden_cases()) >= 10
 
 
 @pytest.mark.parametrize("path", _golden_cases(), ids=lambda p: p.stem)
 def test_golden_fixture(path):
-    import importlib
     spec = json.loads(path.read_text())
     model = getattr(cases, spec["case"])()
     fields = np.array(spec["s"], dtype=np.uint8).reshape(model.field_shape, order="F")
     n = O.proposals_per_sweep(model)
-    ks, us = zip(*(philox.tape(spec["seed"], 0, w, n) for w in range(spec["sweeps"])))
+    assert n * spec["sweeps"] == spec["proposals"]
+    ks, us = zip(*(philox.tape(spec["seed"], spec["chain"], w, n) for w in range(spec["sweeps"])))
     sw = O.phy_update(model, fields, spec["sweeps"], O.Tape(np.concatenate(ks), np.concatenate(us)), True)
+    acc = np.unpackbits(np.frombuffer(bytes.fromhex(spec["accepts_hex"]), np.uint8))[: spec["proposals"]]
+    np.testing.assert_array_equal(np.array(sw.accepts, dtype=bool), acc.astype(bool))
     assert np.ravel(sw.s, order="F").tolist() == spec["s_out"]
     assert sum(sw.accepts) == spec["n_accept"]
     np.testing.assert_allclose(np.array(sw.obs_rows), np.array(spec["obs"]), rtol=1e-9, atol=1e-12)
-    importlib.invalidate_caches()
+    G = np.array(spec["G_re"]) + (1j * np.array(spec["G_im"]) if spec["G_im"] is not None else 0)
+    G = G.reshape(model.Ns, model.Ns, order="F")
+    assert np.linalg.norm(sw.G - G) / np.linalg.norm(G) < 1e-12
+    assert abs(O.log_det(model, sw.s)[0] - spec["log_det"]) < 1e-10 * max(1.0, abs(spec["log_det"]))
 
 
 def test_c_restatement_matches_numpy_oracle():
