@@ -252,6 +252,37 @@ int kdq_set_graphs(kdq_handle* h, int32_t enable);
 /* CUDA stream (cudaStream_t) of the handle, for event timing by callers. */
 void* kdq_stream(kdq_handle* h);
 
+/* Register-tile class of the sweep kernel: rows = 1, 3 or 6 row groups of
+ * 32 sites, at least ceil(Ns / 32) (the default is the smallest class that
+ * fits).  Every class computes the same arithmetic in the same order, so the
+ * choice changes speed only.  kdq_get_tiles returns the current class.
+ * kdq_autotune times one sweep of the handle's own chains per valid class,
+ * keeps the fastest, puts the fields and each chain's random-stream position
+ * back and leaves the handle as kdq_init does; ms[0..2] receive the sweep
+ * times of classes 1, 3, 6 (-1 where a class does not fit).  Choices are
+ * cached per device, model, size, precision and batch for the process.  No
+ * counterpart in the reference (which calls BLAS). */
+int kdq_set_tiles(kdq_handle* h, int32_t rows);
+int kdq_get_tiles(const kdq_handle* h);
+int kdq_autotune(kdq_handle* h, int32_t* chosen, double* ms, int32_t len);
+
+/* Groups: handles of different lattices, models or precisions on one device
+ * swept together.  kdq_group_sweep runs `sweeps` sweeps of every handle of
+ * the group (each initialised by kdq_init) as one CUDA graph per sweep whose
+ * parallel branches are the handles' block launches; results are those of
+ * kdq_sweep on each handle alone (same kernels, same random streams).
+ * kdq_group_synchronize waits and checks every handle's error flags;
+ * kdq_get_obs and the other per-handle calls read the results.  A handle
+ * may belong to several groups but must not be used from another thread
+ * during a group call.  Reference counterpart: none (the reference runs one
+ * model per Julia call, src/tU/phy_update.jl:3). */
+typedef struct kdq_group kdq_group;
+int kdq_group_create(kdq_group** out, kdq_handle* const* handles, int32_t n);
+int kdq_group_sweep(kdq_group* g, int32_t sweeps, int32_t record);
+int kdq_group_synchronize(kdq_group* g);
+const char* kdq_group_last_error(const kdq_group* g);
+void kdq_group_destroy(kdq_group* g);
+
 /* ---------------------------------------------------------------------
  * Self-learning Monte Carlo (t-U).  No counterpart in the reference, which
  * has local updates only (src/tU/phy_update.jl:256-267).

@@ -50,6 +50,14 @@ _SIGS = {
                                 C.c_float, C.c_uint64, C.c_void_p, C.c_void_p, C.c_int32]),
     "kdq_stream": (C.c_void_p, [C.c_void_p]),
     "kdq_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kdq_set_tiles": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kdq_get_tiles": (C.c_int, [C.c_void_p]),
+    "kdq_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
+    "kdq_group_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_int32]),
+    "kdq_group_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "kdq_group_synchronize": (C.c_int, [C.c_void_p]),
+    "kdq_group_last_error": (C.c_char_p, [C.c_void_p]),
+    "kdq_group_destroy": (None, [C.c_void_p]),
     "kdq_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
     "kdq_enable_phase_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "kdq_get_phase_cycles": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -22,6 +22,25 @@ namespace {
 std::mutex g_err_mu;
 std::string g_create_err;
 
+// tile classes chosen by kdq_autotune, per device, model, size, precision
+// and batch (process-wide, so later handles of the same shape reuse them)
+struct TuneKey {
+  int device, kind, Ns, Nt;
+  bool gc, kc;
+  int precision, nchains, slmc;
+  bool operator==(const TuneKey& o) const {
+    return device == o.device && kind == o.kind && Ns == o.Ns && Nt == o.Nt && gc == o.gc && kc == o.kc &&
+           precision == o.precision && nchains == o.nchains && slmc == o.slmc;
+  }
+};
+struct TuneEntry {
+  TuneKey key;
+  int rows;
+  double ms[3];
+};
+std::mutex g_tune_mu;
+std::vector<TuneEntry> g_tune;
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -601,8 +620,13 @@ int kdq_init(kdq_handle* h) {
   return KDQ_OK;
 }
 
-int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
-  if (!h) return KDQ_ERR_ARG;
+}  // extern "C"
+
+namespace {
+
+// Everything a sweep call does before its launches: argument and tape
+// checks, per-call counters, the drift log and the observable rows.
+int sweep_prepare(kdq_handle* h, int32_t sweeps, int32_t record) {
   if (sweeps < 0) return fail(h, KDQ_ERR_ARG, "sweeps must be >= 0");
   if (record < 0 || record > 2) return fail(h, KDQ_ERR_ARG, "record must be 0, 1 or 2");
   if (!h->initialised) return fail(h, KDQ_ERR_STATE, "kdq_init must precede kdq_sweep");
@@ -664,6 +688,25 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
     h->P.mstack_max = fmax;
   }
   h->P.record = record;
+  return KDQ_OK;
+}
+
+// The 2 (NN-1) block launches of one sweep on the handle's stream.
+cudaError_t sweep_launches(kdq_handle* h) {
+  cudaError_t ce = cudaSuccess;
+  for (int k = 1; k <= h->NN - 1 && ce == cudaSuccess; ++k) ce = launch(h, KDQ_MODE_FWD, k);
+  for (int k = h->NN - 1; k >= 1 && ce == cudaSuccess; --k) ce = launch(h, KDQ_MODE_BWD, k);
+  return ce;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
+  if (!h) return KDQ_ERR_ARG;
+  int rc = sweep_prepare(h, sweeps, record);
+  if (rc) return rc;
   auto t0 = std::chrono::steady_clock::now();
   if (h->use_graphs && sweeps > 0) {
     if (!h->graph || std::memcmp(&h->graph_P, &h->P, sizeof(SweepParams)) != 0) {
@@ -673,9 +716,7 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
       }
       cudaGraph_t g = nullptr;
       KDQ_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-      cudaError_t ce = cudaSuccess;
-      for (int k = 1; k <= h->NN - 1 && ce == cudaSuccess; ++k) ce = launch(h, KDQ_MODE_FWD, k);
-      for (int k = h->NN - 1; k >= 1 && ce == cudaSuccess; --k) ce = launch(h, KDQ_MODE_BWD, k);
+      cudaError_t ce = sweep_launches(h);
       cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
       if (ce != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -689,10 +730,7 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record) {
     }
     for (int w = 0; w < sweeps; ++w) KDQ_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
   } else {
-    for (int w = 0; w < sweeps; ++w) {
-      for (int k = 1; k <= h->NN - 1; ++k) KDQ_CUDA(h, launch(h, KDQ_MODE_FWD, k));
-      for (int k = h->NN - 1; k >= 1; --k) KDQ_CUDA(h, launch(h, KDQ_MODE_BWD, k));
-    }
+    for (int w = 0; w < sweeps; ++w) KDQ_CUDA(h, sweep_launches(h));
   }
   if (record) h->obs_rows += sweeps;
   h->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1218,6 +1256,264 @@ int kdq_grover_det_chains(kdq_handle* h, const int32_t* index, int32_t nA, doubl
                                  h->gr_piv.as<int>(), h->gr_det.as<double>(), h->stream));
   KDQ_CUDA(h, cudaMemcpyAsync(det, h->gr_det.p, (size_t)2 * npairs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+  return KDQ_OK;
+}
+
+// ------------------------------------------------------------ tile classes
+int kdq_set_tiles(kdq_handle* h, int32_t rows) {
+  if (!h) return KDQ_ERR_ARG;
+  if (rows != 1 && rows != 3 && rows != 6) return fail(h, KDQ_ERR_ARG, "tile class must be 1, 3 or 6");
+  if (32 * rows < h->Ns)
+    return fail(h, KDQ_ERR_ARG, "tile class " + std::to_string(rows) + " covers at most " +
+                                    std::to_string(32 * rows) + " sites");
+  if (rows != h->maxrm) {
+    KDQ_CUDA(h, cudaSetDevice(h->device));
+    KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->maxrm = rows;
+    if (h->graph) {   // the captured sweep launches the old instantiation
+      KDQ_CUDA(h, cudaGraphExecDestroy(h->graph));
+      h->graph = nullptr;
+    }
+  }
+  return KDQ_OK;
+}
+
+int kdq_get_tiles(const kdq_handle* h) { return h ? h->maxrm : 0; }
+
+int kdq_autotune(kdq_handle* h, int32_t* chosen, double* ms, int32_t len) {
+  if (!h) return KDQ_ERR_ARG;
+  static const int cand[3] = {1, 3, 6};
+  const TuneKey key{h->device, h->kind, h->Ns, h->Nt, h->gc, h->kc, h->precision, h->nchains, h->P.slmc_moves};
+  double t[3] = {-1.0, -1.0, -1.0};
+  int best = -1;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto& e : g_tune)
+      if (e.key == key) {
+        best = e.rows;
+        for (int i = 0; i < 3; ++i) t[i] = e.ms[i];
+      }
+  }
+  KDQ_CUDA(h, cudaSetDevice(h->device));
+  if (best < 0) {
+    // time one sweep per valid class on the handle's own chains, then put
+    // the fields and the per-chain counters (RNG position) back
+    KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    const size_t fbytes = (size_t)h->nchains * h->Nt * h->n_field;
+    const size_t cbytes = (size_t)h->nchains * sizeof(ChainCtl);
+    DevBuf s0, c0;
+    KDQ_CUDA(h, s0.alloc(fbytes));
+    KDQ_CUDA(h, c0.alloc(cbytes));
+    KDQ_CUDA(h, cudaMemcpyAsync(s0.p, h->s.p, fbytes, cudaMemcpyDeviceToDevice, h->stream));
+    KDQ_CUDA(h, cudaMemcpyAsync(c0.p, h->ctl.p, cbytes, cudaMemcpyDeviceToDevice, h->stream));
+    const int keep = h->maxrm;
+    cudaEvent_t e0, e1;
+    KDQ_CUDA(h, cudaEventCreate(&e0));
+    KDQ_CUDA(h, cudaEventCreate(&e1));
+    int rc = KDQ_OK;
+    for (int i = 0; i < 3 && rc == KDQ_OK; ++i) {
+      if (32 * cand[i] < h->Ns) continue;
+      if ((rc = kdq_set_tiles(h, cand[i])) != KDQ_OK) break;
+      if ((rc = kdq_init(h)) != KDQ_OK) break;
+      if ((rc = kdq_sweep(h, 1, 0)) != KDQ_OK) break;    // captures the graph
+      cudaError_t e = cudaEventRecord(e0, h->stream);
+      if (e == cudaSuccess && (rc = kdq_sweep(h, 1, 0)) != KDQ_OK) break;
+      if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float f = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&f, e0, e1);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h->s.p, s0.p, fbytes, cudaMemcpyDeviceToDevice, h->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h->ctl.p, c0.p, cbytes, cudaMemcpyDeviceToDevice, h->stream);
+      if (e != cudaSuccess) {
+        rc = cuda_fail(h, e, "autotune");
+        break;
+      }
+      if ((rc = kdq_synchronize(h)) != KDQ_OK) break;
+      t[i] = f;
+      if (best < 0 || f < t[best]) best = i;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != KDQ_OK) {
+      kdq_set_tiles(h, keep);
+      return rc;
+    }
+    best = cand[best];
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.push_back({key, best, {t[0], t[1], t[2]}});
+  }
+  int rc = kdq_set_tiles(h, best);
+  if (rc) return rc;
+  if (chosen) *chosen = best;
+  for (int i = 0; ms && i < len && i < 3; ++i) ms[i] = t[i];
+  return kdq_init(h);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ groups
+namespace kdq {
+void set_global_error(const std::string& msg);
+}
+
+// Handles of different lattices, models or precisions swept together: one
+// CUDA graph per sweep whose branches are the handles' block launches, so
+// their CTAs share the GPU in one submission.
+struct kdq_group {
+  int device = 0;
+  std::vector<kdq_handle*> hs;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  std::vector<cudaEvent_t> ready, joins;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<SweepParams> graph_P;
+  std::vector<int> graph_rm, graph_prec;
+  std::string err;
+  ~kdq_group() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (auto e : ready) cudaEventDestroy(e);
+    for (auto e : joins) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (done) cudaEventDestroy(done);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+int gfail(kdq_group* g, int code, const std::string& msg) {
+  if (g) g->err = msg;
+  return code;
+}
+#define KDQ_GCUDA(g, call)                                                          \
+  do {                                                                              \
+    cudaError_t _e = (call);                                                        \
+    if (_e != cudaSuccess) return gfail(g, KDQ_ERR_CUDA, std::string(#call) + ": " + \
+                                              cudaGetErrorString(_e));              \
+  } while (0)
+}  // namespace
+
+extern "C" {
+
+int kdq_group_create(kdq_group** out, kdq_handle* const* handles, int32_t n) {
+  if (!out || !handles || n < 1) {
+    kdq::set_global_error("kdq_group_create: NULL argument or empty group");
+    return KDQ_ERR_ARG;
+  }
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!handles[i]) {
+      kdq::set_global_error("kdq_group_create: NULL handle");
+      return KDQ_ERR_ARG;
+    }
+    for (int j = 0; j < i; ++j)
+      if (handles[j] == handles[i]) {
+        kdq::set_global_error("kdq_group_create: a handle appears twice");
+        return KDQ_ERR_ARG;
+      }
+    if (handles[i]->device != handles[0]->device) {
+      kdq::set_global_error("kdq_group_create: handles on different devices");
+      return KDQ_ERR_ARG;
+    }
+  }
+  auto* g = new kdq_group;
+  g->device = handles[0]->device;
+  g->hs.assign(handles, handles + n);
+  auto bad = [&](cudaError_t e) {
+    kdq::set_global_error(std::string("kdq_group_create: ") + cudaGetErrorString(e));
+    delete g;
+    return KDQ_ERR_CUDA;
+  };
+  cudaError_t e = cudaSetDevice(g->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming);
+  g->ready.assign(n, nullptr);
+  g->joins.assign(n, nullptr);
+  for (int i = 0; i < n && e == cudaSuccess; ++i) {
+    e = cudaEventCreateWithFlags(&g->ready[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->joins[i], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) return bad(e);
+  *out = g;
+  return KDQ_OK;
+}
+
+const char* kdq_group_last_error(const kdq_group* g) { return g ? g->err.c_str() : "NULL group"; }
+
+void kdq_group_destroy(kdq_group* g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  cudaStreamSynchronize(g->stream);
+  delete g;
+}
+
+int kdq_group_sweep(kdq_group* g, int32_t sweeps, int32_t record) {
+  if (!g) return KDQ_ERR_ARG;
+  KDQ_GCUDA(g, cudaSetDevice(g->device));
+  const int n = (int)g->hs.size();
+  for (int i = 0; i < n; ++i) {
+    kdq_handle* h = g->hs[i];
+    if (!h->initialised) return gfail(g, KDQ_ERR_STATE, "handle " + std::to_string(i) + ": kdq_init must precede the group sweep");
+    if (int rc = sweep_prepare(h, sweeps, record)) return gfail(g, rc, "handle " + std::to_string(i) + ": " + h->err);
+    KDQ_GCUDA(g, cudaEventRecord(g->ready[i], h->stream));
+    KDQ_GCUDA(g, cudaStreamWaitEvent(g->stream, g->ready[i], 0));
+  }
+  bool same = g->graph != nullptr;
+  for (int i = 0; same && i < n; ++i)
+    same = std::memcmp(&g->graph_P[i], &g->hs[i]->P, sizeof(SweepParams)) == 0 &&
+           g->graph_rm[i] == g->hs[i]->maxrm && g->graph_prec[i] == g->hs[i]->precision;
+  if (sweeps > 0 && !same) {
+    if (g->graph) {
+      KDQ_GCUDA(g, cudaGraphExecDestroy(g->graph));
+      g->graph = nullptr;
+    }
+    cudaGraph_t gr = nullptr;
+    KDQ_GCUDA(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaEventRecord(g->fork, g->stream);
+    for (int i = 0; i < n && ce == cudaSuccess; ++i) {
+      kdq_handle* h = g->hs[i];
+      ce = cudaStreamWaitEvent(h->stream, g->fork, 0);     // the branch joins the capture
+      if (ce == cudaSuccess) ce = sweep_launches(h);
+      if (ce == cudaSuccess) ce = cudaEventRecord(g->joins[i], h->stream);
+      if (ce == cudaSuccess) ce = cudaStreamWaitEvent(g->stream, g->joins[i], 0);
+    }
+    cudaError_t ee = cudaStreamEndCapture(g->stream, &gr);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+      if (gr) cudaGraphDestroy(gr);
+      return gfail(g, KDQ_ERR_CUDA, std::string("group sweep capture: ") +
+                                        cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+    }
+    cudaError_t ie = cudaGraphInstantiate(&g->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    KDQ_GCUDA(g, ie);
+    g->graph_P.resize(n);
+    g->graph_rm.resize(n);
+    g->graph_prec.resize(n);
+    for (int i = 0; i < n; ++i) {
+      g->graph_P[i] = g->hs[i]->P;
+      g->graph_rm[i] = g->hs[i]->maxrm;
+      g->graph_prec[i] = g->hs[i]->precision;
+    }
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  for (int w = 0; w < sweeps; ++w) KDQ_GCUDA(g, cudaGraphLaunch(g->graph, g->stream));
+  // later work on each handle's own stream runs after the group's sweeps
+  KDQ_GCUDA(g, cudaEventRecord(g->done, g->stream));
+  for (int i = 0; i < n; ++i) {
+    kdq_handle* h = g->hs[i];
+    KDQ_GCUDA(g, cudaStreamWaitEvent(h->stream, g->done, 0));
+    if (record) h->obs_rows += sweeps;
+    h->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return KDQ_OK;
+}
+
+int kdq_group_synchronize(kdq_group* g) {
+  if (!g) return KDQ_ERR_ARG;
+  KDQ_GCUDA(g, cudaSetDevice(g->device));
+  KDQ_GCUDA(g, cudaStreamSynchronize(g->stream));
+  for (size_t i = 0; i < g->hs.size(); ++i)
+    if (int rc = kdq_synchronize(g->hs[i])) return gfail(g, rc, "handle " + std::to_string(i) + ": " + g->hs[i]->err);
   return KDQ_OK;
 }
 

@@ -188,6 +188,22 @@ class Sweeper:
         self._ck(self.lib.kdq_set_graphs(self.h, int(bool(enable))))
 
     @property
+    def set_tiles(self, rows: int):
+        """Register-tile class of the sweep kernel (1, 3 or 6 row groups of 32 sites)."""
+        self._ck(self.lib.kdq_set_tiles(self.h, int(rows)))
+
+    @property
+    def tiles(self) -> int:
+        return self.lib.kdq_get_tiles(self.h)
+
+    def autotune(self):
+        """Time one sweep per valid tile class, keep the fastest, restore the
+        fields and random-stream positions; returns (class, {class: ms})."""
+        chosen = C.c_int32()
+        ms = np.empty(3)
+        self._ck(self.lib.kdq_autotune(self.h, C.byref(chosen), ms.ctypes.data, 3))
+        return chosen.value, {r: float(t) for r, t in zip((1, 3, 6), ms) if t >= 0}
+
     def stream(self) -> int:
         return self.lib.kdq_stream(self.h) or 0
 
@@ -526,3 +542,56 @@ def phy_update(path, model, s, Sweeps: int, record: bool = False, *, seed=None, 
             _append_csv(_csv_name(path, model), obs.mean(axis=0)[..., :6 if model.kind == KIND_TU else None])
         return out, obs
     return out
+
+
+class SweeperGroup:
+    """Sweepers of different lattices, models or precisions on one GPU, swept
+    together as one CUDA graph per sweep (``kdq_group_sweep``).  Each
+    sweeper's results equal those of sweeping it alone."""
+
+    def __init__(self, sweepers):
+        self.lib = _lib.load()
+        self.sweepers = list(sweepers)
+        arr = (C.c_void_p * len(self.sweepers))(*[s.h.value for s in self.sweepers])
+        g = C.c_void_p()
+        _lib.check(self.lib.kdq_group_create(C.byref(g), arr, len(self.sweepers)), None)
+        self.g = g
+
+    def close(self):
+        if getattr(self, "g", None):
+            self.lib.kdq_group_destroy(self.g)
+            self.g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _ck(self, rc):
+        if rc != _lib.KDQ_OK:
+            msg = self.lib.kdq_group_last_error(self.g)
+            raise _lib.KdqError(rc, msg.decode() if msg else "")
+
+    def sweep(self, sweeps: int, record=False):
+        self._ck(self.lib.kdq_group_sweep(self.g, int(sweeps), int(record)))
+
+    def synchronize(self):
+        self._ck(self.lib.kdq_group_synchronize(self.g))
+
+    def phy_update(self, sweeps: int, record=False):
+        """Init every sweeper from its fields, sweep all together; returns one
+        obs array (nchains, sweeps, n_obs) per sweeper, or None."""
+        for s in self.sweepers:
+            s.init()
+        self.sweep(sweeps, record)
+        self.synchronize()
+        if not record:
+            return None
+        return [s.get_obs(sweeps) for s in self.sweepers]

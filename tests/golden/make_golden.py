@@ -36,12 +36,41 @@ FIELD_SEED = 100
 SWEEPS = 2
 
 
+def _sensitivity(model, s, tape_k, tape_u, base) -> float:
+    """Largest relative change of the measurement rows when G is perturbed by
+    1e-15 relative noise before every measurement: how strongly the wraps to
+    tau = Nt/2 amplify rounding for these fields."""
+    cls = O._SWEEPS[model.kind]
+    orig = cls.measure
+    rng = np.random.default_rng(0)
+
+    def noisy(self, lt):
+        G = self.G
+        self.G = G * (1 + 1e-15 * rng.standard_normal(G.shape))
+        try:
+            return orig(self, lt)
+        finally:
+            self.G = G
+
+    cls.measure = noisy
+    try:
+        worst = 0.0
+        for _ in range(3):
+            o = np.array(O.phy_update(model, s, SWEEPS, O.Tape(tape_k, tape_u), True).obs_rows)
+            worst = max(worst, float(np.abs(o - base).max() / max(1.0, np.abs(base).max())))
+    finally:
+        cls.measure = orig
+    return worst
+
+
 def make(case: str) -> dict:
     model = getattr(cases, case)()
     s = Initial_s(model, FIELD_SEED)
     n = O.proposals_per_sweep(model)
     ks, us = zip(*(philox.tape(SEED, 0, w, n) for w in range(SWEEPS)))
-    sw = O.phy_update(model, s, SWEEPS, O.Tape(np.concatenate(ks), np.concatenate(us)), True)
+    tape_k, tape_u = np.concatenate(ks), np.concatenate(us)
+    sw = O.phy_update(model, s, SWEEPS, O.Tape(tape_k, tape_u), True)
+    sens = _sensitivity(model, s, tape_k, tape_u, np.array(sw.obs_rows))
     G = np.asarray(sw.G)
     acc = np.packbits(np.array(sw.accepts, dtype=bool)).tobytes().hex()
     return {
@@ -52,6 +81,10 @@ def make(case: str) -> dict:
         "n_accept": int(sum(sw.accepts)),
         "accepts_hex": acc,
         "obs": np.array(sw.obs_rows).tolist(),
+        # another FP64 implementation's rows agree to within the rounding
+        # the measurement wraps amplify (sensitivity x 1000), at least 1e-9
+        "obs_sensitivity": sens,
+        "obs_tol": max(1e-9, 1000.0 * sens),
         "G_re": np.ravel(G.real, order="F").tolist(),
         "G_im": np.ravel(G.imag, order="F").tolist() if np.iscomplexobj(G) else None,
         "log_det": O.log_det(model, sw.s)[0],
@@ -65,7 +98,7 @@ def main() -> None:
         path = HERE / f"sweep_{case}.json"
         path.write_text(json.dumps(spec, separators=(",", ":")) + "\n")
         print(f"{path.name}: {spec['proposals']} proposals, {spec['n_accept']} accepted, "
-              f"{path.stat().st_size} bytes")
+              f"obs tolerance {spec['obs_tol']:.1e}, {path.stat().st_size} bytes")
 
 
 if __name__ == "__main__":

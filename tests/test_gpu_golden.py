@@ -3,8 +3,11 @@
 Each fixture (tests/golden/sweep_*.json, written by make_golden.py) holds a
 small model's initial fields, the Philox stream it consumes and the
 oracle's results after two recorded sweeps.  The GPU must make the same
-accept/reject decisions, end on the same fields, and match G to 1e-10,
-the measurement rows to 1e-9 and log|det| to 1e-9 (relative).  No oracle
+accept/reject decisions, end on the same fields, and match G to 1e-10 and
+log|det| to 1e-9 (relative), and the measurement rows to the fixture's
+``obs_tol``: 1e-9, or 1000 times the change the oracle's own rows show when
+G is perturbed by 1e-15 before each measurement, where the wraps to
+tau = Nt/2 amplify rounding more (t-V, real HS exponentials).  No oracle
 code runs here.
 """
 import json
@@ -20,7 +23,6 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 G_TOL = 1e-10
-OBS_TOL = 1e-9
 LD_TOL = 1e-9
 
 
@@ -44,7 +46,7 @@ def test_gpu_matches_golden_fixture(path):
     assert np.ravel(s_out, order="F").tolist() == spec["s_out"]
     ro = np.array(spec["obs"])
     err = np.abs(obs[0] - ro).max() / max(1.0, np.abs(ro).max())
-    assert err < OBS_TOL, err
+    assert err < spec["obs_tol"], (err, spec["obs_tol"])
     Gw = np.array(spec["G_re"]) + (1j * np.array(spec["G_im"]) if spec["G_im"] is not None else 0)
     Gw = Gw.reshape(model.Ns, model.Ns, order="F")
     rel = np.linalg.norm(G - Gw) / np.linalg.norm(Gw)
