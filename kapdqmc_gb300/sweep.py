@@ -187,7 +187,6 @@ class Sweeper:
         """Replay sweeps from a captured CUDA graph (default) or launch block by block."""
         self._ck(self.lib.kdq_set_graphs(self.h, int(bool(enable))))
 
-    @property
     def set_tiles(self, rows: int):
         """Register-tile class of the sweep kernel (1, 3 or 6 row groups of 32 sites)."""
         self._ck(self.lib.kdq_set_tiles(self.h, int(rows)))
@@ -204,6 +203,7 @@ class Sweeper:
         self._ck(self.lib.kdq_autotune(self.h, C.byref(chosen), ms.ctypes.data, 3))
         return chosen.value, {r: float(t) for r, t in zip((1, 3, 6), ms) if t >= 0}
 
+    @property
     def stream(self) -> int:
         return self.lib.kdq_stream(self.h) or 0
 
