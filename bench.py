@@ -367,6 +367,9 @@ def run_gpu(args):
     # ---- device-resident throughput
     sw.set_fields(fields)
     sw.set_rng(seed)
+    # tile class: one timed sweep per class that covers the lattice (fields
+    # and random-stream positions restored; leaves the handle initialised)
+    tiles, tile_ms = sw.autotune() if not args.no_autotune else (sw.tiles, {})
     sw.init()
     sw.sweep(args.warmup, record=RECORD)
     sw.synchronize()
@@ -463,6 +466,7 @@ def run_gpu(args):
                "max_drift": st["max_drift"],
                "energy_mean": float(ek.mean()), "energy_err": float(ek.mean(axis=1).std() / math.sqrt(NCHAINS)),
                "gpu_launches": args.steps * launches_per_sweep,
+               "tiles": {"class": tiles, "autotune_sweep_ms": tile_ms},
                "roofline": roof, "clocks": clocks,
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
@@ -701,6 +705,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default tile class instead of timing each class first")
     ap.add_argument("--tau-int", type=float, default=None,
                     help="τ_int used to convert chain-sweeps/s (default: the committed long-run value)")
     ap.add_argument("--phases", action="store_true",

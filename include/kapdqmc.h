@@ -142,11 +142,12 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record);
 int kdq_get_obs(kdq_handle* h, double* obs, size_t obs_len);
 int kdq_synchronize(kdq_handle* h);
 
-/* t-U: append to every measurement row the honeycomb structure factors
- * CDW0, CDW1, SDW0, SDW1 with all terms of each correlator (the reference's
- * columns 3-6, src/tU/phy_update.jl:194-235, keep only the first term: its
- * `+adjoint(...)` continuation lines are discarded statements), making 10
- * columns; 0 restores the reference's 6.  Drops rows recorded so far.  No
+/* t-U and complex t-UV: append to every measurement row the honeycomb
+ * structure factors CDW0, CDW1, SDW0, SDW1 with all terms of each correlator
+ * (the reference's columns keep only the first term: its `+adjoint(...)`
+ * continuation lines are discarded statements, src/tU/phy_update.jl:194-235,
+ * src/tUV/phy_update.jl:306-323), making 10 (t-U) or 11 (t-UV) columns; 0
+ * restores the reference's 6 or 7.  Drops rows recorded so far.  No
  * counterpart in the reference. */
 int kdq_set_measure_full(kdq_handle* h, int32_t enable);
 

@@ -7,7 +7,7 @@
 #include "../../include/kapdqmc.h"
 
 #define KDQ_MAX_NS 192          // largest lattice (6 row groups of 32 per lane)
-#define KDQ_MAX_OBS 10          // measurement columns per sweep row
+#define KDQ_MAX_OBS 12          // measurement columns per sweep row
 #define KDQ_THREADS 256         // threads per CTA (one CTA per chain)
 
 // device error flags (ChainCtl::err)
@@ -40,7 +40,7 @@ struct ChainCtl {
 struct SweepParams {
   // model
   int kind, Ns, Nt, z, n_field, NN, n_obs, record;
-  int meas_full;                // t-U: 4 more columns, the structure factors with all terms
+  int meas_full;                // t-U, complex t-UV: 4 more columns, the structure factors with all terms
   int lattice, L1, L2;
   int site_nb;                  // tUV: entries per site in site_bonds
   const int64_t* nodes;         // NN

@@ -1130,11 +1130,12 @@ int kdq_scee_get_green(kdq_handle* h, int32_t chain, int32_t which, double* G, s
 
 int kdq_set_measure_full(kdq_handle* h, int32_t enable) {
   if (!h) return KDQ_ERR_ARG;
-  if (h->kind != KDQ_TU) return fail(h, KDQ_ERR_ARG, "the full structure factors are measured for t-U only");
+  if (h->kind == KDQ_TV || (h->kind == KDQ_TUV && !h->gc))
+    return fail(h, KDQ_ERR_ARG, "the full structure factors are measured for t-U and complex t-UV only");
   KDQ_CUDA(h, cudaSetDevice(h->device));
   KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
   h->P.meas_full = enable ? 1 : 0;
-  h->n_obs = enable ? 10 : 6;
+  h->n_obs = (h->kind == KDQ_TU ? 6 : 7) + (enable ? 4 : 0);
   h->P.n_obs = h->n_obs;
   h->obs_rows = 0;        // rows of the other width are dropped
   h->obs_capacity = 0;

@@ -1119,6 +1119,8 @@ __device__ void observables(Ctx<KIND, T, KT, TW, KW>& c, const TW* G0) {
     acc[1] = P.U * eu;
     acc[2] = P.V * ev;
     for (int q = 0; q < 4; ++q) acc[3 + q] = sf[q] / n2;
+    if (P.meas_full)
+      for (int q = 0; q < 4; ++q) acc[7 + q] = sf[4 + q] / n2;
   }
   if (threadIdx.x == 0) {
     for (int q = 0; q < P.n_obs; ++q) c.ctl->obs_acc[q] += acc[q];

@@ -308,8 +308,8 @@ class Sweeper:
         return (out.view(np.complex128) if cplx else out).reshape(N, N, order="F")
 
     def set_measure_full(self, enable: bool = True):
-        """t-U: also measure the honeycomb structure factors with all terms
-        (columns 6-9 of every measurement row)."""
+        """t-U and complex t-UV: also measure the honeycomb structure factors
+        with all terms (4 more columns after the reference's 6 or 7)."""
         self._ck(self.lib.kdq_set_measure_full(self.h, int(bool(enable))))
         self.n_obs = self.lib.kdq_n_obs(self.h)
 

@@ -128,7 +128,7 @@ class _Sweep:
         self.sweep_no = 0          # Philox sweep counter of the cluster moves
         self.slmc = None           # cluster-move configuration (t-U), see phy_update
         self.slmc_log: list = []   # (u, p) of every cluster-move decision
-        self.full_sf = False       # t-U: append the structure factors with all terms
+        self.full_sf = False       # t-U, complex t-UV: append the structure factors with all terms
 
     def node(self, k):  # 1-based access to nodes
         return self.nodes[k - 1]
@@ -531,13 +531,15 @@ class _TUVSweep(_Sweep):
         out = [Ek, m.U * np.real(Eu), m.V * np.real(Ev), 0.0, 0.0, 0.0, 0.0]
         if "HoneyComb" in m.Lattice:
             out[3:] = _honeycomb_sf_quirk(m.site, G0, m.Ns, spinful_real=not m.is_complex)
+        if self.full_sf:
+            out += _honeycomb_sf_full(m.site, G0, m.Ns) if "HoneyComb" in m.Lattice else [0.0] * 4
         return np.array(out)
 
     def run(self, sweeps):
         m = self.m
         self.init_chain()
         for _ in range(sweeps):
-            acc, cnt = np.zeros(7), 0
+            acc, cnt = np.zeros(11 if self.full_sf else 7), 0
             for lt in range(1, m.Nt + 1):
                 self.G = self.wrap_forward(self.G, lt)
                 self.update_layer(lt)

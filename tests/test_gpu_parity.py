@@ -257,10 +257,11 @@ def test_grover_det_at_middle_slice():
 
 
 @pytest.mark.parametrize("record", [1, 2])
-def test_full_structure_factors(record):
-    # t-U honeycomb with the structure factors' discarded adjoint terms restored
-    # (columns 6-9) next to the reference's columns
-    model = cases.tu_honeycomb()
+@pytest.mark.parametrize("make,ncol", [(cases.tu_honeycomb, 10), (cases.tuv_honeycomb, 11)])
+def test_full_structure_factors(record, make, ncol):
+    # honeycomb t-U and complex t-UV with the structure factors' discarded
+    # adjoint terms restored (4 columns after the reference's)
+    model = make()
     nch, sweeps, seed = 2, 2, 77
     fields = np.stack([Initial_s(model, 300 + c) for c in range(nch)])
     with Sweeper(model, nch) as sw:
@@ -268,7 +269,7 @@ def test_full_structure_factors(record):
         sw.set_fields(fields)
         sw.set_rng(seed)
         obs = sw.phy_update(sweeps, record)
-    assert obs.shape == (nch, sweeps, 10)
+    assert obs.shape == (nch, sweeps, ncol)
     for c in range(nch):
         ref = _oracle_full(model, fields[c], seed, c, sweeps)
         ro = np.array(ref.obs_rows)
