@@ -602,6 +602,62 @@ def run_slmc(args):
     print(json.dumps(out))
 
 
+# Members of the group line: (workload, chains, precision); every configuration
+# with a quarter of its batch, so that no member fills the GPU alone.
+GROUP = [("c1", 64, "fp64"), ("c2", 64, "fp64"), ("c4", 64, "mixed"), ("c5", 64, "mixed")]
+
+
+def run_group(args):
+    """Chains of four lattices and three models swept as one CUDA graph per
+    sweep (kdq_group_sweep) against the same handles swept one after another."""
+    from kapdqmc_gb300 import Initial_s
+    from kapdqmc_gb300.sweep import Sweeper, SweeperGroup
+
+    sws = []
+    for i, (wl, n, prec) in enumerate(GROUP):
+        model = WORKLOADS[wl]["make"]()
+        sw = Sweeper(model, n)
+        sw.set_precision(prec)
+        sw.set_fields(np.stack([Initial_s(model, 4000 + 100 * i + c) for c in range(n)]))
+        sw.set_rng(777 + i)
+        sw.autotune()
+        sws.append(sw)
+    total = sum(n for _, n, _ in GROUP)
+
+    def separate(sweeps):
+        t = time.perf_counter()
+        for sw in sws:
+            sw.sweep(sweeps, record=RECORD)
+            sw.synchronize()
+        return time.perf_counter() - t
+
+    separate(1)                                   # graphs captured, caches warm
+    t_sep = separate(args.steps)
+    with SweeperGroup(sws) as grp:
+        grp.sweep(1, record=RECORD)
+        grp.synchronize()
+        t0 = time.perf_counter()
+        grp.sweep(args.steps, record=RECORD)
+        grp.synchronize()
+        t_grp = time.perf_counter() - t0
+    member_s = {}
+    for (wl, n, prec), sw in zip(GROUP, sws):
+        t = time.perf_counter()
+        sw.sweep(args.steps, record=RECORD)
+        sw.synchronize()
+        member_s[f"{wl}/{n}/{prec}"] = (time.perf_counter() - t) / args.steps
+        sw.close()
+    out = {"metric": "chain-sweeps/s of a group of lattices and models swept as one CUDA graph",
+           "value": total * args.steps / t_grp, "unit": "chain-sweeps/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": 1, "higher_is_better": True, "dtype": "f64 / f32 bulk (mixed members)",
+           "data": "synthetic (seeded HS fields and Philox proposal stream)",
+           "config": {"workload": "group: " + ", ".join(f"{wl} x{n} {p}" for wl, n, p in GROUP)},
+           "separate_value": total * args.steps / t_sep,
+           "speedup_vs_separate": t_sep / t_grp,
+           "seconds_per_sweep_alone": member_s}
+    print(json.dumps(out))
+
+
 def run_scee(args):
     """Coupled SCEE sweep (ctrl_SCEEicr) on a t-U workload: replica pairs of
     the workload's chains, regions A = the first third of the lattice's
@@ -705,6 +761,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--group", action="store_true",
+                    help="lattices of several configurations swept as one CUDA graph vs one after another")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tile class instead of timing each class first")
     ap.add_argument("--tau-int", type=float, default=None,
@@ -740,7 +798,9 @@ def main():
     if args.impl == "reference" and args.workload != "c2":
         print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement covers the t-V workload only"}))
         return
-    if args.scee:
+    if args.group:
+        run_group(args)
+    elif args.scee:
         if args.workload == "c2":
             WL = WORKLOADS["c5"]
             NCHAINS = args.chains or WL["chains"]
