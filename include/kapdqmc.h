@@ -237,9 +237,13 @@ int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32
 int kdq_set_precision(kdq_handle* h, int32_t mode);
 
 /* Per-stage clock counts of the sweep (SM clock cycles, summed over chains):
- * cycles[0] wraps, [1] proposals and updates, [2] measurements, [3] block
- * products of the stabilisation chain, [4] Householder QR, [5] G recompute,
- * [6] self-learning cluster moves (cycles has 8 entries).  Enabling resets the counters and adds a barrier
+ * cycles[0] wraps, [1] G updates of accepted proposals and the proposals'
+ * bookkeeping, [2] measurements, [3] block products of the stabilisation
+ * chain, [4] Householder QR, [5] G recompute, [6] self-learning cluster
+ * moves, [7] acceptance ratios of the mixed-precision sweep (the serial part
+ * of each local proposal, up to the barrier that publishes its decision; the
+ * FP64 sweep overlaps them with the G updates and counts both in [1]);
+ * cycles has 8 entries.  Enabling resets the counters and adds a barrier
  * per stage.  No counterpart in the reference (which has no tracing). */
 int kdq_enable_phase_timing(kdq_handle* h, int32_t enable);
 int kdq_get_phase_cycles(kdq_handle* h, double* cycles);

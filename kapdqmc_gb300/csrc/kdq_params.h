@@ -45,6 +45,8 @@ struct SweepParams {
   int site_nb;                  // tUV: entries per site in site_bonds
   const int64_t* nodes;         // NN
   const double* rtab;           // ratio tables (layout per model, see runtime)
+  const double* dtv;            // t-V: per (slice, old, new) the entries of Delta = UV diag(t2) UV:
+                                //   d00 (= d11), d01 (= d10), 1 + d00
   const double* dtab;           // tU diagonal tables
   const double* vtab;           // tV exponential tables
   const double* gratio;         // 16: gamma[new]/gamma[old], index old*4+new

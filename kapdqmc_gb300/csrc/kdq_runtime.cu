@@ -74,7 +74,7 @@ struct kdq_handle {
   std::string err;
   SweepParams P{};
   // model buffers
-  DevBuf nodes, rtab, dtab, vtab, gratio, xtab, cosr, eta, bx, by, site_bonds;
+  DevBuf nodes, rtab, dtab, vtab, gratio, xtab, cosr, eta, bx, by, site_bonds, dtv;
   DevBuf eK, eKinv, HalfeK, HalfeKinv, K, Pt, PtH;
   // chain buffers
   DevBuf G, W1, W2, Y, Y2, Mss, X, piv, BLs, BRs, s, ctl;
@@ -399,8 +399,21 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
           rt[((size_t)lt * 16 + o * 4 + v) * 2 + 1] = std::exp(-ds) - 1.0;
         }
     }
+    // the entries of Δ = uv diag(t2) uv (uv = [-h -h; -h h]) and 1 + Δ_00 per
+    // (slice, old, new), for the acceptance ratio
+    std::vector<double> dv((size_t)Nt * 16 * 3);
+    const double hh = 0.70710678118654752440;
+    for (size_t q = 0; q < (size_t)Nt * 16; ++q) {
+      const double t0 = rt[2 * q], t1 = rt[2 * q + 1];
+      const double dd = std::fma(-hh * t0, -hh, (-hh * t1) * -hh);
+      const double dof = std::fma(-hh * t0, -hh, (-hh * t1) * hh);
+      dv[3 * q] = dd;
+      dv[3 * q + 1] = dof;
+      dv[3 * q + 2] = 1.0 + dd;
+    }
     KDQ_CK(upload(h->vtab, vt));
     KDQ_CK(upload(h->rtab, rt));
+    KDQ_CK(upload(h->dtv, dv));
   } else {
     // Δ = diag(e^{iΔs}-1, e^{iaΔs}-1) or the real exponentials, and the
     // real-type weight exp((η_old-η_new)(a+1))  (src/tUV/GreenMatrix.jl:73-89,
@@ -501,7 +514,8 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
   SweepParams& P = h->P;
   P.kind = h->kind; P.Ns = N; P.Nt = Nt; P.z = h->z; P.n_field = h->n_field; P.NN = h->NN;
   P.n_obs = h->n_obs; P.record = 0; P.lattice = m->lattice; P.L1 = L1; P.L2 = L2; P.site_nb = site_nb;
-  P.nodes = h->nodes.as<int64_t>(); P.rtab = h->rtab.as<double>(); P.dtab = h->dtab.as<double>();
+  P.nodes = h->nodes.as<int64_t>(); P.rtab = h->rtab.as<double>();
+  P.dtv = h->dtv.as<double>(); P.dtab = h->dtab.as<double>();
   P.vtab = h->vtab.as<double>(); P.gratio = h->gratio.as<double>(); P.xtab = h->xtab.as<double>();
   P.cosr = h->cosr.as<double>(); P.eta = h->eta.as<double>();
   P.a = m->a; P.Ht = m->Ht; P.U = m->U; P.V = m->V;

@@ -67,8 +67,11 @@ __device__ inline void gemm_thin(int M, int N, int K, const TA* A, int lda, cons
 
 // ------------------------------------------------------------ phase timing
 // Optional per-chain clock counts of the sweep's phases (thread 0, between
-// barriers): 0 wraps, 1 proposals and updates, 2 measurements, 3 block
-// products of the stabilisation chain, 4 Householder QR, 5 G recompute.
+// barriers): 0 wraps, 1 G updates and the proposals' bookkeeping, 2
+// measurements, 3 block products of the stabilisation chain, 4 Householder
+// QR, 5 G recompute, 6 cluster moves, 7 acceptance ratios of the FP32
+// working-precision sweep (the FP64 sweep overlaps them with the updates and
+// counts both in 1).
 struct PhaseClock {
   unsigned long long* acc;
   long long t;
@@ -95,8 +98,8 @@ struct Smem {
   double wn[KDQ_MAX_NS / 2];
   T dvec[KDQ_MAX_NS];   // row scaling of the current slice
   T dinv[KDQ_MAX_NS];   // column scaling
-  T ucol[2][KDQ_MAX_NS];
-  T wrow[2][KDQ_MAX_NS];
+  T ucol[4][KDQ_MAX_NS];   // update vectors: [2 buf + r], two buffers of rank 2
+  T wrow[4][KDQ_MAX_NS];
   T rr[4];
   int accept[2];
   int newv;
@@ -135,17 +138,19 @@ struct Ctx {
 // Walks the elements e = tid, tid + nthreads, ... of a column-major M x N
 // matrix keeping (row, col) up to date without a division per element.
 struct Walk {
-  int e, i, j, di, dj, M, total;
-  __device__ Walk(int M_, int N_) : M(M_), total(M_ * N_) {
-    e = threadIdx.x;
+  int e, i, j, di, dj, M, total, st;
+  __device__ Walk(int M_, int N_) : Walk(M_, N_, threadIdx.x, blockDim.x) {}
+  // elements e = start, start + stride, ...
+  __device__ Walk(int M_, int N_, int start, int stride) : M(M_), total(M_ * N_), st(stride) {
+    e = start;
     i = e % M;
     j = e / M;
-    di = blockDim.x % M;
-    dj = blockDim.x / M;
+    di = st % M;
+    dj = st / M;
   }
   __device__ bool ok() const { return e < total; }
   __device__ void next() {
-    e += blockDim.x;
+    e += st;
     i += di;
     j += dj;
     if (i >= M) {
@@ -280,10 +285,79 @@ __device__ void tv_rotate(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int j, int
 
 // ---------------------------------------------------------- local updates
 // Proposal decision and rank-k update (k = 1 for tU, 2 for tV and tUV).
-// Warp 0 evaluates the acceptance ratio (get_r!) and, on acceptance,
-// u' = G[:,S] r into shared memory while the other warps stage the rows
-// G[S,:]; then every thread applies G -= u' (E_S - G[S,:]) (Gupdate!,
-// src/public/Gupdate.jl:5-11).
+// Acceptance ratio p of the proposal sold -> sx (0-based o, nv) on the
+// sites S = {x} (t-U) or {x, y} at slice lt, from G[S,S] (get_r!), and, when
+// tu < p, r = (I + Delta (I - G_SS))^-1 Delta for the update.
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G, int lt, int x, int y, int o,
+                                        int nv, double tu, T& r00, T& r01, T& r10, T& r11) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns;
+  double p;
+  r01 = zero<T>();
+  r10 = zero<T>();
+  r11 = zero<T>();
+  if constexpr (KIND == KDQ_TU) {
+    // get_r!, src/tU/GreenMatrix.jl:49-54; γ ratio src/tU/phy_update.jl:261
+    const cd Δ = reinterpret_cast<const cd*>(P.rtab)[(size_t)(lt - 1) * 16 + o * 4 + nv];
+    const cd g = cvt<cd>(G[x + (size_t)x * N]);
+    const cd pc = cd{1.0, 0.0} + Δ * (cd{1.0, 0.0} - g);
+    p = abs2(pc) * P.gratio[o * 4 + nv];
+    if constexpr (std::is_same_v<T, TW>) {
+      if (tu < p) r00 = Δ / pc;
+    } else if (tu < p) {   // only the G update uses r, in the working precision
+      const cf q = cf{(float)(Δ.x * pc.x + Δ.y * pc.y), (float)(Δ.y * pc.x - Δ.x * pc.y)};
+      const float inv = 1.0f / (float)abs2(pc);
+      r00 = cd{q.x * inv, q.y * inv};
+    }
+  } else if constexpr (KIND == KDQ_TV) {
+    // get_r!, src/tV/GreenMatrix.jl:76-89.  Δ = uv diag(t2) uv with
+    // uv = [-h -h; -h h] is symmetric with equal diagonal entries: dd, do_
+    // and 1 + dd come from the slice table, so the serial chain of a
+    // proposal starts at the G-dependent products.
+    const double* dt = P.dtv + ((size_t)(lt - 1) * 16 + o * 4 + nv) * 3;
+    const double dd = dt[0], do_ = dt[1], dp = dt[2];
+    const double gxx = re(G[x + (size_t)x * N]), gxy = re(G[x + (size_t)y * N]);
+    const double gyx = re(G[y + (size_t)x * N]), gyy = re(G[y + (size_t)y * N]);
+    // r = I + Δ - Δ G_SS
+    const double a00 = dp - (dd * gxx + do_ * gyx), a01 = do_ - (dd * gxy + do_ * gyy);
+    const double a10 = do_ - (do_ * gxx + dd * gyx), a11 = dp - (do_ * gxy + dd * gyy);
+    const double det = a00 * a11 - a01 * a10;
+    p = det * P.gratio[o * 4 + nv];
+    if (tu < p) {   // r = r^-1 Δ = adj(r) Δ / det, needed only for the update
+      const double rd = 1.0 / det;
+      r00 = from_real<T>((a11 * dd - a01 * do_) * rd);
+      r01 = from_real<T>((a11 * do_ - a01 * dd) * rd);
+      r10 = from_real<T>((a00 * do_ - a10 * dd) * rd);
+      r11 = from_real<T>((a00 * dd - a10 * do_) * rd);
+    }
+  } else {
+    // get_r!, src/tUV/GreenMatrix.jl:73-89; weight src/tUV/phy_update.jl:193-197
+    const T* t2 = reinterpret_cast<const T*>(P.rtab) + (size_t)(o * 4 + nv) * 2;
+    const T gxx = cvt<T>(G[x + (size_t)x * N]), gxy = cvt<T>(G[x + (size_t)y * N]);
+    const T gyx = cvt<T>(G[y + (size_t)x * N]), gyy = cvt<T>(G[y + (size_t)y * N]);
+    T a00 = t2[0] - t2[0] * gxx, a01 = zero<T>() - t2[0] * gxy;
+    T a10 = zero<T>() - t2[1] * gyx, a11 = t2[1] - t2[1] * gyy;
+    a00 = a00 + one<T>();
+    a11 = a11 + one<T>();
+    const T det = a00 * a11 - a01 * a10;
+    p = abs2(det) * P.gratio[o * 4 + nv] * P.xtab[o * 4 + nv];
+    if (tu < p) {   // r = r^-1 Δ, needed only for the update
+      const T rd = one<T>() / det;
+      r00 = (a11 * rd) * t2[0];
+      r01 = ((zero<T>() - a01) * rd) * t2[1];
+      r10 = ((zero<T>() - a10) * rd) * t2[0];
+      r11 = (a00 * rd) * t2[1];
+    }
+  }
+  return p;
+}
+
+// Local update with the FP32 working-precision G (the FP64 sweep uses
+// propose_fp64).  Warp 0 evaluates the acceptance ratio (get_r!) and, on
+// acceptance, u' = G[:,S] r into shared memory while the other warps stage
+// the rows G[S,:]; then every thread applies G -= u' (E_S - G[S,:])
+// (Gupdate!, src/public/Gupdate.jl:5-11).
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y, uint8_t* sfield,
                         uint8_t tk, double tu, int logpos, int par) {
@@ -296,64 +370,8 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
     const int sold = *sfield;
     const int sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
     const int o = sold - 1, nv = sx - 1;
-    double p;
-    T r00, r01 = zero<T>(), r10 = zero<T>(), r11 = zero<T>();
-    if constexpr (KIND == KDQ_TU) {
-      // get_r!, src/tU/GreenMatrix.jl:49-54; γ ratio src/tU/phy_update.jl:261
-      const cd Δ = reinterpret_cast<const cd*>(P.rtab)[(size_t)(lt - 1) * 16 + o * 4 + nv];
-      const cd g = cvt<cd>(G[x + (size_t)x * N]);
-      const cd pc = cd{1.0, 0.0} + Δ * (cd{1.0, 0.0} - g);
-      p = abs2(pc) * P.gratio[o * 4 + nv];
-      if constexpr (std::is_same_v<T, TW>) {
-        if (tu < p) r00 = Δ / pc;
-      } else if (tu < p) {   // only the G update uses r, in the working precision
-        const cf q = cf{(float)(Δ.x * pc.x + Δ.y * pc.y), (float)(Δ.y * pc.x - Δ.x * pc.y)};
-        const float inv = 1.0f / (float)abs2(pc);
-        r00 = cd{q.x * inv, q.y * inv};
-      }
-    } else if constexpr (KIND == KDQ_TV) {
-      // get_r!, src/tV/GreenMatrix.jl:76-89
-      const double h = 0.70710678118654752440;
-      const double* t2 = P.rtab + ((size_t)(lt - 1) * 16 + o * 4 + nv) * 2;
-      // Δ = uv diag(t2) uv, uv = [-h -h; -h h]
-      const double q00 = -h * t2[0], q01 = -h * t2[1], q10 = -h * t2[0], q11 = h * t2[1];
-      const double d00 = q00 * -h + q01 * -h, d01 = q00 * -h + q01 * h;
-      const double d10 = q10 * -h + q11 * -h, d11 = q10 * -h + q11 * h;
-      const double gxx = re(G[x + (size_t)x * N]), gxy = re(G[x + (size_t)y * N]);
-      const double gyx = re(G[y + (size_t)x * N]), gyy = re(G[y + (size_t)y * N]);
-      double a00 = d00 - (d00 * gxx + d01 * gyx), a01 = d01 - (d00 * gxy + d01 * gyy);
-      double a10 = d10 - (d10 * gxx + d11 * gyx), a11 = d11 - (d10 * gxy + d11 * gyy);
-      a00 += 1.0;
-      a11 += 1.0;
-      const double det = a00 * a11 - a01 * a10;
-      p = det * P.gratio[o * 4 + nv];
-      if (tu < p) {   // r = r^-1 Δ, needed only for the update
-        const double rd = 1.0 / det;
-        const double i00 = a11 * rd, i01 = -a01 * rd, i10 = -a10 * rd, i11 = a00 * rd;
-        r00 = from_real<T>(i00 * d00 + i01 * d10);
-        r01 = from_real<T>(i00 * d01 + i01 * d11);
-        r10 = from_real<T>(i10 * d00 + i11 * d10);
-        r11 = from_real<T>(i10 * d01 + i11 * d11);
-      }
-    } else {
-      // get_r!, src/tUV/GreenMatrix.jl:73-89; weight src/tUV/phy_update.jl:193-197
-      const T* t2 = reinterpret_cast<const T*>(P.rtab) + (size_t)(o * 4 + nv) * 2;
-      const T gxx = cvt<T>(G[x + (size_t)x * N]), gxy = cvt<T>(G[x + (size_t)y * N]);
-      const T gyx = cvt<T>(G[y + (size_t)x * N]), gyy = cvt<T>(G[y + (size_t)y * N]);
-      T a00 = t2[0] - t2[0] * gxx, a01 = zero<T>() - t2[0] * gxy;
-      T a10 = zero<T>() - t2[1] * gyx, a11 = t2[1] - t2[1] * gyy;
-      a00 = a00 + one<T>();
-      a11 = a11 + one<T>();
-      const T det = a00 * a11 - a01 * a10;
-      p = abs2(det) * P.gratio[o * 4 + nv] * P.xtab[o * 4 + nv];
-      if (tu < p) {   // r = r^-1 Δ, needed only for the update
-        const T rd = one<T>() / det;
-        r00 = (a11 * rd) * t2[0];
-        r01 = ((zero<T>() - a01) * rd) * t2[1];
-        r10 = ((zero<T>() - a10) * rd) * t2[0];
-        r11 = (a00 * rd) * t2[1];
-      }
-    }
+    T r00, r01, r10, r11;
+    const double p = ratio(c, G, lt, x, y, o, nv, tu, r00, r01, r10, r11);
     int acc = tu < p;
     if (!isfinite(p)) {
       acc = 0;
@@ -389,18 +407,8 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
     }
   }
   __syncthreads();
-  if (sm.accept[par] && std::is_same_v<T, TW>) {
-    // FP64: a flat walk over the elements keeps every lane of the FP64 pipe
-    // busy; four elements per step so that their loads overlap
-    for (Walk w(N, N); w.ok(); w.next()) {
-      TW v = G[w.e];
-      madd(v, -sm.ucol[0][w.i], sm.wrow[0][w.j]);
-      if constexpr (RK == 2) madd(v, -sm.ucol[1][w.i], sm.wrow[1][w.j]);
-      G[w.e] = v;
-    }
-    if (tid == 0) *sfield = (uint8_t)sm.newv;
-    __syncthreads();
-  } else if (sm.accept[par]) {
+  c.clk.lap(7);   // the acceptance ratio: the serial part of a proposal
+  if (sm.accept[par]) {
     // FP32: memory latency, not arithmetic, bounds the update; warps own
     // columns, lanes own rows (coalesced), -u' stays in registers across the
     // columns and the row chunks are unrolled so their loads overlap
@@ -433,6 +441,7 @@ __device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y
     if (tid == 0) *sfield = (uint8_t)sm.newv;
     __syncthreads();
   }
+  c.clk.lap(1);
 }
 
 // ------------------------------------------------- self-learning moves (t-U)
@@ -671,6 +680,134 @@ __device__ void finish_tape(Ctx<KIND, T, KT, TW, KW>& c, int n) {
 }
 
 // All proposals of slice lt (tU, tUV) or of direction j of slice lt (tV).
+// G -= u0 w0^T (+ u1 w1^T for rank 2) on the elements start, start + stride,
+// ... of the column-major N x N matrix G, four independent elements per
+// step so that their loads and multiply-adds overlap; with skip, entries in
+// row or column x or y2 are left alone.  Per entry: v = G; v -= u0 w0;
+// v -= u1 w1 (the operation order of Gupdate!, src/public/Gupdate.jl:5-11).
+template <int RK, class TW>
+__device__ __forceinline__ void rank_update(TW* G, int N, const TW* u0, const TW* u1, const TW* w0,
+                                            const TW* w1, int start, int stride, bool skip, int x, int y2) {
+  Walk w[4] = {Walk(N, N, start, 4 * stride), Walk(N, N, start + stride, 4 * stride),
+               Walk(N, N, start + 2 * stride, 4 * stride), Walk(N, N, start + 3 * stride, 4 * stride)};
+  while (w[0].ok()) {
+    bool ok[4];
+    TW v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      ok[k] = w[k].ok() && !(skip && (w[k].i == x || w[k].i == y2 || w[k].j == x || w[k].j == y2));
+      v[k] = ok[k] ? G[w[k].e] : zero<TW>();
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (ok[k]) {
+        madd(v[k], -u0[w[k].i], w0[w[k].j]);
+        if constexpr (RK == 2) madd(v[k], -u1[w[k].i], w1[w[k].j]);
+        G[w[k].e] = v[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) w[k].next();
+  }
+}
+
+// FP64 local updates, pipelined: the G update of the previous accepted
+// proposal is applied while the next proposal is decided.  In the call for
+// proposal m, warps 1.. apply the pending update (m-1) to every entry outside
+// the rows and columns of S_m; warp 0 applies it to those rows and columns,
+// then evaluates the acceptance ratio from the fresh G[S_m,S_m] (get_r!) and,
+// on acceptance, forms u' = G[:,S] r and w = E_S - G[S,:] into the other
+// buffer (Gupdate!, src/public/Gupdate.jl:5-11).  Each entry of G receives
+// the same operations in the same order as in the proposal-by-proposal form
+// (`propose`), so G and every decision are bit for bit the same; the serial
+// ratio now overlaps the previous update's arithmetic.  buf selects the
+// vectors of proposal m; pend says whether buffer buf^1 holds an update.
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void propose_fp64(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y, uint8_t* sfield,
+                             uint8_t tk, double tu, int logpos, int buf, bool pend) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int RK = (KIND == KDQ_TU) ? 1 : 2;
+  Smem<TW>& sm = c.sm;
+  const int y2 = RK == 2 ? y : x;   // S = {x, y2}
+  const int pb = 2 * (buf ^ 1), cb = 2 * buf;
+  const TW* pu0 = sm.ucol[pb];
+  const TW* pu1 = sm.ucol[pb + 1];
+  const TW* pw0 = sm.wrow[pb];
+  const TW* pw1 = sm.wrow[pb + 1];
+  if (warp == 0) {
+    if (pend) {
+      // rows of S (every column), then columns of S (rows outside S)
+      for (int t = lane; t < RK * N; t += 32) {
+        const int a = t < N ? x : y2, b = t < N ? t : t - N;
+        TW v = G[a + (size_t)b * N];
+        madd(v, -pu0[a], pw0[b]);
+        if constexpr (RK == 2) madd(v, -pu1[a], pw1[b]);
+        G[a + (size_t)b * N] = v;
+      }
+      for (int t = lane; t < RK * N; t += 32) {
+        const int b = t < N ? x : y2, a = t < N ? t : t - N;
+        if (a == x || a == y2) continue;
+        TW v = G[a + (size_t)b * N];
+        madd(v, -pu0[a], pw0[b]);
+        if constexpr (RK == 2) madd(v, -pu1[a], pw1[b]);
+        G[a + (size_t)b * N] = v;
+      }
+      __syncwarp();
+    }
+    const int sold = *sfield;
+    const int sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
+    T r00, r01, r10, r11;
+    const double p = ratio(c, G, lt, x, y, sold - 1, sx - 1, tu, r00, r01, r10, r11);
+    int acc = tu < p;
+    if (!isfinite(p)) {
+      acc = 0;
+      if (lane == 0) atomicOr(&c.ctl->err, KDQ_FLAG_NAN);
+    }
+    if (acc) {
+      const TW w00 = cvt<TW>(r00), w01 = cvt<TW>(r01), w10 = cvt<TW>(r10), w11 = cvt<TW>(r11);
+      for (int a = lane; a < N; a += 32) {
+        const TW gx = G[a + (size_t)x * N];
+        if constexpr (RK == 1) {
+          sm.ucol[cb][a] = gx * w00;
+        } else {
+          const TW gy = G[a + (size_t)y * N];
+          sm.ucol[cb][a] = gx * w00 + gy * w10;
+          sm.ucol[cb + 1][a] = gx * w01 + gy * w11;
+        }
+        sm.wrow[cb][a] = (a == x ? one<TW>() : zero<TW>()) - G[x + (size_t)a * N];
+        if constexpr (RK == 2) sm.wrow[cb + 1][a] = (a == y ? one<TW>() : zero<TW>()) - G[y + (size_t)a * N];
+      }
+    }
+    if (lane == 0) {
+      sm.accept[buf] = acc;
+      if (acc) *sfield = (uint8_t)sx;
+      if (c.P.acc_log && logpos >= 0 && logpos < c.P.acc_log_cap)
+        c.P.acc_log[(size_t)c.chain * c.P.acc_log_cap + logpos] = (uint8_t)acc;
+      c.ctl->n_prop += 1;
+      c.ctl->n_acc += acc;
+    }
+  } else if (pend) {
+    rank_update<RK>(G, N, pu0, pu1, pw0, pw1, tid - 32, blockDim.x - 32, true, x, y2);
+  }
+  __syncthreads();
+  c.clk.lap(1);
+}
+
+// The pending update of the last proposal of a layer, on every entry.
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ void flush_update(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int buf) {
+  constexpr int RK = (KIND == KDQ_TU) ? 1 : 2;
+  const int N = c.P.Ns, pb = 2 * buf;
+  const TW* pu0 = c.sm.ucol[pb];
+  const TW* pu1 = c.sm.ucol[pb + 1];
+  const TW* pw0 = c.sm.wrow[pb];
+  const TW* pw1 = c.sm.wrow[pb + 1];
+  rank_update<RK>(G, N, pu0, pu1, pw0, pw1, threadIdx.x, blockDim.x, false, 0, 0);
+  __syncthreads();
+}
+
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fwd) {
   const SweepParams& P = c.P;
@@ -688,6 +825,8 @@ __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fw
   }
   load_tape(c, qs + off, n);
   const int logbase = (int)(c.ctl->log_pos);
+  int buf = 0;
+  bool pend = false;
   for (int m = 0; m < n; ++m) {
     int x, y = 0, f;
     if constexpr (KIND == KDQ_TU) {
@@ -697,7 +836,16 @@ __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fw
     } else {
       x = P.bx[m]; y = P.by[m]; f = m;
     }
-    propose<MAXRM>(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, m & 1);
+    if constexpr (std::is_same_v<T, TW>) {
+      propose_fp64<MAXRM>(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, buf, pend);
+      pend = c.sm.accept[buf] != 0;
+      buf ^= 1;
+    } else {
+      propose<MAXRM>(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, m & 1);
+    }
+  }
+  if constexpr (std::is_same_v<T, TW>) {
+    if (pend) flush_update(c, c.G, buf ^ 1);
   }
   if (threadIdx.x == 0) c.ctl->log_pos += n;
   finish_tape(c, n);

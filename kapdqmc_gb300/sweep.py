@@ -173,7 +173,7 @@ class Sweeper:
         self._ck(self.lib.kdq_set_precision(self.h, code))
         self.precision = mode
 
-    PHASES = ("wrap", "update", "measure", "block_product", "qr", "recompute")
+    PHASES = ("wrap", "update", "measure", "block_product", "qr", "recompute", "cluster_moves", "ratio")
 
     def enable_phase_timing(self, enable: bool = True):
         self._ck(self.lib.kdq_enable_phase_timing(self.h, int(bool(enable))))
@@ -181,7 +181,7 @@ class Sweeper:
     def phase_cycles(self) -> dict:
         out = np.zeros(8)
         self._ck(self.lib.kdq_get_phase_cycles(self.h, out.ctypes.data))
-        return dict(zip(self.PHASES, out[:6].tolist()))
+        return dict(zip(self.PHASES, out[:8].tolist()))
 
     def set_graphs(self, enable: bool):
         """Replay sweeps from a captured CUDA graph (default) or launch block by block."""

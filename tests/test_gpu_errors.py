@@ -38,7 +38,10 @@ def test_model_restrictions():
             sw.slmc_enable(np.zeros(3057, np.float32), 1, 4, 8)
         with pytest.raises(KdqError, match="mixed precision"):
             sw.set_precision("mixed")
-        with pytest.raises(KdqError, match="t-U only"):
+        with pytest.raises(KdqError, match="complex t-UV only"):
+            sw.set_measure_full(True)
+    with Sweeper(cases.tuv_honeycomb(U=-4.0, V=0.3), 2) as sw:     # real t-UV sweep
+        with pytest.raises(KdqError, match="complex t-UV only"):
             sw.set_measure_full(True)
 
 
