@@ -129,7 +129,8 @@ each).  With `record`, one CSV row per sweep, averaged over the chains, is
 appended to the reference's file name under `path`.
 """
 function phy_update(path::String, model, s, Sweeps::Int64, record::Bool=false;
-                    seed::Union{Nothing,Integer}=nothing, tape=nothing, device::Integer=0)
+                    seed::Union{Nothing,Integer}=nothing, tape=nothing, device::Integer=0,
+                    autotune::Bool=false)
     fields = s isa AbstractVector{<:AbstractArray} ? s : [s]
     nch = length(fields)
     h, n_obs = create(model, nch; device=device)
@@ -143,6 +144,10 @@ function phy_update(path::String, model, s, Sweeps::Int64, record::Bool=false;
             k, u = tape
             check(ccall((:kdq_set_tape, libkdq), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Ptr{Float64}, Csize_t),
                         h, UInt8.(k), Float64.(u), length(k) ÷ nch), h)
+        end
+        if autotune   # pick the sweep kernel's tile class (state restored)
+            check(ccall((:kdq_autotune, libkdq), Cint, (Ptr{Cvoid}, Ptr{Int32}, Ptr{Float64}, Int32),
+                        h, C_NULL, C_NULL, 0), h)
         end
         obs = zeros(Float64, n_obs * Sweeps * nch)
         check(ccall((:kdq_phy_update, libkdq), Cint, (Ptr{Cvoid}, Int32, Int32, Ptr{Float64}, Csize_t),
@@ -163,6 +168,65 @@ function phy_update(path::String, model, s, Sweeps::Int64, record::Bool=false;
         destroy(h)
     end
     return s
+end
+
+"""
+    phy_update_group(path, models, ss, Sweeps, record=false; seed, device)
+
+`phy_update` for several models at once (different lattices, models or
+precisions): `models[i]` with the vector of fields `ss[i]` (one chain per
+field, updated in place).  All chains are swept together, one CUDA graph per
+sweep (`kdq_group_sweep`); every model's chains give the same results as a
+`phy_update` of that model alone with the same seed.  With `record`, each
+model's CSV file gets its rows as in `phy_update`.  No counterpart in the
+reference, which runs one model per call.
+"""
+function phy_update_group(path::String, models::Vector, ss::Vector, Sweeps::Int64, record::Bool=false;
+                          seed::Union{Nothing,Integer}=nothing, device::Integer=0)
+    length(models) == length(ss) || error("one vector of fields per model")
+    sd = seed === nothing ? time_ns() : UInt64(seed)
+    hs = Ptr{Cvoid}[]
+    nobs = Int[]
+    g = Ref{Ptr{Cvoid}}(C_NULL)
+    try
+        for (i, (model, fields)) in enumerate(zip(models, ss))
+            h, n_obs = create(model, length(fields); device=device)
+            push!(hs, h)
+            push!(nobs, n_obs)
+            buf = reduce(vcat, [vec(UInt8.(f)) for f in fields])
+            check(ccall((:kdq_set_fields, libkdq), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), h, buf, length(buf)), h)
+            check(ccall((:kdq_set_rng, libkdq), Cint, (Ptr{Cvoid}, UInt64, UInt64), h, sd + (i - 1), 0), h)
+            check(ccall((:kdq_init, libkdq), Cint, (Ptr{Cvoid},), h), h)
+        end
+        rc = ccall((:kdq_group_create, libkdq), Cint, (Ref{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Int32), g, hs, length(hs))
+        rc == 0 || error("kapdqmc: ", unsafe_string(ccall((:kdq_last_error, libkdq), Cstring, (Ptr{Cvoid},), C_NULL)))
+        gerr(rc) = rc == 0 || error("kapdqmc: ", unsafe_string(ccall((:kdq_group_last_error, libkdq), Cstring,
+                                                                     (Ptr{Cvoid},), g[])))
+        gerr(ccall((:kdq_group_sweep, libkdq), Cint, (Ptr{Cvoid}, Int32, Int32), g[], Sweeps, record))
+        gerr(ccall((:kdq_group_synchronize, libkdq), Cint, (Ptr{Cvoid},), g[]))
+        for (i, (model, fields)) in enumerate(zip(models, ss))
+            h, nch = hs[i], length(fields)
+            n = length(fields[1])
+            buf = zeros(UInt8, n * nch)
+            check(ccall((:kdq_get_fields, libkdq), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), h, buf, length(buf)), h)
+            for (c, f) in enumerate(fields)
+                copyto!(f, reshape(buf[(c-1)*n+1:c*n], size(f)))
+            end
+            if record
+                obs = zeros(Float64, nobs[i] * Sweeps * nch)
+                check(ccall((:kdq_get_obs, libkdq), Cint, (Ptr{Cvoid}, Ptr{Float64}, Csize_t), h, obs, length(obs)), h)
+                rows = reshape(obs, nobs[i], Sweeps, nch)
+                mean_rows = dropdims(sum(rows, dims=3), dims=3) ./ nch
+                open(csv_name(path, model), "a") do io
+                    writedlm(io, permutedims(mean_rows), ',')
+                end
+            end
+        end
+    finally
+        g[] == C_NULL || ccall((:kdq_group_destroy, libkdq), Cvoid, (Ptr{Cvoid},), g[])
+        foreach(destroy, hs)
+    end
+    return ss
 end
 
 """
