@@ -68,38 +68,23 @@ def hop_op(i: int, j: int, basis) -> np.ndarray:
     return out
 
 
-def tu_exact(model):
-    """Exact <Ek> and <Eu> of the t-U sweep's measurement at tau = Nt/2.
-
-    Ek = -2 Ht Re sum_ij K_ij <c_ai c_aj^dagger> and Eu = Re sum_i <n_ai (1 - n_bi)>,
-    the expectations of the sweep's per-sample estimates
-    -2 Ht Re sum K .* G0 and sum_i (1 - G0_ii) conj(G0_ii)
-    (src/tU/phy_update.jl:184-190).
-    """
+def _two_species(model, V, ek_sign):
+    """<Ek>, <Eu> of a two-species sweep with weight |det|^2: V(l) is the
+    diagonal field-summed interaction of slice l over (a state, b state)."""
     Ns, Nt = model.Ns, model.Nt
     if Ns > 12:
         raise ValueError(f"Fock-space sum needs Ns <= 12, got {Ns}")
-    ns = Ns // 2
-    basis = _basis(Ns, ns)
-    occ = np.zeros((len(basis), Ns))
-    for k, S in enumerate(basis):
-        occ[k, list(S)] = 1.0
+    basis = _basis(Ns, Ns // 2)
+    occ = _occupations(basis, Ns)
     Ea, Eb = gamma_op(model.eK, basis), gamma_op(model.eK.conj(), basis)
     Ha, Hb = gamma_op(model.HalfeK, basis), gamma_op(model.HalfeK.conj(), basis)
     Hia, Hib = gamma_op(model.HalfeKinv, basis), gamma_op(model.HalfeKinv.conj(), basis)
-    psi = np.outer(slater(model.Pt, basis), slater(model.Pt.conj(), basis))
-    m = occ[:, None, :] - occ[None, :, :]                # n_a - n_b per site, (Sa, Sb, Ns)
-    γ, η = np.asarray(model.γ), np.asarray(model.η)
-
-    def V(l):  # slice l = 1..Nt
-        f = {d: np.sum(γ * np.exp(1j * model.α[l - 1] * η * d)) for d in (-1, 0, 1)}
-        return np.prod(np.select([m == -1, m == 0, m == 1], [f[-1], f[0], f[1]]), axis=2)
-
+    psi = np.outer(slater(model.Pt, basis), slater(model.Pt.conj(), basis)).astype(np.complex128)
     h = Nt // 2
-    R = psi.astype(np.complex128)
+    R = psi.copy()
     for l in range(1, h + 1):
         R = V(l) * (Ea @ R @ Eb.T)
-    L = psi.astype(np.complex128)
+    L = psi.copy()
     for l in range(Nt, h, -1):          # T^H X = Ea^H (conj(V) * X) conj(Eb)
         L = Ea.conj().T @ (V(l).conj() * L) @ Eb.conj()
     norm = np.vdot(L, R)
@@ -118,7 +103,134 @@ def tu_exact(model):
             # <c_i c_j^dagger> = delta_ij - <c_j^dagger c_i>
             g = (1.0 if i == j else 0.0) - expect(hop_op(j, i, basis) @ R1)
             Ek += K[i, j] * g
-    Ek = -2 * model.Ht * Ek.real
+    Ek = ek_sign * 2 * model.Ht * Ek.real
     nb1 = 1.0 - occ                                       # 1 - n_b, per b state
     Eu = sum(expect((occ[:, i][:, None] * nb1[:, i][None, :]) * R1) for i in range(Ns))
     return float(Ek), float(np.real(Eu))
+
+
+def _occupations(basis, Ns):
+    occ = np.zeros((len(basis), Ns))
+    for k, S in enumerate(basis):
+        occ[k, list(S)] = 1.0
+    return occ
+
+
+def tu_exact(model):
+    """Exact <Ek> and <Eu> of the t-U sweep's measurement at tau = Nt/2.
+
+    Ek = -2 Ht Re sum_ij K_ij <c_ai c_aj^dagger> and Eu = Re sum_i <n_ai (1 - n_bi)>,
+    the expectations of the sweep's per-sample estimates
+    -2 Ht Re sum K .* G0 and sum_i (1 - G0_ii) conj(G0_ii)
+    (src/tU/phy_update.jl:184-190).
+    """
+    occ = _occupations(_basis(model.Ns, model.Ns // 2), model.Ns)
+    m = occ[:, None, :] - occ[None, :, :]                # n_a - n_b per site, (Sa, Sb, Ns)
+    γ, η = np.asarray(model.γ), np.asarray(model.η)
+
+    def V(l):  # slice l = 1..Nt
+        f = {d: np.sum(γ * np.exp(1j * model.α[l - 1] * η * d)) for d in (-1, 0, 1)}
+        return np.prod(np.select([m == -1, m == 0, m == 1], [f[-1], f[0], f[1]]), axis=2)
+
+    return _two_species(model, V, -1.0)
+
+
+def tuv_exact(model):
+    """Exact <Ek> and <Eu> / U of the complex t-UV sweep at tau = Nt/2.
+
+    One field per bond (x, y) and slice multiplies species a by
+    exp(i eta (n_x + a n_y)) and species b by its conjugate
+    (src/tUV/GreenMatrix.jl:10-36, src/tUV/phy_update.jl:188-203), so the
+    field sum of a bond is f(m) = sum_k gamma_k exp(i eta_k m) with
+    m = (n_ax + a n_ay) - (n_bx + a n_by).  Returns 2 Ht Re sum K .* G0 and
+    Re sum_i <n_ai (1 - n_bi)> (the sweep's Ek and Eu / U,
+    src/tUV/phy_update.jl:205-235).
+    """
+    if not model.is_complex:
+        raise ValueError("the real t-UV sweep weighs det^2 with extra factors; only the complex one is summed")
+    occ = _occupations(_basis(model.Ns, model.Ns // 2), model.Ns)
+    nn = np.asarray(model.nnidx)
+    X = nn[:, :, 0].ravel(order="F") - 1
+    Y = nn[:, :, 1].ravel(order="F") - 1
+    γ, η = np.asarray(model.γ), np.asarray(model.η)
+    qa = occ[:, X] + model.a * occ[:, Y]                  # per a state and bond
+    m = qa[:, None, :] - qa[None, :, :]                   # (Sa, Sb, bonds)
+    f = np.tensordot(np.exp(1j * m[..., None] * η), γ, axes=([3], [0]))
+    Vc = np.prod(f, axis=2)                               # the same for every slice
+
+    return _two_species(model, lambda l: Vc, 1.0)
+
+
+def tv_exact(model):
+    """Exact <Ek> and <Ev> of the t-V sweep's measurement at tau = Nt/2.
+
+    One fermion species with weight prod(gamma) det(P^H B P),
+    B_l = prod_j (UV_j D_j UV_j) eK (src/tV/GreenMatrix.jl:12-38): a bond
+    (x, y) of direction j acts on its two sites by
+    UV diag(exp(alpha eta), exp(-alpha eta)) UV, UV = [-c -c; -c c], c = 1/sqrt 2,
+    and its field sum is sum_k gamma_k Gamma(that matrix) in Fock space.
+    Returns Ht sum K .* <c c^dagger> and sum_bonds <n_x n_y>, the
+    expectations of the sweep's Ek and Ev (src/tV/phy_update.jl:207-262).
+    """
+    Ns, Nt = model.Ns, model.Nt
+    if Ns > 12:
+        raise ValueError(f"Fock-space sum needs Ns <= 12, got {Ns}")
+    basis = _basis(Ns, Ns // 2)
+    occ = _occupations(basis, Ns)
+    nn = np.asarray(model.nnidx)
+    γ, η = np.asarray(model.γ), np.asarray(model.η)
+    c = 2 ** 0.5 / 2
+    UV = np.array([[-c, -c], [-c, c]])
+
+    def V(l):
+        out = np.eye(len(basis))
+        for j in range(nn.shape[1]):                  # B = (UV_1 D_1 UV_1)(UV_2 D_2 UV_2)... eK
+            Vj = np.eye(len(basis))
+            for b in range(nn.shape[0]):
+                x, y = nn[b, j] - 1
+                S = 0
+                for g, e in zip(γ, η):
+                    v = model.α[l - 1] * e
+                    M = np.eye(Ns)
+                    M[np.ix_([x, y], [x, y])] = UV @ np.diag([np.exp(v), np.exp(-v)]) @ UV
+                    S = S + g * gamma_op(M, basis)
+                Vj = Vj @ S
+            out = out @ Vj
+        return out
+
+    E = gamma_op(model.eK, basis)
+    H, Hi = gamma_op(model.HalfeK, basis), gamma_op(model.HalfeKinv, basis)
+    psi = slater(model.Pt, basis)
+    h = Nt // 2
+    Vs = {}
+
+    def Vl(l):
+        key = float(model.α[l - 1])
+        if key not in Vs:
+            Vs[key] = V(l)
+        return Vs[key]
+
+    R = psi.copy()
+    for l in range(1, h + 1):
+        R = Vl(l) @ (E @ R)
+    L = psi.copy()
+    for l in range(Nt, h, -1):
+        L = E.conj().T @ (Vl(l).conj().T @ L)
+    norm = np.vdot(L, R)
+    R1, L1 = H @ R, Hi.conj().T @ L
+
+    def expect(v):
+        return np.vdot(L1, v) / norm
+
+    K = model.K
+    Ek = 0.0
+    for i in range(Ns):
+        for j in range(Ns):
+            if K[i, j] == 0 and i != j:
+                continue
+            g = (1.0 if i == j else 0.0) - expect(hop_op(j, i, basis) @ R1)
+            Ek += K[i, j] * g
+    x = nn[:, :, 0].ravel() - 1
+    y = nn[:, :, 1].ravel() - 1
+    Ev = expect((occ[:, x] * occ[:, y]).sum(axis=1) * R1)
+    return float(np.real(model.Ht * Ek)), float(np.real(Ev))

@@ -108,3 +108,13 @@ def tu_sq8_flux():
 def tu_hc12():
     return tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Θrelax=1.0, Θquench=0.0, Lattice="HoneyComb120",
                            site=[2, 3], Δt=0.1, BatchSize=5, Initial="H0")
+
+
+def tv_hc8(V=1.0):
+    return tV_Hubbard_Para(Ht=1.0, Hv1=V, Hv2=V, Δt=0.1, Θrelax=1.0, Θquench=0.0,
+                           Lattice="HoneyComb120", site=[2, 2], BatchSize=5, Initial="H0")
+
+
+def tuv_hc8():
+    return tUV_Hubbard_Para(Ht=1.0, Hu=4.0, Hv=0.5, Lattice="HoneyComb120", site=[2, 2], Δt=0.1, Θ=1.0,
+                            BatchSize=5, Initial="H0")

@@ -1,11 +1,12 @@
 """The oracle's Monte Carlo against the exact Fock-space sum of the same
 weights (a known-answer test that does not share the oracle's arithmetic).
 
-oracle/fock_oracle.py sums the t-U sweep's weights over every HS field
-exactly, in the two-species Fock space of an 8-site lattice, and returns the
-expectation of the sweep's per-sample energy estimators at tau = Nt/2.  The
-oracle's chains must reproduce it within five standard errors (independent
-chains, so the error bar is the spread of the chain means).
+oracle/fock_oracle.py sums the sweep's weights over every HS field exactly,
+in the Fock space of an 8-site lattice (two species for t-U and complex
+t-UV, one for t-V), and returns the expectation of the sweep's per-sample
+energy estimators at tau = Nt/2.  The oracle's chains must reproduce it
+within five standard errors (independent chains, so the error bar is the
+spread of the chain means).
 """
 import numpy as np
 
@@ -24,21 +25,44 @@ def test_free_limit_is_exact():
     assert abs(Eu - model.Ns / 4) < 1e-9        # <n_up n_dn> = 1/4 per site
 
 
-def test_oracle_chains_reproduce_exact_sum():
-    model = cases.tu_hc8()
-    Ek, Eu = F.tu_exact(model)
+def _chains(model, nch, sweeps, cols, scale=(1.0, 1.0)):
     n = O.proposals_per_sweep(model)
     means = []
-    for c in range(10):
-        sweeps = 100
+    for c in range(nch):
         ks, us = zip(*(philox.tape(21, c, w, n) for w in range(sweeps)))
         sw = O.phy_update(model, Initial_s(model, 500 + c), sweeps,
                           O.Tape(np.concatenate(ks), np.concatenate(us)), True)
-        means.append(np.array(sw.obs_rows)[10:, :2].mean(0))
+        means.append(np.array(sw.obs_rows)[10:, cols].mean(0) / np.array(scale))
     means = np.array(means)
-    mu, se = means.mean(0), means.std(0, ddof=1) / np.sqrt(len(means))
+    return means.mean(0), means.std(0, ddof=1) / np.sqrt(len(means))
+
+
+def test_oracle_chains_reproduce_exact_sum():
+    model = cases.tu_hc8()
+    Ek, Eu = F.tu_exact(model)
+    mu, se = _chains(model, 10, 100, [0, 1])
     assert abs(mu[0] - Ek) < 5 * se[0], (mu, se, Ek)
     assert abs(mu[1] - Eu) < 5 * se[1], (mu, se, Eu)
     # the interaction must be visible: U = 4 is many error bars from U = 0
     Ek0, Eu0 = F.tu_exact(cases.tu_hc8(U=0.0))
     assert abs(Eu0 - Eu) > 10 * se[1]
+
+
+def test_tv_free_limit_and_oracle_chains():
+    Ek0, Ev0 = F.tv_exact(cases.tv_hc8(V=0.0))
+    m0 = cases.tv_hc8(V=0.0)
+    assert abs(Ek0 - np.linalg.eigvalsh(-m0.Ht * m0.K)[: m0.Ns // 2].sum()) < 1e-6
+    model = cases.tv_hc8()
+    Ek, Ev = F.tv_exact(model)
+    mu, se = _chains(model, 8, 60, [0, 1])
+    assert abs(mu[0] - Ek) < 5 * se[0], (mu, se, Ek)
+    assert abs(mu[1] - Ev) < 5 * se[1], (mu, se, Ev)
+    assert abs(Ev0 - Ev) > 10 * se[1]
+
+
+def test_tuv_oracle_chains():
+    model = cases.tuv_hc8()
+    Ek, Eu = F.tuv_exact(model)
+    mu, se = _chains(model, 6, 50, [0, 1], scale=(1.0, model.U))
+    assert abs(mu[0] - Ek) < 5 * se[0], (mu, se, Ek)
+    assert abs(mu[1] - Eu) < 5 * se[1], (mu, se, Eu)

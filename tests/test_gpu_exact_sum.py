@@ -1,13 +1,13 @@
 """The CUDA sweep's observables against the exact Fock-space sum of its weights.
 
-oracle/fock_oracle.py sums the t-U weights over every HS field exactly on
-8- and 12-site lattices and returns the expectation of the sweep's energy
-estimators at tau = Nt/2.  Hundreds of independent GPU chains must
-reproduce it within five standard errors: in FP64, in mixed precision, with
-a slice-dependent coupling (quench), with a complex hopping matrix (pi
-flux) and with the self-learning cluster moves switched on (their exact
-acceptance must leave the distribution unchanged whatever the network
-proposes).
+oracle/fock_oracle.py sums the weights of the t-U, t-V and complex t-UV
+sweeps over every HS field exactly on 8- and 12-site lattices and returns
+the expectation of the sweep's two energy estimators (columns 0 and 1) at
+tau = Nt/2.  Hundreds of independent GPU chains must reproduce it within
+five standard errors: in FP64, in mixed precision, with a slice-dependent
+coupling (quench), with a complex hopping matrix (pi flux) and with the
+self-learning cluster moves switched on (their exact acceptance must leave
+the distribution unchanged whatever the network proposes).
 """
 import numpy as np
 import pytest
@@ -15,6 +15,7 @@ import pytest
 import cases
 import fock_oracle as F
 from kapdqmc_gb300 import Initial_s, slmc
+from kapdqmc_gb300.model import KIND_TU, KIND_TUV, KIND_TV
 from kapdqmc_gb300.sweep import Sweeper
 
 pytestmark = pytest.mark.gpu
@@ -38,19 +39,35 @@ def _run(model, nchains, precision="fp64", seed=4321, slmc_args=None):
     return mu, se, st
 
 
+def _exact(model):
+    if model.kind == KIND_TU:
+        return F.tu_exact(model)
+    if model.kind == KIND_TV:
+        return F.tv_exact(model)
+    Ek, Eu = F.tuv_exact(model)
+    return Ek, model.U * Eu          # column 1 of t-UV is U * Eu
+
+
 def _check(model, mu, se):
-    Ek, Eu = F.tu_exact(model)
+    Ek, Eu = _exact(model)
     assert abs(mu[0] - Ek) < 5 * se[0] + 1e-9, (mu[0], se[0], Ek)
     assert abs(mu[1] - Eu) < 5 * se[1] + 1e-9, (mu[1], se[1], Eu)
     # the run resolves the answer (the pi-flux lattice's Ek estimator averages to 0)
     assert se[0] < 0.02 * max(1.0, abs(Ek))
 
 
-@pytest.mark.parametrize("make", [cases.tu_hc8, cases.tu_hc8_quench, cases.tu_sq8, cases.tu_sq8_flux])
+@pytest.mark.parametrize("make", [cases.tu_hc8, cases.tu_hc8_quench, cases.tu_sq8, cases.tu_sq8_flux,
+                                  cases.tuv_hc8])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_sweep_reproduces_exact_sum(make, precision):
     model = make()
     mu, se, _ = _run(model, 512, precision)
+    _check(model, mu, se)
+
+
+def test_tv_sweep_reproduces_exact_sum():
+    model = cases.tv_hc8()             # real HS factors: FP64 only
+    mu, se, _ = _run(model, 512, "fp64")
     _check(model, mu, se)
 
 
