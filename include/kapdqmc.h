@@ -264,7 +264,8 @@ void* kdq_stream(kdq_handle* h);
  * kdq_autotune times one sweep of the handle's own chains per valid class,
  * keeps the fastest, puts the fields and each chain's random-stream position
  * back and leaves the handle as kdq_init does; ms[0..2] receive the sweep
- * times of classes 1, 3, 6 (-1 where a class does not fit).  Choices are
+ * times of classes 1, 3, 6 (-1 where a class does not fit).  On failure the
+ * fields and positions are put back and kdq_init must run again.  Choices are
  * cached per device, model, size, precision and batch for the process.  No
  * counterpart in the reference (which calls BLAS). */
 int kdq_set_tiles(kdq_handle* h, int32_t rows);
@@ -279,7 +280,9 @@ int kdq_autotune(kdq_handle* h, int32_t* chosen, double* ms, int32_t len);
  * kdq_group_synchronize waits and checks every handle's error flags;
  * kdq_get_obs and the other per-handle calls read the results.  A handle
  * may belong to several groups but must not be used from another thread
- * during a group call.  Reference counterpart: none (the reference runs one
+ * during a group call, and a group must be destroyed before its handles.
+ * The group always replays a captured graph (kdq_set_graphs does not
+ * apply).  Reference counterpart: none (the reference runs one
  * model per Julia call, src/tU/phy_update.jl:3). */
 typedef struct kdq_group kdq_group;
 int kdq_group_create(kdq_group** out, kdq_handle* const* handles, int32_t n);

@@ -1349,8 +1349,14 @@ int kdq_autotune(kdq_handle* h, int32_t* chosen, double* ms, int32_t len) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (rc != KDQ_OK) {
+    if (rc != KDQ_OK) {   // put the fields and counters back, keep the message
+      const std::string msg = h->err;
+      cudaStreamSynchronize(h->stream);
+      cudaMemcpy(h->s.p, s0.p, fbytes, cudaMemcpyDeviceToDevice);
+      cudaMemcpy(h->ctl.p, c0.p, cbytes, cudaMemcpyDeviceToDevice);
       kdq_set_tiles(h, keep);
+      h->initialised = false;
+      h->err = msg;
       return rc;
     }
     best = cand[best];
