@@ -435,6 +435,27 @@ def run_gpu(args):
               file=sys.stderr, flush=True)
         sw.enable_phase_timing(False)
 
+    # ---- Rényi-2 entropy of the left half (t-UV 8x8): chain pairs (2c, 2c+1)
+    # are the replicas; e^{-S2} = <|det g_A|^2> with g_A the Grover matrix of
+    # the pair's G at tau = Nt/2 (untimed sweeps after the timed region)
+    renyi = None
+    if WL is WORKLOADS["c4"]:
+        from kapdqmc_gb300.geometry import area_index
+        index = area_index("SQUARE45", list(model.site), ((1, 1), (model.site[0], model.site[1])))
+        sw.keep_middle_green(True)
+        vals = []
+        for _ in range(args.renyi_sweeps):
+            sw.sweep(1, record=RECORD)
+            sw.synchronize()
+            vals.append(np.abs(sw.grover_det_middle(index)) ** 2)
+        sw.keep_middle_green(False)
+        v = np.array(vals)                       # (sweeps, pairs)
+        pair_means = v.mean(axis=0)
+        mean, err = float(pair_means.mean()), float(pair_means.std(ddof=1) / math.sqrt(len(pair_means)))
+        renyi = {"S2": -math.log(mean), "S2_err": err / mean, "region": f"left half, {len(index)} sites",
+                 "pairs": len(pair_means), "sweeps": args.renyi_sweeps,
+                 "estimator": "e^-S2 = <|det(2 G1 G2 - G1 - G2 + I)_A|^2>, pair means over sweeps"}
+
     # ---- end to end through kdq_phy_update with host buffers
     e2e_steps = max(2, min(args.steps, 5))
     cur = sw.get_fields()
@@ -457,7 +478,8 @@ def run_gpu(args):
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+               "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64" if PRECISION == "fp64" else "f32 bulk products and updates, f64 ratios/QR/recompute",
                "data": "synthetic (seeded HS fields and Philox proposal stream)",
                "config": dict(config(), parallelism=f"replicas x{world}"),
                "chain_sweeps_per_s": cs_per_s, "tau_int": tau, "tau_int_live": tau_live,
@@ -467,6 +489,7 @@ def run_gpu(args):
                "energy_mean": float(ek.mean()), "energy_err": float(ek.mean(axis=1).std() / math.sqrt(NCHAINS)),
                "gpu_launches": args.steps * launches_per_sweep,
                "tiles": {"class": tiles, "autotune_sweep_ms": tile_ms},
+               **({"renyi2": renyi} if renyi else {}),
                "roofline": roof, "clocks": clocks,
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
@@ -763,6 +786,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--group", action="store_true",
                     help="lattices of several configurations swept as one CUDA graph vs one after another")
+    ap.add_argument("--renyi-sweeps", type=int, default=10,
+                    help="t-UV 8x8 (c4): untimed sweeps whose replica pairs estimate S2 of the left half")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tile class instead of timing each class first")
     ap.add_argument("--tau-int", type=float, default=None,
