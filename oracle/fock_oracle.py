@@ -29,6 +29,7 @@ from __future__ import annotations
 from itertools import combinations
 
 import numpy as np
+import scipy.linalg
 
 
 def _basis(Ns: int, n: int):
@@ -82,11 +83,13 @@ def _two_species(model, V, ek_sign):
     psi = np.outer(slater(model.Pt, basis), slater(model.Pt.conj(), basis)).astype(np.complex128)
     h = Nt // 2
     R = psi.copy()
-    for l in range(1, h + 1):
+    for l in range(1, h + 1):           # rescaled every slice: <O> is a ratio
         R = V(l) * (Ea @ R @ Eb.T)
+        R /= np.linalg.norm(R)
     L = psi.copy()
     for l in range(Nt, h, -1):          # T^H X = Ea^H (conj(V) * X) conj(Eb)
         L = Ea.conj().T @ (V(l).conj() * L) @ Eb.conj()
+        L /= np.linalg.norm(L)
     norm = np.vdot(L, R)
     R1 = Ha @ R @ Hb.T                  # A |R>
     L1 = Hia.conj().T @ L @ Hib.conj()  # (A^-1)^H |L>
@@ -211,11 +214,13 @@ def tv_exact(model):
         return Vs[key]
 
     R = psi.copy()
-    for l in range(1, h + 1):
+    for l in range(1, h + 1):           # rescaled every slice: <O> is a ratio
         R = Vl(l) @ (E @ R)
+        R /= np.linalg.norm(R)
     L = psi.copy()
     for l in range(Nt, h, -1):
         L = E.conj().T @ (Vl(l).conj().T @ L)
+        L /= np.linalg.norm(L)
     norm = np.vdot(L, R)
     R1, L1 = H @ R, Hi.conj().T @ L
 
@@ -234,3 +239,32 @@ def tv_exact(model):
     y = nn[:, :, 1].ravel() - 1
     Ev = expect((occ[:, x] * occ[:, y]).sum(axis=1) * R1)
     return float(np.real(model.Ht * Ek)), float(np.real(Ev))
+
+
+def hubbard_ground_state(model, U: float):
+    """Ground-state energy and double occupancy sum_i <n_i,up n_i,dn> of
+    H = Ht sum_s c_s^dagger K c_s + U sum_i (n_i,up - 1/2)(n_i,dn - 1/2) at half
+    filling, by exact diagonalisation (dense, Ns <= 8): the Hamiltonian the
+    t-U sweep's Trotterised projection converges to as dt -> 0, Theta -> oo
+    (the model's Hu1 = Hu2 = U, src/tU/model.jl:39-96)."""
+    Ns = model.Ns
+    if Ns > 8:
+        raise ValueError(f"dense diagonalisation needs Ns <= 8, got {Ns}")
+    basis = _basis(Ns, Ns // 2)
+    D = len(basis)
+    occ = _occupations(basis, Ns)
+    K = np.asarray(model.K)
+    K = K.real if not np.any(np.imag(K)) else K
+    Hk = np.zeros((D, D), dtype=K.dtype)
+    for i in range(Ns):
+        for j in range(Ns):
+            if K[i, j] != 0:
+                Hk += K[i, j] * hop_op(i, j, basis)
+    eye = np.eye(D)
+    H = model.Ht * (np.kron(Hk, eye) + np.kron(eye, Hk))
+    pair = (occ[:, None, :] - 0.5) * (occ[None, :, :] - 0.5)       # (up state, dn state, site)
+    H += np.diag(U * pair.sum(axis=2).reshape(D * D))
+    w, v = scipy.linalg.eigh(H, subset_by_index=[0, 0])
+    g = np.abs(v[:, 0]) ** 2
+    docc = float(((occ[:, None, :] * occ[None, :, :]).sum(axis=2).reshape(D * D) * g).sum())
+    return float(w[0]), docc

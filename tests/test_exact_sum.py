@@ -14,7 +14,7 @@ import cases
 import dqmc_oracle as O
 import fock_oracle as F
 import philox
-from kapdqmc_gb300 import Initial_s
+from kapdqmc_gb300 import Initial_s, tU_Hubbard_Para
 
 
 def test_free_limit_is_exact():
@@ -66,3 +66,26 @@ def test_tuv_oracle_chains():
     mu, se = _chains(model, 6, 50, [0, 1], scale=(1.0, model.U))
     assert abs(mu[0] - Ek) < 5 * se[0], (mu, se, Ek)
     assert abs(mu[1] - Eu) < 5 * se[1], (mu, se, Eu)
+
+
+def test_trotterised_projection_converges_to_hubbard_ground_state():
+    """The exact sum of the sweep's weights (no sampling) against exact
+    diagonalisation of the Hubbard Hamiltonian the model encodes: the total
+    energy Ek + U Eu - U Ns/4 approaches E0 as dt shrinks (8-site honeycomb,
+    U = 4, Theta = 3), which checks the model's K, alpha, gamma, eta and the
+    sign conventions of the estimators against the physics."""
+    U = 4.0
+
+    def model(dt):
+        return tU_Hubbard_Para(Ht=1.0, Hu1=U, Hu2=U, Δt=dt, Θrelax=3.0, Θquench=0.0,
+                               Lattice="HoneyComb120", site=[2, 2], BatchSize=5, Initial="H0")
+
+    E0, docc = F.hubbard_ground_state(model(0.1), U)
+    errs = []
+    for dt in (0.1, 0.05):
+        m = model(dt)
+        Ek, Eu = F.tu_exact(m)
+        errs.append(abs(Ek + U * Eu - U * m.Ns / 4 - E0))
+    assert errs[0] < 2e-3 and errs[1] < 2e-4 and errs[1] < errs[0] / 4, (E0, errs)
+    Ek, Eu = F.tu_exact(model(0.05))
+    assert abs(Eu - docc) < 1e-2, (Eu, docc)
