@@ -268,3 +268,26 @@ def hubbard_ground_state(model, U: float):
     g = np.abs(v[:, 0]) ** 2
     docc = float(((occ[:, None, :] * occ[None, :, :]).sum(axis=2).reshape(D * D) * g).sum())
     return float(w[0]), docc
+
+
+def tv_ground_state(model, V: float):
+    """Ground-state energy and sum_bonds <n_x n_y> of the spinless
+    H = -Ht c^dagger K c + V sum_bonds (n_x - 1/2)(n_y - 1/2) at half filling,
+    by exact diagonalisation: the Hamiltonian the t-V sweep's Trotterised
+    projection converges to (the model's Hv1 = Hv2 = V, src/tV/model.jl:30-122)."""
+    Ns = model.Ns
+    if Ns > 12:
+        raise ValueError(f"dense diagonalisation needs Ns <= 12, got {Ns}")
+    basis = _basis(Ns, Ns // 2)
+    occ = _occupations(basis, Ns)
+    K = np.asarray(model.K).real
+    H = np.zeros((len(basis), len(basis)))
+    for i in range(Ns):
+        for j in range(Ns):
+            if K[i, j] != 0:
+                H -= model.Ht * K[i, j] * hop_op(i, j, basis)
+    nn = np.asarray(model.nnidx)
+    x, y = nn[:, :, 0].ravel() - 1, nn[:, :, 1].ravel() - 1
+    H += np.diag(V * ((occ[:, x] - 0.5) * (occ[:, y] - 0.5)).sum(axis=1))
+    w, v = np.linalg.eigh(H)
+    return float(w[0]), float(((occ[:, x] * occ[:, y]).sum(axis=1) * v[:, 0] ** 2).sum())

@@ -14,7 +14,7 @@ import cases
 import dqmc_oracle as O
 import fock_oracle as F
 import philox
-from kapdqmc_gb300 import Initial_s, tU_Hubbard_Para
+from kapdqmc_gb300 import Initial_s, tU_Hubbard_Para, tV_Hubbard_Para
 
 
 def test_free_limit_is_exact():
@@ -89,3 +89,23 @@ def test_trotterised_projection_converges_to_hubbard_ground_state():
     assert errs[0] < 2e-3 and errs[1] < 2e-4 and errs[1] < errs[0] / 4, (E0, errs)
     Ek, Eu = F.tu_exact(model(0.05))
     assert abs(Eu - docc) < 1e-2, (Eu, docc)
+
+
+def test_tv_trotterised_projection_converges_to_ground_state():
+    """t-V: Ek + V (Ev - z Ns / 8) of the exact weight sum approaches the
+    exact-diagonalisation ground state of the spinless t-V Hamiltonian."""
+    V = 1.0
+
+    def model(dt):
+        return tV_Hubbard_Para(Ht=1.0, Hv1=V, Hv2=V, Δt=dt, Θrelax=3.0, Θquench=0.0,
+                               Lattice="HoneyComb120", site=[2, 2], BatchSize=5, Initial="H0")
+
+    m = model(0.1)
+    E0, nxny = F.tv_ground_state(m, V)
+    z = m.nnidx.shape[1]
+    errs = []
+    for dt in (0.1, 0.05):
+        Ek, Ev = F.tv_exact(model(dt))
+        errs.append(abs(Ek + V * (Ev - z * m.Ns / 8) - E0))
+    assert errs[0] < 1e-4 and errs[1] < 1e-5 and errs[1] < errs[0] / 4, (E0, errs)
+    assert abs(Ev - nxny) < 1e-2
