@@ -102,6 +102,7 @@ struct Smem {
   T wrow[4][KDQ_MAX_NS];
   T rr[4];
   int accept[2];
+  int nxt[2];      // next proposal of a layer after a window (FP64)
   int newv;
   int bad;
 };
@@ -354,7 +355,7 @@ __device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G
 }
 
 // Local update with the FP32 working-precision G (the FP64 sweep uses
-// propose_fp64).  Warp 0 evaluates the acceptance ratio (get_r!) and, on
+// propose_window).  Warp 0 evaluates the acceptance ratio (get_r!) and, on
 // acceptance, u' = G[:,S] r into shared memory while the other warps stage
 // the rows G[S,:]; then every thread applies G -= u' (E_S - G[S,:])
 // (Gupdate!, src/public/Gupdate.jl:5-11).
@@ -711,101 +712,101 @@ __device__ __forceinline__ void rank_update(TW* G, int N, const TW* u0, const TW
   }
 }
 
-// FP64 local updates, pipelined: the G update of the previous accepted
-// proposal is applied while the next proposal is decided.  In the call for
-// proposal m, warps 1.. apply the pending update (m-1) to every entry outside
-// the rows and columns of S_m; warp 0 applies it to those rows and columns,
-// then evaluates the acceptance ratio from the fresh G[S_m,S_m] (get_r!) and,
-// on acceptance, forms u' = G[:,S] r and w = E_S - G[S,:] into the other
-// buffer (Gupdate!, src/public/Gupdate.jl:5-11).  Each entry of G receives
-// the same operations in the same order as in the proposal-by-proposal form
-// (`propose`), so G and every decision are bit for bit the same; the serial
-// ratio now overlaps the previous update's arithmetic.  buf selects the
-// vectors of proposal m; pend says whether buffer buf^1 holds an update.
+__device__ __forceinline__ double shfl_from(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ cd shfl_from(cd v, int src) {
+  return cd{__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src)};
+}
+
+// Sites and field index of proposal m of a layer (direction jd for t-V).
+template <int KIND>
+__device__ __forceinline__ void proposal_sites(const SweepParams& P, int jd, int n, int m, int& x, int& y, int& f) {
+  if constexpr (KIND == KDQ_TU) {
+    x = m; y = 0; f = m;
+  } else if constexpr (KIND == KDQ_TV) {
+    x = P.bx[jd * n + m]; y = P.by[jd * n + m]; f = jd * n + m;
+  } else {
+    x = P.bx[m]; y = P.by[m]; f = m;
+  }
+}
+
+// FP64 local updates, a window of proposals at a time.  A rejected proposal
+// leaves G unchanged, so the acceptance ratios of proposals m0, m0+1, ...
+// are those a one-by-one sweep computes until the first acceptance: lane k
+// of warp 0 evaluates proposal m0+k (get_r!) from the current G, the first
+// accepting lane (ballot) ends the window, the proposals before it are
+// rejections, and the accepted one's u' = G[:,S] r and E_S - G[S,:] are
+// formed by the warp; then every thread applies G -= u' (E_S - G[S,:])
+// (Gupdate!, src/public/Gupdate.jl:5-11).  The next window starts after the
+// accepted proposal.  Every decision and every entry of G are bit for bit
+// those of the one-by-one order; the serial FP64 ratio chain is paid once
+// per accepted proposal instead of once per proposal.  Returns the index of
+// the next proposal (uniform over the block); par alternates per window.
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
-__device__ void propose_fp64(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y, uint8_t* sfield,
-                             uint8_t tk, double tu, int logpos, int buf, bool pend) {
+__device__ int propose_window(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int jd, int n, int m0, int logbase,
+                              uint8_t* sl, int par) {
   const SweepParams& P = c.P;
   const int N = P.Ns;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr int RK = (KIND == KDQ_TU) ? 1 : 2;
   Smem<TW>& sm = c.sm;
-  const int y2 = RK == 2 ? y : x;   // S = {x, y2}
-  const int pb = 2 * (buf ^ 1), cb = 2 * buf;
-  const TW* pu0 = sm.ucol[pb];
-  const TW* pu1 = sm.ucol[pb + 1];
-  const TW* pw0 = sm.wrow[pb];
-  const TW* pw1 = sm.wrow[pb + 1];
   if (warp == 0) {
-    if (pend) {
-      // rows of S (every column), then columns of S (rows outside S)
-      for (int t = lane; t < RK * N; t += 32) {
-        const int a = t < N ? x : y2, b = t < N ? t : t - N;
-        TW v = G[a + (size_t)b * N];
-        madd(v, -pu0[a], pw0[b]);
-        if constexpr (RK == 2) madd(v, -pu1[a], pw1[b]);
-        G[a + (size_t)b * N] = v;
-      }
-      for (int t = lane; t < RK * N; t += 32) {
-        const int b = t < N ? x : y2, a = t < N ? t : t - N;
-        if (a == x || a == y2) continue;
-        TW v = G[a + (size_t)b * N];
-        madd(v, -pu0[a], pw0[b]);
-        if constexpr (RK == 2) madd(v, -pu1[a], pw1[b]);
-        G[a + (size_t)b * N] = v;
-      }
-      __syncwarp();
+    const int W = min(32, n - m0);
+    const int m = m0 + lane;
+    const bool valid = lane < W;
+    int x = 0, y = 0, f = 0, sx = 0, acc = 0;
+    bool bad = false;
+    T r00 = zero<T>(), r01 = zero<T>(), r10 = zero<T>(), r11 = zero<T>();
+    if (valid) {
+      proposal_sites<KIND>(P, jd, n, m, x, y, f);
+      const int sold = sl[f];
+      const int tk = c.tk[m];
+      sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
+      const double p = ratio(c, G, lt, x, y, sold - 1, sx - 1, c.tu[m], r00, r01, r10, r11);
+      bad = !isfinite(p);
+      acc = !bad && c.tu[m] < p;
     }
-    const int sold = *sfield;
-    const int sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
-    T r00, r01, r10, r11;
-    const double p = ratio(c, G, lt, x, y, sold - 1, sx - 1, tu, r00, r01, r10, r11);
-    int acc = tu < p;
-    if (!isfinite(p)) {
-      acc = 0;
-      if (lane == 0) atomicOr(&c.ctl->err, KDQ_FLAG_NAN);
+    const unsigned amask = __ballot_sync(0xffffffffu, acc);
+    const int ja = amask ? __ffs(amask) - 1 : W;   // first accepting lane, W if none
+    const int nres = ja < W ? ja + 1 : W;          // proposals decided by this window
+    if (lane < nres && bad) atomicOr(&c.ctl->err, KDQ_FLAG_NAN);
+    if (lane < nres) {
+      const int logpos = logbase + m;
+      if (P.acc_log && logpos >= 0 && logpos < P.acc_log_cap)
+        P.acc_log[(size_t)c.chain * P.acc_log_cap + logpos] = (uint8_t)(lane == ja);
     }
-    if (acc) {
-      const TW w00 = cvt<TW>(r00), w01 = cvt<TW>(r01), w10 = cvt<TW>(r10), w11 = cvt<TW>(r11);
+    if (ja < W && lane == ja) sl[f] = (uint8_t)sx;   // lane W (no acceptance) holds no proposal
+    if (ja < W) {
+      const int xa = __shfl_sync(0xffffffffu, x, ja), ya = __shfl_sync(0xffffffffu, y, ja);
+      const TW w00 = cvt<TW>(shfl_from(r00, ja)), w01 = cvt<TW>(shfl_from(r01, ja));
+      const TW w10 = cvt<TW>(shfl_from(r10, ja)), w11 = cvt<TW>(shfl_from(r11, ja));
       for (int a = lane; a < N; a += 32) {
-        const TW gx = G[a + (size_t)x * N];
+        const TW gx = G[a + (size_t)xa * N];
         if constexpr (RK == 1) {
-          sm.ucol[cb][a] = gx * w00;
+          sm.ucol[0][a] = gx * w00;
         } else {
-          const TW gy = G[a + (size_t)y * N];
-          sm.ucol[cb][a] = gx * w00 + gy * w10;
-          sm.ucol[cb + 1][a] = gx * w01 + gy * w11;
+          const TW gy = G[a + (size_t)ya * N];
+          sm.ucol[0][a] = gx * w00 + gy * w10;
+          sm.ucol[1][a] = gx * w01 + gy * w11;
         }
-        sm.wrow[cb][a] = (a == x ? one<TW>() : zero<TW>()) - G[x + (size_t)a * N];
-        if constexpr (RK == 2) sm.wrow[cb + 1][a] = (a == y ? one<TW>() : zero<TW>()) - G[y + (size_t)a * N];
+        sm.wrow[0][a] = (a == xa ? one<TW>() : zero<TW>()) - G[xa + (size_t)a * N];
+        if constexpr (RK == 2) sm.wrow[1][a] = (a == ya ? one<TW>() : zero<TW>()) - G[ya + (size_t)a * N];
       }
     }
     if (lane == 0) {
-      sm.accept[buf] = acc;
-      if (acc) *sfield = (uint8_t)sx;
-      if (c.P.acc_log && logpos >= 0 && logpos < c.P.acc_log_cap)
-        c.P.acc_log[(size_t)c.chain * c.P.acc_log_cap + logpos] = (uint8_t)acc;
-      c.ctl->n_prop += 1;
-      c.ctl->n_acc += acc;
+      sm.accept[par] = ja < W;
+      sm.nxt[par] = m0 + nres;
+      c.ctl->n_prop += nres;
+      c.ctl->n_acc += (ja < W) ? 1 : 0;
     }
-  } else if (pend) {
-    rank_update<RK>(G, N, pu0, pu1, pw0, pw1, tid - 32, blockDim.x - 32, true, x, y2);
   }
   __syncthreads();
+  const int next = sm.nxt[par];
+  if (sm.accept[par]) {
+    rank_update<RK>(G, N, sm.ucol[0], sm.ucol[1], sm.wrow[0], sm.wrow[1], tid, blockDim.x, false, 0, 0);
+    __syncthreads();
+  }
   c.clk.lap(1);
-}
-
-// The pending update of the last proposal of a layer, on every entry.
-template <int KIND, class T, class KT, class TW, class KW>
-__device__ void flush_update(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int buf) {
-  constexpr int RK = (KIND == KDQ_TU) ? 1 : 2;
-  const int N = c.P.Ns, pb = 2 * buf;
-  const TW* pu0 = c.sm.ucol[pb];
-  const TW* pu1 = c.sm.ucol[pb + 1];
-  const TW* pw0 = c.sm.wrow[pb];
-  const TW* pw1 = c.sm.wrow[pb + 1];
-  rank_update<RK>(G, N, pu0, pu1, pw0, pw1, threadIdx.x, blockDim.x, false, 0, 0);
-  __syncthreads();
+  return next;
 }
 
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
@@ -825,27 +826,15 @@ __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fw
   }
   load_tape(c, qs + off, n);
   const int logbase = (int)(c.ctl->log_pos);
-  int buf = 0;
-  bool pend = false;
-  for (int m = 0; m < n; ++m) {
-    int x, y = 0, f;
-    if constexpr (KIND == KDQ_TU) {
-      x = m; f = m;
-    } else if constexpr (KIND == KDQ_TV) {
-      x = P.bx[j * n + m]; y = P.by[j * n + m]; f = j * n + m;
-    } else {
-      x = P.bx[m]; y = P.by[m]; f = m;
-    }
-    if constexpr (std::is_same_v<T, TW>) {
-      propose_fp64<MAXRM>(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, buf, pend);
-      pend = c.sm.accept[buf] != 0;
-      buf ^= 1;
-    } else {
+  if constexpr (std::is_same_v<T, TW>) {
+    int par = 0;
+    for (int m = 0; m < n; par ^= 1) m = propose_window<MAXRM>(c, c.G, lt, j, n, m, logbase, sl, par);
+  } else {
+    for (int m = 0; m < n; ++m) {
+      int x, y, f;
+      proposal_sites<KIND>(P, j, n, m, x, y, f);
       propose<MAXRM>(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, m & 1);
     }
-  }
-  if constexpr (std::is_same_v<T, TW>) {
-    if (pend) flush_update(c, c.G, buf ^ 1);
   }
   if (threadIdx.x == 0) c.ctl->log_pos += n;
   finish_tape(c, n);
