@@ -1,4 +1,4 @@
-"""Write the golden fixtures of the sweep (``sweep_*.json``) from the CPU oracle.
+"""Write the golden fixtures (``sweep_*.json``, ``scee_*.json``, ``cnn_*.json``) from the CPU oracle.
 
 The reference ships no stored outputs (its tests run sweeps without
 assertions), so these fixtures pin the oracle's own results on small models:
@@ -25,9 +25,11 @@ for p in (ROOT, ROOT / "oracle", HERE.parent):
         sys.path.insert(0, str(p))
 
 import cases                     # noqa: E402
+import cnn_oracle as CNN         # noqa: E402
 import dqmc_oracle as O          # noqa: E402
 import philox                    # noqa: E402
-from kapdqmc_gb300 import Initial_s   # noqa: E402
+import scee_oracle as S          # noqa: E402
+from kapdqmc_gb300 import Initial_s, area_index   # noqa: E402
 
 CASES = ["tu_square", "tu_honeycomb", "tu_quench", "tu_square90_flux", "tu_honeycomb60",
          "tv_honeycomb", "tv_honeycomb60", "tuv_honeycomb", "tuv_square", "tuv_honeycomb60"]
@@ -92,6 +94,50 @@ def make(case: str) -> dict:
     }
 
 
+def scee_tape(seed, sweeps, n_rep):
+    """Philox stream of replica pair 0 in the coupled sweep's consumption order."""
+    ks, us = [], []
+    for w in range(sweeps):
+        k0, u0 = philox.tape(seed, 0, w, n_rep)
+        k1, u1 = philox.tape(seed, 1, w, n_rep)
+        ks.append(np.stack([k0, k1], axis=1).ravel())
+        us.append(np.stack([u0, u1], axis=1).ravel())
+    return np.concatenate(ks), np.concatenate(us)
+
+
+def make_scee() -> dict:
+    """ctrl_SCEEicr on the 3x3 honeycomb t-U model: one replica pair, two sweeps."""
+    m = cases.tu_honeycomb()
+    L = m.site[1]
+    A = area_index(m.Lattice, m.site, ([1, 1], [L // 3, L]))
+    B = area_index(m.Lattice, m.site, ([1, 1], [L // 3, 2 * L // 3]))
+    s1, s2 = Initial_s(m, 70), Initial_s(m, 71)
+    sweeps, lam, nlam = 2, 0.5, 2
+    k, u = scee_tape(SEED, sweeps, 2 * m.Ns * m.Nt)
+    ref = S.SCEE(m, s1, s2, A, B, lam, nlam, O.Tape(k, u)).run(sweeps)
+    G0 = np.asarray(ref.G0[0])
+    return {"case": "tu_honeycomb", "seed": SEED, "sweeps": sweeps, "lam": lam, "nlam": nlam,
+            "A": list(map(int, A)), "B": list(map(int, B)),
+            "s": [np.ravel(s1, order="F").tolist(), np.ravel(s2, order="F").tolist()],
+            "s_out": [np.ravel(ref.s[0], order="F").tolist(), np.ravel(ref.s[1], order="F").tolist()],
+            "accepts_hex": np.packbits(np.array(ref.accepts, dtype=bool)).tobytes().hex(),
+            "n_decisions": len(ref.accepts), "O": list(map(float, ref.O)),
+            "G0_re": np.ravel(G0.real, order="F").tolist(), "G0_im": np.ravel(G0.imag, order="F").tolist()}
+
+
+def make_cnn() -> dict:
+    """The effective model's F and its parameter gradient on seeded fields."""
+    rng = np.random.default_rng(5)
+    fields = rng.integers(1, 5, size=(3, 12, 18)).astype(np.uint8)
+    params = CNN.init_params(3)
+    F, _ = CNN.forward(fields, params)
+    dF = np.array([1.0, -0.5, 0.25])
+    g = CNN.grad(fields, dF, params)
+    return {"fields": fields.ravel().tolist(), "shape": list(fields.shape), "param_seed": 3,
+            "dF": dF.tolist(), "F": np.asarray(F, dtype=np.float64).tolist(),
+            "grad": np.asarray(g, dtype=np.float64).tolist()}
+
+
 def main() -> None:
     for case in CASES:
         spec = make(case)
@@ -99,6 +145,10 @@ def main() -> None:
         path.write_text(json.dumps(spec, separators=(",", ":")) + "\n")
         print(f"{path.name}: {spec['proposals']} proposals, {spec['n_accept']} accepted, "
               f"obs tolerance {spec['obs_tol']:.1e}, {path.stat().st_size} bytes")
+    for name, spec in (("scee_tu_honeycomb.json", make_scee()), ("cnn_forward_grad.json", make_cnn())):
+        path = HERE / name
+        path.write_text(json.dumps(spec, separators=(",", ":")) + "\n")
+        print(f"{path.name}: {path.stat().st_size} bytes")
 
 
 if __name__ == "__main__":

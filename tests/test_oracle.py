@@ -6,7 +6,8 @@
   ground-state energy of the hopping matrix and every proposal's ratio is the
   γ ratio;
 * Philox4x32-10 matches the published known-answer vectors;
-* committed golden fixtures (tests/golden/) reproduce.
+* committed golden fixtures (tests/golden/: sweeps of every model, a
+  coupled SCEE run, the effective model's F and gradient) reproduce.
 """
 import json
 from pathlib import Path
@@ -129,3 +130,37 @@ def test_c_restatement_matches_numpy_oracle():
     np.testing.assert_array_equal(acc.astype(bool), np.array(ref.accepts))
     np.testing.assert_array_equal(s2, ref.s)
     np.testing.assert_allclose(obs, np.array(ref.obs_rows), rtol=1e-9, atol=1e-10)
+
+
+def test_golden_scee_fixture():
+    """The coupled SCEE restatement reproduces its committed fixture."""
+    import importlib.util
+    import scee_oracle as S
+    spec_mod = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec_mod)
+    spec_mod.loader.exec_module(mg)
+    scee_tape = mg.scee_tape
+    spec = json.loads((GOLDEN / "scee_tu_honeycomb.json").read_text())
+    m = getattr(cases, spec["case"])()
+    s1, s2 = (np.array(v, dtype=np.uint8).reshape(m.field_shape, order="F") for v in spec["s"])
+    k, u = scee_tape(spec["seed"], spec["sweeps"], 2 * m.Ns * m.Nt)
+    ref = S.SCEE(m, s1, s2, spec["A"], spec["B"], spec["lam"], spec["nlam"], O.Tape(k, u)).run(spec["sweeps"])
+    acc = np.unpackbits(np.frombuffer(bytes.fromhex(spec["accepts_hex"]), np.uint8))[: spec["n_decisions"]]
+    np.testing.assert_array_equal(np.array(ref.accepts, dtype=bool), acc.astype(bool))
+    for r in range(2):
+        assert np.ravel(ref.s[r], order="F").tolist() == spec["s_out"][r]
+    np.testing.assert_allclose(ref.O, spec["O"], rtol=1e-10)
+    G0 = (np.array(spec["G0_re"]) + 1j * np.array(spec["G0_im"])).reshape(m.Ns, m.Ns, order="F")
+    assert np.linalg.norm(ref.G0[0] - G0) / np.linalg.norm(G0) < 1e-12
+
+
+def test_golden_cnn_fixture():
+    """The effective model's restatement reproduces F and its gradient."""
+    import cnn_oracle as CNN
+    spec = json.loads((GOLDEN / "cnn_forward_grad.json").read_text())
+    fields = np.array(spec["fields"], dtype=np.uint8).reshape(spec["shape"])
+    params = CNN.init_params(spec["param_seed"])
+    F, _ = CNN.forward(fields, params)
+    np.testing.assert_allclose(F, spec["F"], rtol=1e-12, atol=1e-12)
+    g = CNN.grad(fields, np.array(spec["dF"]), params)
+    np.testing.assert_allclose(g, spec["grad"], rtol=1e-10, atol=1e-12)
