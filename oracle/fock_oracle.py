@@ -291,3 +291,104 @@ def tv_ground_state(model, V: float):
     H += np.diag(V * ((occ[:, x] - 0.5) * (occ[:, y] - 0.5)).sum(axis=1))
     w, v = np.linalg.eigh(H)
     return float(w[0]), float(((occ[:, x] * occ[:, y]).sum(axis=1) * v[:, 0] ** 2).sum())
+
+
+def _split_sign(S, A):
+    """Sign of reordering the occupied modes S (ascending sites) so that the
+    sites in A come first (each in ascending order)."""
+    inv, seen_b = 0, 0
+    for i in S:
+        if i in A:
+            inv += seen_b
+        else:
+            seen_b += 1
+    return -1.0 if inv & 1 else 1.0
+
+
+def _region_split(basis, A):
+    """Row (region) and column (rest) index and sign of every two-species
+    basis state (Sa, Sb), modes reordered as (a_A, b_A, a_B, b_B)."""
+    keyA, keyB = {}, {}
+    rows, cols, sg = [], [], []
+    for Sa in basis:
+        aA = tuple(i for i in Sa if i in A)
+        aB = tuple(i for i in Sa if i not in A)
+        for Sb in basis:
+            bA = tuple(i for i in Sb if i in A)
+            bB = tuple(i for i in Sb if i not in A)
+            s = _split_sign(Sa, A) * _split_sign(Sb, A) * (-1.0 if (len(bA) * len(aB)) & 1 else 1.0)
+            rows.append(keyA.setdefault((aA, bA), len(keyA)))
+            cols.append(keyB.setdefault((aB, bB), len(keyB)))
+            sg.append(s)
+    return np.array(rows), np.array(cols), np.array(sg), (len(keyA), len(keyB))
+
+
+def tr_rho_rho(R1, L1, R2, L2, basis, A):
+    """Tr(rho1_A rho2_A) for the two-species operators rho_k = |R_k><L_k| / <L_k|R_k>
+    (R, L as (a state, b state) amplitude matrices), A a set of 0-based sites."""
+    rows, cols, sg, shape = _region_split(basis, set(int(a) for a in A))
+
+    def mat(X):
+        P = np.zeros(shape, dtype=np.complex128)
+        P[rows, cols] = sg * X.ravel()
+        return P
+
+    r1 = mat(R1) @ mat(L1).conj().T / np.vdot(L1, R1)
+    r2 = mat(R2) @ mat(L2).conj().T / np.vdot(L2, R2)
+    return complex(np.trace(r1 @ r2))
+
+
+def tu_states(model, V):
+    """R = T_h .. T_1 |Psi> and L = T_{h+1}^H .. T_Nt^H |Psi> (h = Nt/2) of the
+    two-species t-U transfer matrices with slice interactions V(l)."""
+    Ns, Nt = model.Ns, model.Nt
+    basis = _basis(Ns, Ns // 2)
+    Ea, Eb = gamma_op(model.eK, basis), gamma_op(model.eK.conj(), basis)
+    psi = np.outer(slater(model.Pt, basis), slater(model.Pt.conj(), basis)).astype(np.complex128)
+    h = Nt // 2
+    R = psi.copy()
+    for l in range(1, h + 1):
+        R = V(l) * (Ea @ R @ Eb.T)
+        R /= np.linalg.norm(R)
+    L = psi.copy()
+    for l in range(Nt, h, -1):
+        L = Ea.conj().T @ (V(l).conj() * L) @ Eb.conj()
+        L /= np.linalg.norm(L)
+    return R, L, basis
+
+
+def tu_config_states(model, s):
+    """tu_states for one field configuration s (Ns x Nt): species a sees
+    cis(alpha eta) on occupied sites, species b its conjugate."""
+    basis = _basis(model.Ns, model.Ns // 2)
+    occ = _occupations(basis, model.Ns)
+    η = np.asarray(model.η)
+
+    def V(l):
+        ph = model.α[l - 1] * η[np.asarray(s)[:, l - 1].astype(np.int64) - 1]
+        fa = np.exp(1j * occ @ ph)
+        return np.outer(fa, fa.conj())
+
+    return tu_states(model, V)
+
+
+def tu_renyi2(model, A):
+    """Exact e^{-S2} = Tr(rho_A^2) of the t-U sweep's two-species state at
+    tau = Nt/2, rho = |R><L| / <L|R> with R = T_h .. T_1 |Psi>,
+    <L| = <Psi| T_Nt .. T_{h+1} (the field sums of tu_exact), and A a set of
+    0-based sites taken in both species.  This is what the replica estimator
+    |det(2 G1 G2 - G1 - G2 + I)_A|^2 over independent pairs of the sweep's
+    configurations at tau = Nt/2 converges to (GroverMatrix!,
+    src/public/GF.jl:101-109; |det|^2 as in src/tU/SCEE.jl:264-276)."""
+    if model.Ns > 8:
+        raise ValueError(f"Fock-space replica sum needs Ns <= 8, got {model.Ns}")
+    occ = _occupations(_basis(model.Ns, model.Ns // 2), model.Ns)
+    m = occ[:, None, :] - occ[None, :, :]
+    γ, η = np.asarray(model.γ), np.asarray(model.η)
+
+    def V(l):
+        f = {d: np.sum(γ * np.exp(1j * model.α[l - 1] * η * d)) for d in (-1, 0, 1)}
+        return np.prod(np.select([m == -1, m == 0, m == 1], [f[-1], f[0], f[1]]), axis=2)
+
+    R, L, basis = tu_states(model, V)
+    return tr_rho_rho(R, L, R, L, basis, A)

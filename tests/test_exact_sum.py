@@ -109,3 +109,29 @@ def test_tv_trotterised_projection_converges_to_ground_state():
         errs.append(abs(Ek + V * (Ev - z * m.Ns / 8) - E0))
     assert errs[0] < 1e-4 and errs[1] < 1e-5 and errs[1] < errs[0] / 4, (E0, errs)
     assert abs(Ev - nxny) < 1e-2
+
+
+def test_replica_estimator_identity_and_free_limit():
+    """Rényi-2: for two field configurations, the Fock-space Tr(rho1_A rho2_A)
+    of their two-species states at tau = Nt/2 equals the replica estimator
+    |det(2 G1 G2 - G1 - G2 + I)_A|^2 on the restricted Green's functions (for
+    regions that are not prefixes of the site order too); summed over the
+    fields it is exact e^{-S2}, which at U = 0 is the free-fermion value."""
+    m = cases.tu_hc8()
+    s1, s2 = Initial_s(m, 1), Initial_s(m, 2)
+    R1, L1, basis = F.tu_config_states(m, s1)
+    R2, L2, _ = F.tu_config_states(m, s2)
+    h = m.Nt // 2
+    G1, G2 = O.G_tau(m, s1, h), O.G_tau(m, s2, h)
+    for A in ([0, 1, 2, 3], [0, 2, 5], [1, 4, 6, 7], [3]):
+        a, b = G1[np.ix_(A, A)], G2[np.ix_(A, A)]
+        d = np.linalg.det(2 * a @ b - a - b + np.eye(len(A)))
+        fock = F.tr_rho_rho(R1, L1, R2, L2, basis, A)
+        assert abs(fock - abs(d) ** 2) < 1e-9 * max(1.0, abs(d) ** 2), (A, fock, abs(d) ** 2)
+    m0 = cases.tu_hc8(U=0.0)
+    A = [0, 1, 2, 3]
+    G = np.eye(m0.Ns) - m0.Pt @ np.linalg.inv(m0.Pt.conj().T @ m0.Pt) @ m0.Pt.conj().T
+    g = G[np.ix_(A, A)]
+    free = abs(np.linalg.det(g @ g + (np.eye(4) - g) @ (np.eye(4) - g))) ** 2
+    assert abs(F.tu_renyi2(m0, A) - free) < 1e-9
+    assert 0.0 < F.tu_renyi2(m, A).real < 1.0
