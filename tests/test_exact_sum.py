@@ -135,3 +135,30 @@ def test_replica_estimator_identity_and_free_limit():
     free = abs(np.linalg.det(g @ g + (np.eye(4) - g) @ (np.eye(4) - g))) ** 2
     assert abs(F.tu_renyi2(m0, A) - free) < 1e-9
     assert 0.0 < F.tu_renyi2(m, A).real < 1.0
+
+
+def test_scee_estimator_converges_to_exact_replica_ratio():
+    """The coupled SCEE sweep (ctrl_SCEEicr restated) with lambda = 0 and
+    N_lambda = 1 samples pairs with weight w(s1) w(s2) |det g_B|^2 and averages
+    |det g_A|^2 / |det g_B|^2, so its estimator converges to
+    Tr(rho_A^2) / Tr(rho_B^2) of the exact replica sums."""
+    import scee_oracle as S
+    m = cases.tu_hc8()
+    A, B = [0, 1, 2, 3], [0, 1]
+    exact = F.tu_renyi2(m, A).real / F.tu_renyi2(m, B).real
+    n_rep = 2 * m.Ns * m.Nt
+    means = []
+    for p in range(5):
+        sweeps = 100
+        ks, us = [], []
+        for w in range(sweeps):
+            k0, u0 = philox.tape(5, 2 * p, w, n_rep)
+            k1, u1 = philox.tape(5, 2 * p + 1, w, n_rep)
+            ks.append(np.stack([k0, k1], axis=1).ravel())
+            us.append(np.stack([u0, u1], axis=1).ravel())
+        ref = S.SCEE(m, Initial_s(m, 300 + 2 * p), Initial_s(m, 301 + 2 * p), [a + 1 for a in A],
+                     [b + 1 for b in B], 0.0, 1, O.Tape(np.concatenate(ks), np.concatenate(us))).run(sweeps)
+        means.append(np.mean(ref.O[20:]))
+    mu, se = np.mean(means), np.std(means, ddof=1) / np.sqrt(len(means))
+    assert abs(mu - exact) < 5 * se, (mu, se, exact)
+    assert se < 0.1 * exact
