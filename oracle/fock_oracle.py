@@ -392,3 +392,26 @@ def tu_renyi2(model, A):
 
     R, L, basis = tu_states(model, V)
     return tr_rho_rho(R, L, R, L, basis, A)
+
+
+def tu_disorder(model, region, alpha: float):
+    """Exact <exp(i alpha (N_a,R - N_b,R))> of the t-U sweep's two-species state
+    at tau = Nt/2 (region R: 0-based sites): the average over the sweep's
+    configurations of |det X_R|^2, X = e^{i alpha} I + (1 - e^{i alpha}) G[R,R]
+    (the disorder operator of ctrl_SCDOPicr, src/tU/disorder_operate.jl:202-224),
+    since det X_R is the Slater expectation of exp(i alpha N_R) of species a and
+    its conjugate that of exp(-i alpha N_R) of species b."""
+    if model.Ns > 12:
+        raise ValueError(f"Fock-space sum needs Ns <= 12, got {model.Ns}")
+    occ = _occupations(_basis(model.Ns, model.Ns // 2), model.Ns)
+    m = occ[:, None, :] - occ[None, :, :]
+    γ, η = np.asarray(model.γ), np.asarray(model.η)
+
+    def V(l):
+        f = {d: np.sum(γ * np.exp(1j * model.α[l - 1] * η * d)) for d in (-1, 0, 1)}
+        return np.prod(np.select([m == -1, m == 0, m == 1], [f[-1], f[0], f[1]]), axis=2)
+
+    R, L, _ = tu_states(model, V)
+    nR = occ[:, list(region)].sum(axis=1)
+    D = np.exp(1j * alpha * (nR[:, None] - nR[None, :]))
+    return complex(np.vdot(L, D * R) / np.vdot(L, R))

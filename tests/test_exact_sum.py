@@ -162,3 +162,30 @@ def test_scee_estimator_converges_to_exact_replica_ratio():
     mu, se = np.mean(means), np.std(means, ddof=1) / np.sqrt(len(means))
     assert abs(mu - exact) < 5 * se, (mu, se, exact)
     assert se < 0.1 * exact
+
+
+def test_dop_estimator_converges_to_exact_disorder_ratio():
+    """ctrl_SCDOPicr restated, lambda = 0, N_lambda = 1: the chain is weighted by
+    |det X_B|^2 and averages |det X_A|^2 / |det X_B|^2, whose exact value is
+    <exp(i alpha (N_a,A - N_b,A))> / <... B ...> in the sweep's two-species
+    state (fock_oracle.tu_disorder); at U = 0 the exact sum is the Slater
+    value |det X_A|^2."""
+    import scee_oracle as S
+    m = cases.tu_hc8()
+    A, B, alpha = [0, 1, 2, 3], [0, 1], 1.0
+    m0 = cases.tu_hc8(U=0.0)
+    G = np.eye(m0.Ns) - m0.Pt @ np.linalg.inv(m0.Pt.conj().T @ m0.Pt) @ m0.Pt.conj().T
+    e = np.exp(1j * alpha)
+    X = e * np.eye(4) + (1 - e) * G[np.ix_(A, A)]
+    assert abs(F.tu_disorder(m0, A, alpha) - abs(np.linalg.det(X)) ** 2) < 1e-9
+    exact = (F.tu_disorder(m, A, alpha) / F.tu_disorder(m, B, alpha)).real
+    means = []
+    for c in range(8):
+        sweeps = 120
+        ks, us = zip(*(philox.tape(8, c, w, 2 * m.Ns * m.Nt) for w in range(sweeps)))
+        ref = S.DOP(m, Initial_s(m, 400 + c), alpha, [a + 1 for a in A], [b + 1 for b in B], 0.0, 1,
+                    O.Tape(np.concatenate(ks), np.concatenate(us))).run(sweeps)
+        means.append(np.mean(ref.O[20:]))
+    mu, se = np.mean(means), np.std(means, ddof=1) / np.sqrt(len(means))
+    assert abs(mu - exact) < 5 * se, (mu, se, exact)
+    assert se < 0.02
