@@ -42,3 +42,20 @@ def test_every_entry_point_is_mapped_in_the_integration_guide():
     guide = (HEADER.parent.parent / "INTEGRATION.md").read_text()
     missing = [n for n in declared() if f"`{n}`" not in guide and n not in guide]
     assert not missing, missing
+
+
+def _prototypes():
+    """name -> number of parameters of every kdq_ function the header declares."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(kdq_\w+)\s*\(([^;{)]*)\)\s*;", text):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_header_arity():
+    protos = _prototypes()
+    assert set(protos) == set(_lib._SIGS), set(protos) ^ set(_lib._SIGS)
+    wrong = {n: (k, len(_lib._SIGS[n][1])) for n, k in protos.items() if k != len(_lib._SIGS[n][1])}
+    assert not wrong, wrong
