@@ -59,3 +59,26 @@ def test_ctypes_signatures_match_header_arity():
     assert set(protos) == set(_lib._SIGS), set(protos) ^ set(_lib._SIGS)
     wrong = {n: (k, len(_lib._SIGS[n][1])) for n, k in protos.items() if k != len(_lib._SIGS[n][1])}
     assert not wrong, wrong
+
+
+def test_julia_binding_ccalls_match_header_arity():
+    """Julia is not installed here, so its binding is checked as text: every
+    ccall names a declared entry point with the header's parameter count."""
+    src = (HEADER.parent.parent / "julia" / "KAPDQMCGPU" / "src" / "KAPDQMCGPU.jl").read_text()
+    protos = _prototypes()
+    calls = re.findall(r"ccall\(\(:(kdq_\w+),\s*libkdq\),\s*\w+,\s*\(([^()]*)\)", src, re.S)
+    assert len(calls) >= 20
+    for name, types in calls:
+        depth, count, cur = 0, 0, ""
+        for ch in types + ",":
+            if ch == "{":
+                depth += 1
+            elif ch == "}":
+                depth -= 1
+            if ch == "," and depth == 0:
+                count += bool(cur.strip())
+                cur = ""
+            else:
+                cur += ch
+        assert name in protos, name
+        assert count == protos[name], (name, count, protos[name])
