@@ -69,9 +69,12 @@ def hop_op(i: int, j: int, basis) -> np.ndarray:
     return out
 
 
-def _two_species(model, V, ek_sign):
-    """<Ek>, <Eu> of a two-species sweep with weight |det|^2: V(l) is the
-    diagonal field-summed interaction of slice l over (a state, b state)."""
+def _two_species(model, V, ek_sign, same_species=False):
+    """<Ek>, <Eu> of a two-species sweep: V(l) is the diagonal field-summed
+    interaction of slice l over (a state, b state).  Eu is
+    sum_i <n_ai (1 - n_bi)> for |det|^2 weights (species b the conjugate of a,
+    whose per-sample estimator is (1 - G_ii) conj(G_ii)) or, with
+    same_species, sum_i <n_ai n_bi> for det^2 weights (estimator (1 - G_ii)^2)."""
     Ns, Nt = model.Ns, model.Nt
     if Ns > 12:
         raise ValueError(f"Fock-space sum needs Ns <= 12, got {Ns}")
@@ -107,8 +110,8 @@ def _two_species(model, V, ek_sign):
             g = (1.0 if i == j else 0.0) - expect(hop_op(j, i, basis) @ R1)
             Ek += K[i, j] * g
     Ek = ek_sign * 2 * model.Ht * Ek.real
-    nb1 = 1.0 - occ                                       # 1 - n_b, per b state
-    Eu = sum(expect((occ[:, i][:, None] * nb1[:, i][None, :]) * R1) for i in range(Ns))
+    nb = occ if same_species else 1.0 - occ               # n_b or 1 - n_b, per b state
+    Eu = sum(expect((occ[:, i][:, None] * nb[:, i][None, :]) * R1) for i in range(Ns))
     return float(Ek), float(np.real(Eu))
 
 
@@ -139,7 +142,7 @@ def tu_exact(model):
 
 
 def tuv_exact(model):
-    """Exact <Ek> and <Eu> / U of the complex t-UV sweep at tau = Nt/2.
+    """Exact <Ek> and <Eu> / U of the t-UV sweep at tau = Nt/2.
 
     One field per bond (x, y) and slice multiplies species a by
     exp(i eta (n_x + a n_y)) and species b by its conjugate
@@ -149,19 +152,23 @@ def tuv_exact(model):
     Re sum_i <n_ai (1 - n_bi)> (the sweep's Ek and Eu / U,
     src/tUV/phy_update.jl:205-235).
     """
-    if not model.is_complex:
-        raise ValueError("the real t-UV sweep weighs det^2 with extra factors; only the complex one is summed")
     occ = _occupations(_basis(model.Ns, model.Ns // 2), model.Ns)
     nn = np.asarray(model.nnidx)
     X = nn[:, :, 0].ravel(order="F") - 1
     Y = nn[:, :, 1].ravel(order="F") - 1
     γ, η = np.asarray(model.γ), np.asarray(model.η)
     qa = occ[:, X] + model.a * occ[:, Y]                  # per a state and bond
-    m = qa[:, None, :] - qa[None, :, :]                   # (Sa, Sb, bonds)
-    f = np.tensordot(np.exp(1j * m[..., None] * η), γ, axes=([3], [0]))
+    if model.is_complex:
+        m = qa[:, None, :] - qa[None, :, :]               # (Sa, Sb, bonds)
+        f = np.tensordot(np.exp(1j * m[..., None] * η), γ, axes=([3], [0]))
+    else:
+        # real sweep: both species see exp(+eta (n_x + a n_y)) and each field
+        # carries exp(-(a + 1) eta) (src/tUV/phy_update.jl:195-197), weight det^2
+        m = qa[:, None, :] + qa[None, :, :]
+        f = np.tensordot(np.exp(m[..., None] * η), γ * np.exp(-(model.a + 1.0) * η), axes=([3], [0]))
     Vc = np.prod(f, axis=2)                               # the same for every slice
 
-    return _two_species(model, lambda l: Vc, 1.0)
+    return _two_species(model, lambda l: Vc, 1.0, same_species=not model.is_complex)
 
 
 def tv_exact(model):

@@ -118,3 +118,9 @@ def tv_hc8(V=1.0):
 def tuv_hc8():
     return tUV_Hubbard_Para(Ht=1.0, Hu=4.0, Hv=0.5, Lattice="HoneyComb120", site=[2, 2], Δt=0.1, Θ=1.0,
                             BatchSize=5, Initial="H0")
+
+
+def tuv_hc8_real():
+    # U < 0: the real t-UV sweep (det^2 weights with the exp(-(a+1) eta) field factor)
+    return tUV_Hubbard_Para(Ht=1.0, Hu=-4.0, Hv=0.3, Lattice="HoneyComb120", site=[2, 2], Δt=0.1, Θ=1.0,
+                            BatchSize=5, Initial="H0")

@@ -2,13 +2,14 @@
 weights (a known-answer test that does not share the oracle's arithmetic).
 
 oracle/fock_oracle.py sums the sweep's weights over every HS field exactly,
-in the Fock space of an 8-site lattice (two species for t-U and complex
-t-UV, one for t-V), and returns the expectation of the sweep's per-sample
+in the Fock space of an 8-site lattice (two species for t-U and t-UV,
+one for t-V), and returns the expectation of the sweep's per-sample
 energy estimators at tau = Nt/2.  The oracle's chains must reproduce it
 within five standard errors (independent chains, so the error bar is the
 spread of the chain means).
 """
 import numpy as np
+import pytest
 
 import cases
 import dqmc_oracle as O
@@ -60,8 +61,9 @@ def test_tv_free_limit_and_oracle_chains():
     assert abs(Ev0 - Ev) > 10 * se[1]
 
 
-def test_tuv_oracle_chains():
-    model = cases.tuv_hc8()
+@pytest.mark.parametrize("make", [cases.tuv_hc8, cases.tuv_hc8_real])
+def test_tuv_oracle_chains(make):
+    model = make()
     Ek, Eu = F.tuv_exact(model)
     mu, se = _chains(model, 6, 50, [0, 1], scale=(1.0, model.U))
     assert abs(mu[0] - Ek) < 5 * se[0], (mu, se, Ek)
