@@ -422,3 +422,50 @@ def tu_disorder(model, region, alpha: float):
     nR = occ[:, list(region)].sum(axis=1)
     D = np.exp(1j * alpha * (nR[:, None] - nR[None, :]))
     return complex(np.vdot(L, D * R) / np.vdot(L, R))
+
+
+def tu_structure_factors(model):
+    """Exact CDW0, CDW1, SDW0, SDW1 of the t-U honeycomb sweep's measurement
+    with every term (the estimator kdq_set_measure_full adds): with
+    n_up = n_a and n_dn = 1 - n_b (species b is the particle-hole conjugate of
+    spin down), rho = n_up + n_dn and m = n_up - n_dn, and for cells c1, c2 with
+    A and B sites, CDW = sum_{c1,c2} w(c2 - c1) <(rho_A1 - rho_B1)(rho_A2 - rho_B2)> / Ns^2
+    (SDW with m), w = 1 (…0) or cos(2 pi rx / L1 + 2 pi ry / L2) (…1); the
+    reference's correlators, src/tU/phy_update.jl:194-235, with their
+    discarded +adjoint terms restored."""
+    Ns = model.Ns
+    if Ns > 12:
+        raise ValueError(f"Fock-space sum needs Ns <= 12, got {Ns}")
+    basis = _basis(Ns, Ns // 2)
+    occ = _occupations(basis, Ns)
+    m = occ[:, None, :] - occ[None, :, :]
+    γ, η = np.asarray(model.γ), np.asarray(model.η)
+
+    def V(l):
+        f = {d: np.sum(γ * np.exp(1j * model.α[l - 1] * η * d)) for d in (-1, 0, 1)}
+        return np.prod(np.select([m == -1, m == 0, m == 1], [f[-1], f[0], f[1]]), axis=2)
+
+    R, L, _ = tu_states(model, V)
+    Ha, Hb = gamma_op(model.HalfeK, basis), gamma_op(model.HalfeK.conj(), basis)
+    Hia, Hib = gamma_op(model.HalfeKinv, basis), gamma_op(model.HalfeKinv.conj(), basis)
+    R1 = Ha @ R @ Hb.T
+    L1 = Hia.conj().T @ L @ Hib.conj()
+    norm = np.vdot(L1, R1)
+    nup = occ[:, None, :]                       # (Sa, 1, site)
+    ndn = 1.0 - occ[None, :, :]                 # (1, Sb, site)
+    L1_, L2_ = model.site
+    cells = {(ix, iy): 2 * (ix + (iy - 1) * L1_) - 2 for ix in range(1, L1_ + 1) for iy in range(1, L2_ + 1)}
+    out = []
+    for sgn in (1.0, -1.0):                     # charge, then spin
+        dens = nup + sgn * ndn                   # (Sa, Sb, site)
+        stag = {c: dens[..., a] - dens[..., a + 1] for c, a in cells.items()}
+        s0 = s1 = 0.0
+        for (ix, iy), d1 in stag.items():
+            for rx in range(1, L1_ + 1):
+                for ry in range(1, L2_ + 1):
+                    c2 = ((ix + rx - 1) % L1_ + 1, (iy + ry - 1) % L2_ + 1)
+                    v = np.vdot(L1, d1 * stag[c2] * R1) / norm
+                    s0 += v
+                    s1 += np.cos(2 * np.pi / L1_ * rx + 2 * np.pi / L2_ * ry) * v
+        out += [float(np.real(s0)) / Ns ** 2, float(np.real(s1)) / Ns ** 2]
+    return out[0], out[1], out[2], out[3]

@@ -1,5 +1,11 @@
+import os
 import sys
 from pathlib import Path
+
+# the oracle works on small matrices, where BLAS threads cost more than they
+# save; set before numpy is first imported
+for _v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+    os.environ.setdefault(_v, "1")
 
 ROOT = Path(__file__).resolve().parent.parent
 for p in (ROOT, ROOT / "oracle"):

@@ -191,3 +191,24 @@ def test_dop_estimator_converges_to_exact_disorder_ratio():
     mu, se = np.mean(means), np.std(means, ddof=1) / np.sqrt(len(means))
     assert abs(mu - exact) < 5 * se, (mu, se, exact)
     assert se < 0.02
+
+
+def test_full_structure_factors_converge_to_exact_correlations():
+    """The structure factors with every term (kdq_set_measure_full; the
+    oracle's full_sf) average to the staggered charge and spin correlations
+    of the exact state: CDW = sum_{c1,c2} w <(rho_A1 - rho_B1)(rho_A2 - rho_B2)> / Ns^2
+    with rho = n_up + n_dn (SDW with n_up - n_dn)."""
+    m = cases.tu_hc8()
+    exact = np.array(F.tu_structure_factors(m))
+    n = O.proposals_per_sweep(m)
+    means = []
+    for c in range(12):
+        sweeps = 150
+        ks, us = zip(*(philox.tape(77, c, w, n) for w in range(sweeps)))
+        sw = O.phy_update(m, Initial_s(m, 700 + c), sweeps, O.Tape(np.concatenate(ks), np.concatenate(us)),
+                          True, full_sf=True)
+        means.append(np.array(sw.obs_rows)[20:, 6:10].mean(0))
+    means = np.array(means)
+    mu, se = means.mean(0), means.std(0, ddof=1) / np.sqrt(len(means))
+    assert np.all(np.abs(mu - exact) < 5 * se), (mu, se, exact)
+    assert np.all(se < 0.1 * np.abs(exact))
