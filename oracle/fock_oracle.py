@@ -171,22 +171,18 @@ def tuv_exact(model):
     return _two_species(model, lambda l: Vc, 1.0, same_species=not model.is_complex)
 
 
-def tv_exact(model):
-    """Exact <Ek> and <Ev> of the t-V sweep's measurement at tau = Nt/2.
-
-    One fermion species with weight prod(gamma) det(P^H B P),
-    B_l = prod_j (UV_j D_j UV_j) eK (src/tV/GreenMatrix.jl:12-38): a bond
-    (x, y) of direction j acts on its two sites by
-    UV diag(exp(alpha eta), exp(-alpha eta)) UV, UV = [-c -c; -c c], c = 1/sqrt 2,
-    and its field sum is sum_k gamma_k Gamma(that matrix) in Fock space.
-    Returns Ht sum K .* <c c^dagger> and sum_bonds <n_x n_y>, the
-    expectations of the sweep's Ek and Ev (src/tV/phy_update.jl:207-262).
-    """
+def tv_states(model):
+    """(R1, L1, basis): the t-V sweep's one-species states at tau = Nt/2 with
+    the HalfeK symmetrisation of the measurement, R1 = A T_h .. T_1 |Psi>,
+    L1 = (A^-1)^H T_{h+1}^H .. T_Nt^H |Psi>, A = Gamma(HalfeK).  A bond (x, y)
+    of direction j acts on its two sites by UV diag(exp(alpha eta),
+    exp(-alpha eta)) UV, UV = [-c -c; -c c], c = 1/sqrt 2, and its field sum is
+    sum_k gamma_k Gamma(that matrix); B_l = prod_j (UV_j D_j UV_j) eK
+    (src/tV/GreenMatrix.jl:12-38)."""
     Ns, Nt = model.Ns, model.Nt
     if Ns > 12:
         raise ValueError(f"Fock-space sum needs Ns <= 12, got {Ns}")
     basis = _basis(Ns, Ns // 2)
-    occ = _occupations(basis, Ns)
     nn = np.asarray(model.nnidx)
     γ, η = np.asarray(model.γ), np.asarray(model.η)
     c = 2 ** 0.5 / 2
@@ -228,8 +224,18 @@ def tv_exact(model):
     for l in range(Nt, h, -1):
         L = E.conj().T @ (Vl(l).conj().T @ L)
         L /= np.linalg.norm(L)
-    norm = np.vdot(L, R)
-    R1, L1 = H @ R, Hi.conj().T @ L
+    return H @ R, Hi.conj().T @ L, basis
+
+
+def tv_exact(model):
+    """Exact <Ek> and <Ev> of the t-V sweep's measurement at tau = Nt/2: one
+    fermion species with weight prod(gamma) det(P^H B P) (see tv_states).
+    Returns Ht sum K .* <c c^dagger> and sum_bonds <n_x n_y>, the
+    expectations of the sweep's Ek and Ev (src/tV/phy_update.jl:207-262)."""
+    Ns = model.Ns
+    R1, L1, basis = tv_states(model)
+    occ = _occupations(basis, Ns)
+    norm = np.vdot(L1, R1)
 
     def expect(v):
         return np.vdot(L1, v) / norm
@@ -242,10 +248,35 @@ def tv_exact(model):
                 continue
             g = (1.0 if i == j else 0.0) - expect(hop_op(j, i, basis) @ R1)
             Ek += K[i, j] * g
+    nn = np.asarray(model.nnidx)
     x = nn[:, :, 0].ravel() - 1
     y = nn[:, :, 1].ravel() - 1
     Ev = expect((occ[:, x] * occ[:, y]).sum(axis=1) * R1)
     return float(np.real(model.Ht * Ek)), float(np.real(Ev))
+
+
+def tv_structure_factors(model):
+    """Exact R0[4], R1[4] of the t-V honeycomb measurement: for cells c1, c2
+    and the sublattice pairs (A,A), (B,B), (B1,A2), (A1,B2),
+    4 / Ns^2 sum_{c1,c2} w <n_X1 n_Y2> with w = 1 (R0) or
+    cos(2 pi rx / L1 + 2 pi ry / L2) (R1) (src/tV/phy_update.jl:268-294)."""
+    R1, L1, basis = tv_states(model)
+    occ = _occupations(basis, model.Ns)
+    norm = np.vdot(L1, R1)
+    L1_, L2_ = model.site
+    cells = {(ix, iy): 2 * (ix + (iy - 1) * L1_) - 2 for ix in range(1, L1_ + 1) for iy in range(1, L2_ + 1)}
+    R0, Rq = np.zeros(4), np.zeros(4)
+    for (ix, iy), a1 in cells.items():
+        for rx in range(1, L1_ + 1):
+            for ry in range(1, L2_ + 1):
+                a2 = cells[((ix + rx - 1) % L1_ + 1, (iy + ry - 1) % L2_ + 1)]
+                b1, b2 = a1 + 1, a2 + 1
+                ph = np.cos(2 * np.pi / L1_ * rx + 2 * np.pi / L2_ * ry)
+                for k, (p, q) in enumerate(((a1, a2), (b1, b2), (b1, a2), (a1, b2))):
+                    v = np.real(np.vdot(L1, occ[:, p] * occ[:, q] * R1) / norm)
+                    R0[k] += v
+                    Rq[k] += ph * v
+    return R0 * 4 / model.Ns ** 2, Rq * 4 / model.Ns ** 2
 
 
 def hubbard_ground_state(model, U: float):

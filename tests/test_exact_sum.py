@@ -26,14 +26,14 @@ def test_free_limit_is_exact():
     assert abs(Eu - model.Ns / 4) < 1e-9        # <n_up n_dn> = 1/4 per site
 
 
-def _chains(model, nch, sweeps, cols, scale=(1.0, 1.0)):
+def _chains(model, nch, sweeps, cols, scale=None):
     n = O.proposals_per_sweep(model)
     means = []
     for c in range(nch):
         ks, us = zip(*(philox.tape(21, c, w, n) for w in range(sweeps)))
         sw = O.phy_update(model, Initial_s(model, 500 + c), sweeps,
                           O.Tape(np.concatenate(ks), np.concatenate(us)), True)
-        means.append(np.array(sw.obs_rows)[10:, cols].mean(0) / np.array(scale))
+        means.append(np.array(sw.obs_rows)[10:, cols].mean(0) / (np.array(scale) if scale else 1.0))
     means = np.array(means)
     return means.mean(0), means.std(0, ddof=1) / np.sqrt(len(means))
 
@@ -50,14 +50,17 @@ def test_oracle_chains_reproduce_exact_sum():
 
 
 def test_tv_free_limit_and_oracle_chains():
+    """t-V: the free limit, then Ek, Ev and the density structure factors
+    R0, R1 (src/tV/phy_update.jl:268-294) of the oracle's chains."""
     Ek0, Ev0 = F.tv_exact(cases.tv_hc8(V=0.0))
     m0 = cases.tv_hc8(V=0.0)
     assert abs(Ek0 - np.linalg.eigvalsh(-m0.Ht * m0.K)[: m0.Ns // 2].sum()) < 1e-6
     model = cases.tv_hc8()
     Ek, Ev = F.tv_exact(model)
-    mu, se = _chains(model, 8, 60, [0, 1])
-    assert abs(mu[0] - Ek) < 5 * se[0], (mu, se, Ek)
-    assert abs(mu[1] - Ev) < 5 * se[1], (mu, se, Ev)
+    R0, R1 = F.tv_structure_factors(model)
+    want = np.concatenate([[Ek, Ev], R0, R1])
+    mu, se = _chains(model, 8, 60, list(range(10)))
+    assert np.all(np.abs(mu - want) < 5 * se + 1e-12), (mu, se, want)
     assert abs(Ev0 - Ev) > 10 * se[1]
 
 
