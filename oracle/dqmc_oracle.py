@@ -11,7 +11,11 @@ reference's consumption order instead of an unseedable MersenneTwister.
 
 Parity is unpinned: the reference is Julia (not installed here) and ships no
 golden vectors; this restatement is checked by invariants instead (the
-brute-force ``Gτ`` recompute, free-fermion energies, eK*eKinv = I).
+brute-force ``Gτ`` recompute, free-fermion energies, eK*eKinv = I) and by
+known answers that share none of its arithmetic: on 8-site lattices its
+chains reproduce the exact Fock-space sums of the same weights
+(fock_oracle.py; energies, structure factors, Rényi-2 and disorder ratios),
+and those sums converge to exact diagonalisation of the Hamiltonians.
 
 References (KAPDQMC): src/tU/phy_update.jl, src/tU/GreenMatrix.jl,
 src/tV/phy_update.jl, src/tV/GreenMatrix.jl, src/tUV/phy_update.jl,
