@@ -242,7 +242,7 @@ int kdq_set_precision(kdq_handle* h, int32_t mode);
  * chain, [4] Householder QR, [5] G recompute, [6] self-learning cluster
  * moves, [7] acceptance ratios of the mixed-precision sweep (the serial part
  * of each local proposal, up to the barrier that publishes its decision; the
- * FP64 sweep overlaps them with the G updates and counts both in [1]);
+ * FP64 sweep evaluates them in windows of proposals and counts them in [1]);
  * cycles has 8 entries.  Enabling resets the counters and adds a barrier
  * per stage.  No counterpart in the reference (which has no tracing). */
 int kdq_enable_phase_timing(kdq_handle* h, int32_t enable);

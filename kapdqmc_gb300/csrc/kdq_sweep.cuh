@@ -70,8 +70,8 @@ __device__ inline void gemm_thin(int M, int N, int K, const TA* A, int lda, cons
 // barriers): 0 wraps, 1 G updates and the proposals' bookkeeping, 2
 // measurements, 3 block products of the stabilisation chain, 4 Householder
 // QR, 5 G recompute, 6 cluster moves, 7 acceptance ratios of the FP32
-// working-precision sweep (the FP64 sweep overlaps them with the updates and
-// counts both in 1).
+// working-precision sweep (the FP64 sweep evaluates them in windows of
+// proposals and counts them in 1).
 struct PhaseClock {
   unsigned long long* acc;
   long long t;
