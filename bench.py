@@ -213,9 +213,9 @@ def _cpu_worker(args):
     """One chain of the workload through the C restatement of the reference sweep."""
     seed, chain, sweeps = args
     sys.path.insert(0, str(ROOT / "oracle"))
-    import cport_tv
+    import cport
     if sweeps == 0:                       # warm-up: load the library only
-        cport_tv.load()
+        cport.load()
         return 0.0
     import dqmc_oracle as O
     import philox
@@ -224,9 +224,9 @@ def _cpu_worker(args):
     s = Initial_s(model, 1000 + chain)
     n = O.proposals_per_sweep(model)
     ks, us = zip(*(philox.tape(seed, chain, w, n) for w in range(sweeps)))
-    cport_tv.load()
+    cport.load()
     t0 = time.perf_counter()
-    cport_tv.tv_phy_update(model, s, sweeps, np.concatenate(ks), np.concatenate(us), record=True)
+    cport.tv_phy_update(model, s, sweeps, np.concatenate(ks), np.concatenate(us), record=True)
     return time.perf_counter() - t0
 
 
@@ -242,8 +242,8 @@ class CpuArm:
     def __init__(self, cores: int):
         import multiprocessing as mp
         sys.path.insert(0, str(ROOT / "oracle"))
-        import cport_tv
-        cport_tv.build()
+        import cport
+        cport.build()
         self.cores = cores
         saved = {v: os.environ.get(v) for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
         for v in saved:                     # inherited by the workers before numpy loads

@@ -217,9 +217,12 @@ int kdq_grover_det_middle(kdq_handle* h, const int32_t* index, int32_t nA, doubl
  * GPU, shared by all calls: requests needing more (npairs * (3 nA^2 elements
  * + nA ints) plus nA ints, with 256-byte padding) fail with KDQ_ERR_ARG, and
  * calls that overlap on the GPU race on the array.  Region indices outside
- * 1..Ns give NaN determinants.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
- * Errors are reported through kdq_last_error(NULL). */
+ * 1..Ns give NaN determinants.  Every call whose stream is not capturing
+ * looks up the array's device address (again after a cudaDeviceReset, which
+ * can move it); a call inside a stream capture reuses the address of the
+ * device's last uncaptured call, so make the first call on a device before
+ * any stream capture, and one more after a cudaDeviceReset.  Errors are
+ * reported through kdq_last_error(NULL). */
 int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32_t npairs,
                            const int32_t* index, int32_t nA, double* det, void* stream);
 

@@ -24,6 +24,7 @@ module KAPDQMCGPU
 
 using KAPDQMC
 using DelimitedFiles
+using Random
 
 const libkdq = get(ENV, "KAPDQMC_GPU_LIB",
                    joinpath(@__DIR__, "..", "..", "..", "kapdqmc_gb300", "libkapdqmc_gpu.so"))
@@ -168,6 +169,42 @@ function phy_update(path::String, model, s, Sweeps::Int64, record::Bool=false;
         destroy(h)
     end
     return s
+end
+
+"""
+    reference_tape(model, s, rng::AbstractRNG, Sweeps) -> (k, u)
+
+The proposal tape that the reference's own `phy_update` draws from `rng`
+over `Sweeps` sweeps of one chain with field `s`, for `phy_update(...;
+tape=(k, u))`: with `rng = MersenneTwister(seed)` patched into the
+reference's driver in place of its clock-seeded generator
+(src/tU/phy_update.jl:31, src/tV/phy_update.jl:25, src/tUV/phy_update.jl:24),
+both runs consume the same random stream and must make the same accept /
+reject decisions.  Each proposal of the reference takes exactly one
+`rand(rng, model.samplers_dict[s_i])` and then one `rand(rng)`, accepted or
+not (src/tU/phy_update.jl:259,262, src/tV/phy_update.jl:194,200,
+src/tUV/phy_update.jl:192,198), and a sweep makes 2 proposals per field
+entry (forward and backward over every slice).  Every sampler of
+`samplers_dict` (src/tU/model.jl:87-93) draws an index into the ascending
+3-element list of the values other than its key with the same call, so
+drawing through the sampler of key 1 consumes the stream exactly as the
+reference does whatever the current field; the drawn value v in {2, 3, 4}
+is index v - 2 of that list, which is the tape's choice index k (the k-th
+of {1,2,3,4} without the current value, ascending).  For a batch of chains,
+concatenate the chains' tapes chain by chain.  Not yet run: no Julia
+installation was available where this binding was written, so this helper
+is untested.
+"""
+function reference_tape(model, s, rng::AbstractRNG, Sweeps::Integer)
+    n = 2 * length(s) * Sweeps
+    k = Vector{UInt8}(undef, n)
+    u = Vector{Float64}(undef, n)
+    sp = model.samplers_dict[UInt8(1)]
+    for m in 1:n
+        k[m] = UInt8(rand(rng, sp) - 2)
+        u[m] = rand(rng)
+    end
+    return k, u
 end
 
 """

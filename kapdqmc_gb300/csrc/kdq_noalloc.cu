@@ -34,19 +34,29 @@ void* g_scratch_addr[KDQ_NOALLOC_MAX_DEVICES] = {};
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// Device address of the scratch array for the current device, looked up once
-// per device (host code cannot use the array's name as a device pointer).
-cudaError_t scratch_for_current_device(void** out) {
+// Device address of the scratch array for the current device.  Host code
+// cannot use the array's name as a device pointer, so the address comes from
+// cudaGetSymbolAddress with the device current.  It is looked up again on
+// every call whose stream is not capturing (cudaDeviceReset reloads the
+// module, and the array may then sit at another address); while a stream
+// captures, the address from the device's last uncaptured call is used, so
+// the first call on a device has to come before any capture.
+cudaError_t scratch_for_current_device(cudaStream_t st, void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= KDQ_NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_grover_scratch);
     if (e != cudaSuccess) return e;
     g_scratch_addr[dev] = p;
+  } else if (!g_scratch_addr[dev]) {
+    return cudaErrorStreamCaptureUnsupported;
   }
   *out = g_scratch_addr[dev];
   return cudaSuccess;
@@ -98,8 +108,9 @@ extern "C" int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_com
                           " bytes (use fewer pairs per call)");
     return KDQ_ERR_ARG;
   }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
   void* base = nullptr;
-  cudaError_t e = scratch_for_current_device(&base);
+  cudaError_t e = scratch_for_current_device(st, &base);
   if (e != cudaSuccess) {
     kdq::set_global_error(std::string("kdq_grover_det_noalloc: scratch address: ") + cudaGetErrorString(e));
     return KDQ_ERR_CUDA;
@@ -109,7 +120,6 @@ extern "C" int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_com
   int* index0 = flag + 1;
   int* piv = reinterpret_cast<int*>(b + head);
   void* blocks = b + head + pivs;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   k_region_index<<<1, 256, 0, st>>>(index, nA, Ns, flag, index0);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = kdq::launch_grover(G, Ns, g_complex != 0, index0, nA, npairs, blocks, piv, det, st);

@@ -1,4 +1,4 @@
-// Coupled incremental SCEE sweep (t-U): ctrl_SCEEicr, src/tU/SCEE.jl:1-287.
+// Coupled incremental SCEE sweep (t-U): ctrl_SCEEicr, src/tU/SCEE.jl:1-324.
 //
 // One CTA per replica pair (chains 2p and 2p+1 of the handle), one launch
 // per stabilisation block, like the plain sweep.  Each replica keeps four
@@ -315,7 +315,7 @@ __device__ __noinline__ double scee_grover(Ctx<KIND, T, KT, T, KT>& c, const T* 
   gj_inverse(n, inv, fcol, c.piv, &bad, &lg, &ph);
   if (threadIdx.x == 0 && bad) atomicOr(&c.ctl->err, KDQ_FLAG_SINGULAR);
   if constexpr (KIND == KDQ_TV) return ph.x * exp(lg);   // det g itself (src/tV/SCEE.jl:437)
-  return exp(2.0 * lg);                                   // |det g|^2 (src/tU/SCEE.jl:267)
+  return exp(2.0 * lg);                                   // |det g|^2 (src/tU/SCEE.jl:268)
 }
 
 // Disorder-operator matrix X = e^{i alpha} I + (1 - e^{i alpha}) G0[R,R] of a
@@ -406,7 +406,7 @@ __device__ void scee_wrap(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, int
 }
 
 // One proposal of replica r (0 or 1) at site i of slice lt (UpdateSCEELayer!,
-// src/tU/SCEE.jl:230-287); co / qo: the other replica.
+// src/tU/SCEE.jl:278-324); co / qo: the other replica.
 template <int MAXRM, int KIND, class T, class KT>
 __device__ void scee_propose(Ctx<KIND, T, KT, T, KT>& c, const SceeChain<T>& q, const SceeChain<T>& qo, int r,
                              int lt, int i, int kk, double u, long long logpos, SceeSmem<T>& ss, int pair) {

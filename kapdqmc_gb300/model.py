@@ -21,7 +21,7 @@ import numpy as np
 
 from .geometry import LATTICES, nnK_Matrix, nnidx_F
 
-# 4-valued SU(2) Hubbard-Stratonovich constants, src/tU/model.jl:108-109
+# 4-valued SU(2) Hubbard-Stratonovich constants, src/tU/model.jl:55-56
 _S6 = math.sqrt(6.0)
 GAMMA = np.array([1 + _S6 / 3, 1 + _S6 / 3, 1 - _S6 / 3, 1 - _S6 / 3])
 ETA = np.array([math.sqrt(2 * (3 - _S6)), -math.sqrt(2 * (3 - _S6)),
@@ -31,7 +31,7 @@ KIND_TU, KIND_TV, KIND_TUV = 0, 1, 2
 
 
 def _nodes(Nt: int, BatchSize: int) -> np.ndarray:
-    """Stabilisation nodes, symmetric about Nt/2.  src/tU/model.jl:134-138."""
+    """Stabilisation nodes, symmetric about Nt/2.  src/tU/model.jl:81-85."""
     half = Nt // 2
     if half % BatchSize == 0:
         return np.arange(0, Nt + 1, BatchSize, dtype=np.int64)
@@ -49,7 +49,7 @@ def _linrange(a: float, b: float, n: int) -> np.ndarray:
 def _profile(H1: float, H2: float, Θrelax: float, Θquench: float, Δt: float, Nt: int):
     """Interaction strength per slice, constant or a symmetric quench ramp.
 
-    src/tU/model.jl:94-105 (tU) and src/tV/model.jl:79-90 (tV).
+    src/tU/model.jl:41-52 (tU) and src/tV/model.jl:79-90 (tV).
     """
     if Θquench > 0.0 and abs(H1 - H2) > 0:
         ramp = _linrange(H1, H2, round(Θquench / Δt) + 1)[1:]
@@ -69,7 +69,7 @@ def _profile(H1: float, H2: float, Θrelax: float, Θquench: float, Δt: float, 
 def _kinetic(HK: np.ndarray, Δt: float):
     """HalfeK, eK, HalfeKinv, eKinv from the eigendecomposition of HK.
 
-    src/tU/model.jl:114-119 (``syevd`` then ``V * Diagonal(exp(..)) * V'``).
+    src/tU/model.jl:61-66 (``syevd`` then ``V * Diagonal(exp(..)) * V'``).
     """
     E, V = np.linalg.eigh(HK)
     Vh = V.conj().T

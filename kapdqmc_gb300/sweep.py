@@ -11,6 +11,8 @@ src/tUV/phy_update.jl:1-186, src/KAPDQMC.jl:12-28.
 from __future__ import annotations
 
 import ctypes as C
+import decimal
+import math
 import os
 import threading
 
@@ -369,6 +371,36 @@ def grover_det(G1, G2, index, device: int = 0):
     return out.view(np.complex128)
 
 
+
+def julia_float(x) -> str:
+    """A Float64 as Julia's ``print`` writes it (what ``writedlm`` puts in
+    the reference's CSV files and ``$(x)`` in its file names): the shortest
+    round-trip digits, written plainly when the decimal point falls within
+    -4 < pt <= 6 digits of the first digit (whole values end in ".0"), else
+    as d.ddde<exp> with no exponent padding ("1.0e-5", "1.234567e6").  Julia
+    chooses this in Base.Ryu.writeshortest."""
+    x = float(x)
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "Inf" if x > 0 else "-Inf"
+    if x == 0.0:
+        return "-0.0" if math.copysign(1.0, x) < 0 else "0.0"
+    sign, digits, exp = decimal.Decimal(repr(x)).as_tuple()   # repr: shortest round-trip digits
+    full = "".join(map(str, digits))
+    d = full.rstrip("0")
+    exp += len(full) - len(d)                                    # trailing zeros move into the exponent
+    olength = len(d)
+    pt = exp + olength
+    neg = "-" if sign else ""
+    if -4 < pt <= 6 and not (pt >= olength and abs(math.fmod(abs(x) + 0.05, 10.0 ** (pt - olength)) - 0.05) > 0.05):
+        if pt <= 0:
+            return neg + "0." + "0" * (-pt) + d
+        if pt >= olength:
+            return neg + d + "0" * (pt - olength) + ".0"
+        return neg + d[:pt] + "." + d[pt:]
+    return neg + d[0] + "." + (d[1:] or "0") + "e" + str(pt - 1)
+
 # ------------------------------------------------------------------------
 # reference-shaped entry points
 # ------------------------------------------------------------------------
@@ -378,8 +410,7 @@ def _csv_name(path, model):
     src/tU/phy_update.jl:12-27, src/tV/phy_update.jl:10-23,
     src/tUV/phy_update.jl:13-22 (the tV/tUV square case is named "□").
     """
-    def f(x):  # Julia prints whole floats as 1.0
-        return repr(float(x))
+    f = julia_float
 
     site = "[" + ", ".join(str(int(v)) for v in model.site) + "]"
     if model.kind == KIND_TU:
@@ -407,13 +438,12 @@ def _append_csv(file, rows):
         lk = _CSV_LOCKS.setdefault(os.path.abspath(file), threading.Lock())
     with lk, open(file, "a") as io:
         for r in rows:
-            io.write(",".join(repr(float(v)) for v in r) + "\n")
+            io.write(",".join(julia_float(v) for v in np.ravel(r)) + "\n")
 
 
 def _scee_csv_name(path, model, nlam):
     """src/tU/SCEE.jl:16-32, src/tV/SCEE.jl:16-32."""
-    def f(x):
-        return repr(float(x))
+    f = julia_float
 
     site = "[" + ", ".join(str(int(v)) for v in model.site) + "]"
     if model.kind == KIND_TUV:   # src/tUV/SCEE.jl:16-26
@@ -467,8 +497,7 @@ def ctrl_SCEEicr(path, model, indexA, indexB, Sweeps: int, λ: float, Nλ: int, 
 
 def _dop_csv_name(path, model, nlam):
     """src/tU/disorder_operate.jl:15-31 (the quench variant keyed on a non-constant alpha profile)."""
-    def f(x):
-        return repr(float(x))
+    f = julia_float
 
     site = "[" + ", ".join(str(int(v)) for v in model.site) + "]"
     name = {"SQUARE90": "□90", "SQUARE45": "□45", "HoneyComb60": "HC", "HoneyComb120": "HC120"}[model.Lattice]

@@ -1,6 +1,7 @@
-"""ctypes driver of the C restatement of the t-V sweep (oracle/cport/kdq_cpu.c).
+"""ctypes driver of the C restatement of the t-V and t-U sweeps
+(oracle/cport/kdq_cpu.c).
 
-TEST INFRASTRUCTURE ONLY: the timed CPU baseline and its parity test.  The
+TEST INFRASTRUCTURE ONLY: the timed CPU baseline and its parity tests.  The
 BLAS/LAPACK it calls come from the OpenBLAS bundled with numpy.
 """
 from __future__ import annotations
@@ -44,6 +45,7 @@ def load():
         if lib.kdq_cpu_load_blas(openblas_path().encode()) != 0:
             raise RuntimeError("BLAS/LAPACK symbols not found in numpy's OpenBLAS")
         lib.kdq_cpu_tv_phy_update.restype = C.c_int
+        lib.kdq_cpu_tu_phy_update.restype = C.c_int
         _lib = lib
     return _lib
 
@@ -77,3 +79,28 @@ def tv_phy_update(model, s, sweeps, k, u, record=True, log=False):
         raise RuntimeError(f"kdq_cpu_tv_phy_update failed with {rc}")
     s_out = flat_s.reshape(model.field_shape, order="F")
     return s_out, obs.reshape(-1, 10)[:sweeps], acc
+
+
+def tu_phy_update(model, s, sweeps, k, u, record=True, log=False):
+    """Run the C restatement of the t-U sweep; returns (s, obs rows (sweeps, 6), accept log or None)."""
+    lib = load()
+    s = np.asfortranarray(np.array(s, dtype=np.uint8))
+    flat_s = np.ascontiguousarray(np.ravel(s, order="F"))
+    z = lambda m: np.ascontiguousarray(np.ravel(np.asarray(m, dtype=np.complex128), order="F")).view(np.float64)
+    mats = [z(model.eK), z(model.eKinv), z(model.HalfeK), z(model.HalfeKinv), z(model.K), z(model.Pt)]
+    nodes = np.ascontiguousarray(model.nodes, dtype=np.int64)
+    alpha, gamma, eta = (np.ascontiguousarray(x, dtype=np.float64) for x in (model.α, model.γ, model.η))
+    k = np.ascontiguousarray(k, dtype=np.uint8)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    obs = np.zeros(max(sweeps, 1) * 6)
+    acc = np.zeros(len(k), dtype=np.uint8) if log else None
+    hc = int("HoneyComb" in model.Lattice)
+    rc = lib.kdq_cpu_tu_phy_update(
+        C.c_int(model.Ns), C.c_int(model.Nt), C.c_int(len(nodes)), _p(nodes), _p(alpha), _p(gamma), _p(eta),
+        *(_p(m) for m in mats[:5]), C.c_double(model.Ht), _p(mats[5]), C.c_int(model.site[0]),
+        C.c_int(model.site[1]), C.c_int(hc), _p(flat_s), C.c_int(sweeps), C.c_int(int(record)), _p(k), _p(u),
+        C.c_size_t(len(k)), _p(obs), _p(acc) if log else None)
+    if rc != 0:
+        raise RuntimeError(f"kdq_cpu_tu_phy_update failed with {rc}")
+    s_out = flat_s.reshape(model.field_shape, order="F")
+    return s_out, obs.reshape(-1, 6)[:sweeps], acc

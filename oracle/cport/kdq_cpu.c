@@ -1,21 +1,28 @@
 /*
- * kdq_cpu.c — CPU restatement of the t-V projector-DQMC sweep, for timing.
+ * kdq_cpu.c — CPU restatement of the t-V and t-U projector-DQMC sweeps, for
+ * timing.
  *
- * TEST INFRASTRUCTURE ONLY: the CPU baseline of bench.py and a parity test
+ * TEST INFRASTRUCTURE ONLY: the CPU baseline of bench.py and parity tests
  * against the numpy oracle use it; the product never calls it.
  *
- * It follows the reference operation by operation, dense bond-rotation
- * GEMMs included, with the same BLAS/LAPACK routines (dgemm, dgerqf/dorgrq,
- * dgeqrf/dorgqr, dgetrf/dgetrs) taken at run time from an OpenBLAS shared
- * library (numpy's bundled ILP64 build), as Julia's LinearAlgebra does:
- *   phy_update          src/tV/phy_update.jl:1-188
- *   UpdatePhyLayer!     src/tV/phy_update.jl:190-205
- *   phy_measure         src/tV/phy_update.jl:207-314 (xy_i with 3 arguments)
- *   BM_F!, get_r!, WrapV!  src/tV/GreenMatrix.jl:12-38,76-89,99-119
- *   Gupdate!, get_G!    src/public/Gupdate.jl:5-11,139-157
+ * It follows the reference operation by operation (t-V: dense
+ * bond-rotation GEMMs included; t-U: complex eK, complex GEMMs), with the
+ * same BLAS/LAPACK routines (?gemm, ?gerqf/?orgrq|?ungrq, ?geqrf/?orgqr|
+ * ?ungqr, ?getrf/?getrs) taken at run time from an OpenBLAS shared library
+ * (numpy's bundled ILP64 build), as Julia's LinearAlgebra does:
+ *   t-V phy_update       src/tV/phy_update.jl:1-188
+ *       UpdatePhyLayer!  src/tV/phy_update.jl:190-205
+ *       phy_measure      src/tV/phy_update.jl:207-314 (xy_i with 3 arguments)
+ *       BM_F!, get_r!, WrapV!  src/tV/GreenMatrix.jl:12-38,76-89,99-119
+ *   t-U phy_update       src/tU/phy_update.jl:3-152
+ *       UpdatePhyLayer!  src/tU/phy_update.jl:256-267
+ *       phy_measure      src/tU/phy_update.jl:154-254
+ *       BM_F!, get_r!, WrapKV!  src/tU/GreenMatrix.jl:10-27,49-54,56-86
+ *   Gupdate!, get_G!     src/public/Gupdate.jl:5-11,139-157
  * The proposal stream is an explicit tape (choice index, uniform) in the
  * reference's consumption order.
  */
+#include <complex.h>
 #include <dlfcn.h>
 #include <math.h>
 #include <stdint.h>
@@ -41,6 +48,22 @@ static orgq_t p_dorgqr, p_dorgrq;
 static getrf_t p_dgetrf;
 static getrs_t p_dgetrs;
 
+typedef double _Complex zc;
+typedef void (*zgemm_t)(const char*, const char*, const bint*, const bint*, const bint*, const zc*, const zc*,
+                        const bint*, const zc*, const bint*, const zc*, zc*, const bint*);
+typedef void (*zqrf_t)(const bint*, const bint*, zc*, const bint*, zc*, zc*, const bint*, bint*);
+typedef void (*zungq_t)(const bint*, const bint*, const bint*, zc*, const bint*, const zc*, zc*, const bint*,
+                        bint*);
+typedef void (*zgetrf_t)(const bint*, const bint*, zc*, const bint*, bint*, bint*);
+typedef void (*zgetrs_t)(const char*, const bint*, const bint*, const zc*, const bint*, const bint*, zc*,
+                         const bint*, bint*);
+
+static zgemm_t p_zgemm;
+static zqrf_t p_zgeqrf, p_zgerqf;
+static zungq_t p_zungqr, p_zungrq;
+static zgetrf_t p_zgetrf;
+static zgetrs_t p_zgetrs;
+
 static void* sym(void* h, const char* base) {
   char name[64];
   const char* forms[] = {"scipy_%s_64_", "%s_64_", "%s_"};
@@ -63,7 +86,15 @@ int kdq_cpu_load_blas(const char* path) {
   p_dorgrq = (orgq_t)sym(h, "dorgrq");
   p_dgetrf = (getrf_t)sym(h, "dgetrf");
   p_dgetrs = (getrs_t)sym(h, "dgetrs");
-  return !(p_dgemm && p_dgeqrf && p_dgerqf && p_dorgqr && p_dorgrq && p_dgetrf && p_dgetrs);
+  p_zgemm = (zgemm_t)sym(h, "zgemm");
+  p_zgeqrf = (zqrf_t)sym(h, "zgeqrf");
+  p_zgerqf = (zqrf_t)sym(h, "zgerqf");
+  p_zungqr = (zungq_t)sym(h, "zungqr");
+  p_zungrq = (zungq_t)sym(h, "zungrq");
+  p_zgetrf = (zgetrf_t)sym(h, "zgetrf");
+  p_zgetrs = (zgetrs_t)sym(h, "zgetrs");
+  return !(p_dgemm && p_dgeqrf && p_dgerqf && p_dorgqr && p_dorgrq && p_dgetrf && p_dgetrs && p_zgemm &&
+           p_zgeqrf && p_zgerqf && p_zungqr && p_zungrq && p_zgetrf && p_zgetrs);
 }
 
 /* C = A B, column-major, A m x k, B k x n */
@@ -390,6 +421,302 @@ int kdq_cpu_tv_phy_update(int Ns, int Nt, int z, int NN, const int64_t* nodes, c
     }
     if (record && obs)
       for (int q = 0; q < 10; ++q) obs[(size_t)w * 10 + q] = row[q] / counter;
+  }
+  if (S.tape_pos > tape_len) rc = 5;
+  free(mem);
+  free(S.ipiv);
+  return rc;
+}
+
+/* ======================================================================
+ * t-U (complex) sweep
+ * ====================================================================== */
+
+/* C = A B, complex, column-major */
+static void zmm(bint m, bint n, bint k, const zc* A, bint lda, const zc* B, bint ldb, zc* C, bint ldc) {
+  const zc one = 1.0, zero = 0.0;
+  p_zgemm("N", "N", &m, &n, &k, &one, A, &lda, B, &ldb, &zero, C, &ldc);
+}
+
+typedef struct {
+  int Ns, ns, Nt, NN, L1, L2, honeycomb;
+  const int64_t* nodes;
+  const double *alpha, *gamma, *eta;
+  const zc *eK, *eKinv, *HalfeK, *HalfeKinv, *K;
+  double Ht;
+  zc *G, *tmpNN, *BM, *BLs, *BRs, *tmpNn, *tmpnN, *tmpnn, *tmpN, *tau, *work, *G0, *zN, *gcol;
+  bint* ipiv;
+  bint lwork;
+  const uint8_t* tk;
+  const double* tu;
+  size_t tape_len, tape_pos;
+  uint8_t* acc_log;
+  size_t log_pos;
+} Su;
+
+/* tmpN[i] = cis(sign * alpha[lt] * eta[s[i, lt]]) (src/tU/phy_update.jl:61-63,123-125) */
+static void u_setD(Su* S, int lt, const uint8_t* s, double sign) {
+  const uint8_t* sl = s + (size_t)(lt - 1) * S->Ns;
+  for (int i = 0; i < S->Ns; ++i) S->tmpN[i] = cexp(I * (sign * S->alpha[lt - 1] * S->eta[sl[i] - 1]));
+}
+
+/* X[r, c] <- X[r, c] * D[c] after D <- 1 ./ D, from tmpNN = Diagonal(D) X */
+static void u_diag_both(Su* S, zc* X) {
+  const int N = S->Ns;
+  for (int c = 0; c < N; ++c)
+    for (int r = 0; r < N; ++r) S->tmpNN[r + (size_t)c * N] = S->tmpN[r] * X[r + (size_t)c * N];
+  for (int r = 0; r < N; ++r) S->tmpN[r] = 1.0 / S->tmpN[r];
+  for (int c = 0; c < N; ++c)
+    for (int r = 0; r < N; ++r) X[r + (size_t)c * N] = S->tmpNN[r + (size_t)c * N] * S->tmpN[c];
+}
+
+/* WrapKV!(.., "Forward", "B"), src/tU/GreenMatrix.jl:64-69 */
+static void u_wrap_fwd(Su* S, zc* X) {
+  const int N = S->Ns;
+  zmm(N, N, N, S->eK, N, X, N, S->tmpNN, N);
+  zmm(N, N, N, S->tmpNN, N, S->eKinv, N, X, N);
+  u_diag_both(S, X);
+}
+
+/* WrapKV!(.., "Backward", "B"), src/tU/GreenMatrix.jl:78-83 */
+static void u_wrap_bwd(Su* S, zc* X) {
+  const int N = S->Ns;
+  u_diag_both(S, X);
+  zmm(N, N, N, S->eKinv, N, X, N, S->tmpNN, N);
+  zmm(N, N, N, S->tmpNN, N, S->eK, N, X, N);
+}
+
+/* BM_F!, src/tU/GreenMatrix.jl:10-27 */
+static void u_BM_F(Su* S, const uint8_t* s, int idx) {
+  const int N = S->Ns;
+  memset(S->BM, 0, sizeof(zc) * N * N);
+  for (int i = 0; i < N; ++i) S->BM[i + (size_t)i * N] = 1.0;
+  for (int lt = (int)S->nodes[idx - 1] + 1; lt <= (int)S->nodes[idx]; ++lt) {
+    u_setD(S, lt, s, 1.0);
+    zmm(N, N, N, S->eK, N, S->BM, N, S->tmpNN, N);
+    for (int c = 0; c < N; ++c)
+      for (int r = 0; r < N; ++r) S->BM[r + (size_t)c * N] = S->tmpN[r] * S->tmpNN[r + (size_t)c * N];
+  }
+}
+
+/* get_G!, src/public/Gupdate.jl:139-157 */
+static int u_get_G(Su* S, const zc* BL, const zc* BR) {
+  const bint N = S->Ns, n = S->ns;
+  bint info;
+  zmm(n, n, N, BL, n, BR, N, S->tmpnn, n);
+  p_zgetrf(&n, &n, S->tmpnn, &n, S->ipiv, &info);
+  if (info) return 1;
+  memcpy(S->tmpnN, BL, sizeof(zc) * n * N);
+  p_zgetrs("N", &n, &N, S->tmpnn, &n, S->ipiv, S->tmpnN, &n, &info);
+  zmm(N, N, n, BR, N, S->tmpnN, n, S->G, N);
+  for (bint i = 0; i < N * N; ++i) S->G[i] = -S->G[i];
+  for (bint i = 0; i < N; ++i) S->G[i + i * N] += 1.0;
+  return 0;
+}
+
+static void u_orth_rows(Su* S, zc* A) { /* gerqf! + orgrq! on n x N */
+  const bint n = S->ns, N = S->Ns;
+  bint info;
+  p_zgerqf(&n, &N, A, &n, S->tau, S->work, &S->lwork, &info);
+  p_zungrq(&n, &N, &n, A, &n, S->tau, S->work, &S->lwork, &info);
+}
+
+static void u_orth_cols(Su* S, zc* A) { /* geqrf! + orgqr! on N x n */
+  const bint n = S->ns, N = S->Ns;
+  bint info;
+  p_zgeqrf(&N, &n, A, &N, S->tau, S->work, &S->lwork, &info);
+  p_zungqr(&N, &n, &n, A, &N, S->tau, S->work, &S->lwork, &info);
+}
+
+/* UpdatePhyLayer! of slice lt, src/tU/phy_update.jl:256-267, with get_r!
+ * (src/tU/GreenMatrix.jl:49-54) and Gupdate! (src/public/Gupdate.jl:5-11) */
+static void u_update_layer(Su* S, uint8_t* s, int lt) {
+  const int N = S->Ns;
+  uint8_t* sl = s + (size_t)(lt - 1) * N;
+  for (int i = 0; i < N; ++i) {
+    const int k = S->tape_pos < S->tape_len ? S->tk[S->tape_pos] : 0;
+    const double u = S->tape_pos < S->tape_len ? S->tu[S->tape_pos] : 2.0;
+    S->tape_pos++;
+    const int sold = sl[i];
+    const int sx = k + (k + 1 >= sold ? 2 : 1);
+    const zc delta = cexp(I * (S->alpha[lt - 1] * (S->eta[sx - 1] - S->eta[sold - 1]))) - 1.0;
+    const zc pc = 1.0 + delta * (1.0 - S->G[i + (size_t)i * N]);
+    const zc r = delta / pc;
+    double p = creal(pc) * creal(pc) + cimag(pc) * cimag(pc);
+    p *= S->gamma[sx - 1] / S->gamma[sold - 1];
+    const int acc = u < p;
+    if (S->acc_log) S->acc_log[S->log_pos] = (uint8_t)acc;
+    S->log_pos++;
+    if (acc) {
+      for (int c = 0; c < N; ++c) S->zN[c] = -(r * S->G[i + (size_t)c * N]);
+      S->zN[i] += r;
+      memcpy(S->gcol, S->G + (size_t)i * N, sizeof(zc) * N);
+      for (int c = 0; c < N; ++c) {
+        const zc z0 = S->zN[c];
+        zc* col = S->G + (size_t)c * N;
+        for (int rr = 0; rr < N; ++rr) col[rr] -= S->gcol[rr] * z0;
+      }
+      sl[i] = (uint8_t)sx;
+    }
+  }
+}
+
+/* phy_measure, src/tU/phy_update.jl:154-254: Ek, Eu and (honeycomb) the
+ * structure factors as the reference accumulates them (only the first term
+ * of each correlator line; the `+adjoint(...)` continuation lines are
+ * separate statements whose values are discarded). */
+static void u_measure(Su* S, const uint8_t* s, int lt, double* row) {
+  const int N = S->Ns;
+  zc* G0 = S->G0;
+  memcpy(G0, S->G, sizeof(zc) * N * N);
+  if (2 * lt > S->Nt) {
+    for (int t = lt; t > S->Nt / 2; --t) {
+      u_setD(S, t, s, -1.0);
+      u_wrap_bwd(S, G0);
+    }
+  } else {
+    for (int t = lt + 1; t <= S->Nt / 2; ++t) {
+      u_setD(S, t, s, 1.0);
+      u_wrap_fwd(S, G0);
+    }
+  }
+  zmm(N, N, N, S->HalfeK, N, G0, N, S->tmpNN, N);
+  zmm(N, N, N, S->tmpNN, N, S->HalfeKinv, N, G0, N);
+  zc ks = 0.0, eu = 0.0;
+  for (size_t e = 0; e < (size_t)N * N; ++e) ks += S->K[e] * G0[e];
+  for (int i = 0; i < N; ++i) eu += (1.0 - G0[i + (size_t)i * N]) * conj(G0[i + (size_t)i * N]);
+  zc cdw0 = 0.0, cdw1 = 0.0, sdw0 = 0.0, sdw1 = 0.0;
+  if (S->honeycomb) {
+    const int L1 = S->L1, L2 = S->L2;
+#define g(i, j) G0[(i) + (size_t)(j) * N]
+    for (int rx = 1; rx <= L1; ++rx)
+      for (int ry = 1; ry <= L2; ++ry) {
+        zc t1 = 0.0, t2 = 0.0;
+        for (int ix = 1; ix <= L1; ++ix)
+          for (int iy = 1; iy <= L2; ++iy) {
+            const int jx = (ix + rx - 1) % L1 + 1, jy = (iy + ry - 1) % L2 + 1;
+            const int a1 = 2 * (ix + (iy - 1) * L1) - 2, a2 = 2 * (jx + (jy - 1) * L1) - 2;
+            const int b1 = a1 + 1, b2 = a2 + 1;
+            const double dl = a1 == a2 ? 1.0 : 0.0;
+            t1 += (1.0 - g(a1, a1)) * (1.0 - g(a2, a2)) + (dl - g(a1, a2)) * g(a2, a1);
+            t1 += (1.0 - g(b1, b1)) * (1.0 - g(b2, b2)) + (dl - g(b1, b2)) * g(b2, b1);
+            t1 -= (1.0 - g(b1, b1)) * (1.0 - g(a2, a2)) - g(b1, a2) * g(a2, b1);
+            t1 -= (1.0 - g(a1, a1)) * (1.0 - g(b2, b2)) - g(a1, b2) * g(b2, a1);
+            t2 += (1.0 - g(a1, a1)) * conj(g(a2, a2));
+            t2 += (1.0 - g(b1, b1)) * conj(g(b2, b2));
+            t2 -= (1.0 - g(a1, a1)) * conj(g(b2, b2));
+            t2 -= (1.0 - g(b1, b1)) * conj(g(a2, a2));
+          }
+        const double ph = cos(2 * M_PI / L1 * rx + 2 * M_PI / L2 * ry);
+        cdw0 += t1 + t2;
+        cdw1 += ph * (t1 + t2);
+        sdw0 += t1 - t2;
+        sdw1 += ph * (t1 - t2);
+      }
+#undef g
+  }
+  const double n2 = (double)N * N;
+  row[0] += -2.0 * S->Ht * creal(ks);
+  row[1] += creal(eu);
+  row[2] += creal(cdw0) / n2;
+  row[3] += creal(cdw1) / n2;
+  row[4] += creal(sdw0) / n2;
+  row[5] += creal(sdw1) / n2;
+}
+
+static int u_is_node(const Su* S, int lt) {
+  for (int k = 0; k < S->NN; ++k)
+    if (S->nodes[k] == lt) return 1;
+  return 0;
+}
+
+/* The reference's phy_update for one t-U chain (complex matrices as
+ * interleaved (re, im) doubles).  obs: 6 doubles per sweep.  Returns 0 on
+ * success. */
+int kdq_cpu_tu_phy_update(int Ns, int Nt, int NN, const int64_t* nodes, const double* alpha, const double* gamma,
+                          const double* eta, const double* eK, const double* eKinv, const double* HalfeK,
+                          const double* HalfeKinv, const double* K, double Ht, const double* Pt, int L1, int L2,
+                          int honeycomb, uint8_t* s, int sweeps, int record, const uint8_t* tape_k,
+                          const double* tape_u, size_t tape_len, double* obs, uint8_t* acc_log) {
+  if (!p_zgemm || Ns > 512) return 2;
+  Su S;
+  memset(&S, 0, sizeof S);
+  S.Ns = Ns; S.ns = Ns / 2; S.Nt = Nt; S.NN = NN; S.L1 = L1; S.L2 = L2; S.honeycomb = honeycomb;
+  S.nodes = nodes; S.alpha = alpha; S.gamma = gamma; S.eta = eta;
+  S.eK = (const zc*)eK; S.eKinv = (const zc*)eKinv; S.HalfeK = (const zc*)HalfeK;
+  S.HalfeKinv = (const zc*)HalfeKinv; S.K = (const zc*)K; S.Ht = Ht;
+  S.tk = tape_k; S.tu = tape_u; S.tape_len = tape_len; S.acc_log = acc_log;
+  const size_t NNe = (size_t)Ns * Ns, Nn = (size_t)Ns * S.ns;
+  S.lwork = 64 * (bint)Ns;
+  zc* mem = (zc*)calloc(4 * NNe + 2 * (size_t)NN * Nn + 2 * Nn + (size_t)S.ns * S.ns + Ns + S.ns +
+                            (size_t)S.lwork + 2 * (size_t)Ns,
+                        sizeof(zc));
+  S.ipiv = (bint*)calloc(S.ns, sizeof(bint));
+  if (!mem || !S.ipiv) {
+    free(mem);
+    free(S.ipiv);
+    return 3;
+  }
+  zc* p = mem;
+  S.G = p; p += NNe; S.tmpNN = p; p += NNe; S.BM = p; p += NNe; S.G0 = p; p += NNe;
+  S.BLs = p; p += (size_t)NN * Nn; S.BRs = p; p += (size_t)NN * Nn;
+  S.tmpNn = p; p += Nn; S.tmpnN = p; p += Nn;
+  S.tmpnn = p; p += (size_t)S.ns * S.ns; S.tmpN = p; p += Ns; S.tau = p; p += S.ns;
+  S.work = p; p += S.lwork; S.zN = p; p += Ns; S.gcol = p;
+  const int Θidx = NN / 2 + 1;
+  /* BRs[1] = Pt; BLs[NN] = Pt' (adjoint) */
+  const zc* P = (const zc*)Pt;
+  memcpy(S.BRs, P, sizeof(zc) * Nn);
+  zc* BLN = S.BLs + (size_t)(NN - 1) * Nn;
+  for (int i = 0; i < Ns; ++i)
+    for (int c = 0; c < S.ns; ++c) BLN[c + (size_t)i * S.ns] = conj(P[i + (size_t)c * Ns]);
+  for (int idx = NN - 1; idx >= 1; --idx) {
+    u_BM_F(&S, s, idx);
+    zmm(S.ns, Ns, Ns, S.BLs + (size_t)idx * Nn, S.ns, S.BM, Ns, S.tmpnN, S.ns);
+    u_orth_rows(&S, S.tmpnN);
+    memcpy(S.BLs + (size_t)(idx - 1) * Nn, S.tmpnN, sizeof(zc) * Nn);
+  }
+  int idx = 1, rc = 0;
+  if (u_get_G(&S, S.BLs, S.BRs)) rc = 4;
+  for (int w = 0; w < sweeps && !rc; ++w) {
+    double row[6] = {0};
+    int counter = 0;
+    for (int lt = 1; lt <= Nt; ++lt) {
+      u_setD(&S, lt, s, 1.0);
+      u_wrap_fwd(&S, S.G);
+      u_update_layer(&S, s, lt);
+      if (record && Θidx - idx >= 0 && Θidx - idx <= 1) {
+        u_measure(&S, s, lt, row);
+        counter++;
+      }
+      if (u_is_node(&S, lt)) {
+        idx += 1;
+        u_BM_F(&S, s, idx - 1);
+        zmm(Ns, S.ns, Ns, S.BM, Ns, S.BRs + (size_t)(idx - 2) * Nn, Ns, S.tmpNn, Ns);
+        u_orth_cols(&S, S.tmpNn);
+        memcpy(S.BRs + (size_t)(idx - 1) * Nn, S.tmpNn, sizeof(zc) * Nn);
+        if (u_get_G(&S, S.BLs + (size_t)(idx - 1) * Nn, S.BRs + (size_t)(idx - 1) * Nn)) rc = 4;
+      }
+    }
+    for (int lt = Nt; lt >= 1; --lt) {
+      u_update_layer(&S, s, lt);
+      if (record && idx - Θidx >= 0 && idx - Θidx <= 1) {
+        u_measure(&S, s, lt, row);
+        counter++;
+      }
+      u_setD(&S, lt, s, -1.0);
+      u_wrap_bwd(&S, S.G);
+      if (u_is_node(&S, lt - 1)) {
+        idx -= 1;
+        u_BM_F(&S, s, idx);
+        zmm(S.ns, Ns, Ns, S.BLs + (size_t)idx * Nn, S.ns, S.BM, Ns, S.tmpnN, S.ns);
+        u_orth_rows(&S, S.tmpnN);
+        memcpy(S.BLs + (size_t)(idx - 1) * Nn, S.tmpnN, sizeof(zc) * Nn);
+        if (u_get_G(&S, S.BLs + (size_t)(idx - 1) * Nn, S.BRs + (size_t)(idx - 1) * Nn)) rc = 4;
+      }
+    }
+    if (record && obs)
+      for (int q = 0; q < 6; ++q) obs[(size_t)w * 6 + q] = counter ? row[q] / counter : 0.0;
   }
   if (S.tape_pos > tape_len) rc = 5;
   free(mem);

@@ -48,7 +48,7 @@ class Tape:
 
 
 def _sx(sold: int, k: int) -> int:
-    """k-th element of {1,2,3,4} minus sold (ascending): src/tU/model.jl:140-146."""
+    """k-th element of {1,2,3,4} minus sold (ascending): src/tU/model.jl:87-93."""
     return (1, 2, 3, 4, 5)[k + (k + 1 >= sold)]
 
 

@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY: the checker of the CUDA SCEE sweep; the product
 never calls it.
 
-``ctrl_SCEEicr`` (src/tU/SCEE.jl:1-211) runs two replicas of the t-U field
+``ctrl_SCEEicr`` (src/tU/SCEE.jl:1-262) runs two replicas of the t-U field
 whose weight is reweighted by the Rényi-2 Grover determinants of two regions,
 |det g_A|^(2 λ) |det g_B|^(2 (1 - λ)), and records the mean over slices of
 (|det g_A|^2 / |det g_B|^2)^(1/Nλ) per sweep (the incremental estimator of
@@ -12,7 +12,7 @@ src/public/Buffer.jl:22-31): Gt = G(τ, τ), G0 = G(τ0, τ0) at the middle node
 Gt0 = G(τ, τ0), G0t = G(τ0, τ), and the inverse Grover matrices of A and B
 are kept up to date by rank-1 updates.  Numerics follow src/public/Gupdate.jl
 (G4! :159-212, G4update! :23-37, get_abTau1!/2! :91-132, GMupdate! :45-58)
-and src/tU/SCEE.jl (get_ABGM! :213-228, UpdateSCEELayer! :230-287), with the
+and src/tU/SCEE.jl (get_ABGM! :264-276, UpdateSCEELayer! :278-324), with the
 random draws taken from an explicit tape in the reference's consumption
 order: per site, replica 1's (choice, uniform) then replica 2's.
 """
@@ -87,7 +87,7 @@ class SCEE:
         g = 2 * a @ b - a - b + np.eye(len(idx_region))
         return abs(np.linalg.det(g)) ** 2, np.linalg.inv(g)
 
-    def ABGM(self, idx, forward):   # get_ABGM!, src/tU/SCEE.jl:213-228
+    def ABGM(self, idx, forward):   # get_ABGM!, src/tU/SCEE.jl:264-276
         self.G4(0, idx, forward)
         self.G4(1, idx, forward)
         self.detA, self.invA = self.grover(self.A)
@@ -136,7 +136,7 @@ class SCEE:
             Gt -= np.outer(ct, zN)
             s[i, lt - 1] = sx
 
-    def layer(self, lt):   # UpdateSCEELayer!, src/tU/SCEE.jl:230-287
+    def layer(self, lt):   # UpdateSCEELayer!, src/tU/SCEE.jl:278-324
         for i in range(self.m.Ns):
             self.propose(0, lt, i)
             self.propose(1, lt, i)
@@ -215,7 +215,7 @@ class SCEE:
         return val
 
     def run(self, sweeps: int):
-        """src/tU/SCEE.jl:84-197: forward then backward over the slices, the
+        """src/tU/SCEE.jl:89-246: forward then backward over the slices, the
         estimator accumulated after every slice's updates."""
         self.init()
         for _ in range(sweeps):

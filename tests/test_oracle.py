@@ -119,14 +119,14 @@ def test_golden_fixture(path):
 
 def test_c_restatement_matches_numpy_oracle():
     """The timed CPU baseline (C, dense bond GEMMs) makes the oracle's decisions."""
-    import cport_tv
+    import cport
     model = cases.tv_honeycomb()
     s = Initial_s(model, 3)
     n = O.proposals_per_sweep(model)
     ks, us = zip(*(philox.tape(5, 0, w, n) for w in range(2)))
     k, u = np.concatenate(ks), np.concatenate(us)
     ref = O.phy_update(model, s, 2, O.Tape(k, u), True)
-    s2, obs, acc = cport_tv.tv_phy_update(model, s, 2, k, u, True, log=True)
+    s2, obs, acc = cport.tv_phy_update(model, s, 2, k, u, True, log=True)
     np.testing.assert_array_equal(acc.astype(bool), np.array(ref.accepts))
     np.testing.assert_array_equal(s2, ref.s)
     np.testing.assert_allclose(obs, np.array(ref.obs_rows), rtol=1e-9, atol=1e-10)
@@ -164,3 +164,19 @@ def test_golden_cnn_fixture():
     np.testing.assert_allclose(F, spec["F"], rtol=1e-12, atol=1e-12)
     g = CNN.grad(fields, np.array(spec["dF"]), params)
     np.testing.assert_allclose(g, spec["grad"], rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("make", [cases.tu_honeycomb, cases.tu_square, cases.tu_quench], ids=["hc", "sq", "quench"])
+def test_c_restatement_tu_matches_numpy_oracle(make):
+    """The timed t-U CPU baseline (C, complex GEMMs as the reference) makes the oracle's decisions."""
+    import cport
+    model = make()
+    s = Initial_s(model, 4)
+    n = O.proposals_per_sweep(model)
+    ks, us = zip(*(philox.tape(6, 0, w, n) for w in range(2)))
+    k, u = np.concatenate(ks), np.concatenate(us)
+    ref = O.phy_update(model, s, 2, O.Tape(k, u), True)
+    s2, obs, acc = cport.tu_phy_update(model, s, 2, k, u, True, log=True)
+    np.testing.assert_array_equal(acc.astype(bool), np.array(ref.accepts))
+    np.testing.assert_array_equal(s2, ref.s)
+    np.testing.assert_allclose(obs, np.array(ref.obs_rows)[:, :6], rtol=1e-9, atol=1e-10)
