@@ -1,13 +1,18 @@
 """Benchmark of the projector-DQMC sweep on GB300.
 
-Workload: 256 independent Markov chains of the spinless t-V model on the
-6x6 honeycomb lattice (N = 72 sites, V/t = 1, dt = 0.05, 2Θ = 20 -> 400
-slices, n_wrap = 10), FP64 throughout, energy and density structure factor
+Workload (the metric's own configuration): 256 independent Markov chains of
+the t-U Hubbard model on the 12x12 square lattice (N = 144, U/t = 8,
+dt = 0.05, 2Θ = 16 -> 320 slices, n_wrap = 8), energy and double occupancy
 measured every sweep.  One step = one forward+backward sweep of every chain.
 
-Metric: effective samples/s = (chain-sweeps/s) / τ_int(E_kin), summed over
-all GPUs.  τ_int is estimated (Sokal window) from the measured energy series
-of the timed sweeps, pooled over the chains.
+Metric: effective samples/s = chain-sweeps/s / (2 τ_int(E_kin)) of the
+mixed-precision sweep (FP32 bulk products and updates, FP64 ratios,
+stabilisation and recompute), summed over all GPUs; `vs_baseline` is its
+ratio to the plain FP64 GPU sweep measured in the same run on the same
+fields (the metric's "vs plain FP64 DQMC").  τ_int (Sokal window, τ_int >= 1/2
+for uncorrelated samples, so N sweeps are worth N / (2 τ_int) independent
+samples) comes from a committed long run of each arm (`--tau-run`) and is
+also estimated live from the timed sweeps.
 
   value   device-resident: fields and B chains live in HBM, one kdq_sweep
           per step, timed with CUDA events on the library's stream
@@ -15,8 +20,9 @@ of the timed sweeps, pooled over the chains.
           buffers: fields uploaded, chain rebuilt, one sweep, fields and
           measurement rows read back, every step
 
-`--impl reference` times the CPU restatement of the reference algorithm (the
-oracle) on the host cores instead.
+`--impl reference` times the C restatement of the reference algorithm on
+the host cores instead; `--workload c1|c2|c4|c5` selects the other
+configurations.
 """
 from __future__ import annotations
 
@@ -36,17 +42,19 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "eff. samples/s (sweeps/s÷τ_int) vs plain FP64 DQMC, 1 GB300, obs within 1σ"
-UNIT = "chain-sweeps/s / tau_int"
+UNIT = "chain-sweeps/s / (2 tau_int)"
 NCHAINS = 256
 RECORD = 2   # measurements as the reference's estimator, wraps folded into two products (kdq_phy_update)
-TAU_FILE = ROOT / "profiles" / "tau_int_tv_honeycomb_6x6.json"
 
 
-def reference_tau_int():
-    """τ_int of the plain local-update sweep on this workload, from a long
-    committed GPU run (both arms run the same Markov chain algorithm)."""
+def tau_file():
+    return ROOT / "profiles" / f"tau_int_{WL['tag']}.json"
+
+
+def committed_tau(precision):
+    """τ_int(E_kin) of `precision` on this workload from its committed long run."""
     try:
-        return float(json.loads(TAU_FILE.read_text())["tau_int"])
+        return float(json.loads(tau_file().read_text())[precision]["tau_int"])
     except Exception:
         return None
 
@@ -81,32 +89,33 @@ def _tu_hc_9x9():
                            Lattice="HoneyComb120", site=[9, 9], BatchSize=10, Initial="H0")
 
 
-# The bench line is c2 (the metric's configuration: batched plain FP64 sweep);
-# the others are the remaining single-GPU configurations, for `--workload`.
+# The bench line is c3 at the spec batch (256 chains at N = 144, the
+# metric's configuration); the others are the remaining single-GPU
+# configurations, for `--workload`.
 WORKLOADS = {
-    "c1": dict(make=_tu_4x4, chains=1, Ns=16, Nt=100, n_wrap=10,
+    "c1": dict(make=_tu_4x4, chains=1, Ns=16, Nt=100, n_wrap=10, tag="tu_square_4x4",
                desc="t-U 4x4 square (N=16), 100 slices, n_wrap=10, U/t=4, dt=0.1, one chain, "
                     "energy + double occupancy per sweep",
                model="tU_Hubbard_Para(SQUARE45, site=[2,4])"),
-    "c2": dict(make=_tv_6x6, chains=256, Ns=72, Nt=400, n_wrap=10,
+    "c2": dict(make=_tv_6x6, chains=256, Ns=72, Nt=400, n_wrap=10, tag="tv_honeycomb_6x6",
                desc="t-V 6x6 honeycomb (N=72), 400 slices, n_wrap=10, V/t=1, dt=0.05, 256 independent "
                     "chains, energy + density structure factor per sweep",
                model="tV_Hubbard_Para(HoneyComb120, site=[6,6])"),
-    "c3": dict(make=_tu_12x12, chains=128, Ns=144, Nt=320, n_wrap=8,
-               desc="t-U 12x12 square (N=144), 320 slices, n_wrap=8, U/t=8, dt=0.05, 128 independent "
+    "c3": dict(make=_tu_12x12, chains=256, Ns=144, Nt=320, n_wrap=8, tag="tu_square_12x12",
+               desc="t-U 12x12 square (N=144), 320 slices, n_wrap=8, U/t=8, dt=0.05, 256 independent "
                     "chains, energy + double occupancy per sweep",
                model="tU_Hubbard_Para(SQUARE45, site=[6,12])"),
-    "c4": dict(make=_tuv_8x8, chains=256, Ns=64, Nt=200, n_wrap=10,
+    "c4": dict(make=_tuv_8x8, chains=256, Ns=64, Nt=200, n_wrap=10, tag="tuv_square_8x8",
                desc="t-UV 8x8 square (N=64), 200 slices, n_wrap=10, U/t=4, V/t=0.5, dt=0.1, 256 chains "
                     "(128 replica pairs), energies per sweep",
                model="tUV_Hubbard_Para(SQUARE45, site=[4,8], allow_marginal=True)"),
-    "c5": dict(make=_tu_hc_9x9, chains=256, Ns=162, Nt=200, n_wrap=10,
+    "c5": dict(make=_tu_hc_9x9, chains=256, Ns=162, Nt=200, n_wrap=10, tag="tu_honeycomb_9x9",
                desc="t-U 9x9 honeycomb (N=162), 200 slices, n_wrap=10, U/t=4, dt=0.1, 256 chains, "
                     "energy, double occupancy and structure factors per sweep",
                model="tU_Hubbard_Para(HoneyComb120, site=[9,9])"),
 }
-WL = WORKLOADS["c2"]
-PRECISION = "fp64"
+WL = WORKLOADS["c3"]
+PRECISION = "mixed"
 
 
 def make_model():
@@ -116,6 +125,7 @@ def make_model():
 def config():
     return {"workload": WL["desc"] + f", {PRECISION}", "model": WL["model"], "chains_per_gpu": NCHAINS,
             "Ns": WL["Ns"], "Nt": WL["Nt"], "n_wrap": WL["n_wrap"], "precision": PRECISION,
+            "parallelism": f"replicas x{int(os.environ.get('WORLD_SIZE', '1'))}",
             "l2": "no flush: per-GPU chain state (B chains, fields, G) is larger than the 129 MB L2"}
 
 
@@ -193,10 +203,11 @@ def fp64_peak_tflops(torch, dev):
 
 
 def traffic_per_launch():
-    """DRAM bytes (read + write) per sweep-kernel launch from the committed ncu capture."""
+    """DRAM bytes (read + write) per sweep-kernel launch from the committed ncu
+    capture of this workload and precision, scaled to the bench's chains."""
     try:
-        return float(json.loads((ROOT / "profiles" / "k_block_tv6x6_traffic.json").read_text())
-                     ["dram_bytes_per_launch"])
+        d = json.loads((ROOT / "profiles" / f"k_block_{WL['tag']}_{PRECISION}_traffic.json").read_text())
+        return float(d["dram_bytes_per_launch_per_chain"]) * NCHAINS
     except Exception:
         return None
 
@@ -209,35 +220,60 @@ def hbm_peak_gbs():
 
 
 # ---------------------------------------------------------------- CPU arm
-def _cpu_worker(args):
-    """One chain of the workload through the C restatement of the reference sweep."""
-    seed, chain, sweeps = args
+_CPU = {}   # per worker process: model, this worker's chain field, tapes
+
+
+def _cpu_init(wl, counter):
+    """Pool initializer: each worker owns one chain (numbered by the shared
+    counter) of workload `wl`; model, field and library are built here,
+    outside any timed call."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import cport
-    if sweeps == 0:                       # warm-up: load the library only
-        cport.load()
-        return 0.0
+    from kapdqmc_gb300 import Initial_s
+    global WL
+    WL = WORKLOADS[wl]
+    with counter.get_lock():
+        chain = counter.value
+        counter.value += 1
+    model = make_model()
+    cport.load()
+    _CPU.update(model=model, chain=chain, s=Initial_s(model, 1000 + chain))
+
+
+def _cpu_worker(args):
+    """Sweep this worker's chain `sweeps` times through the C restatement of
+    the reference sweep, with a tape drawn before the clock starts; returns
+    the seconds of the C call."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cport
     import dqmc_oracle as O
     import philox
-    from kapdqmc_gb300 import Initial_s
-    model = make_model()
-    s = Initial_s(model, 1000 + chain)
+    seed, sweeps = args
+    model, chain = _CPU["model"], _CPU["chain"]
     n = O.proposals_per_sweep(model)
     ks, us = zip(*(philox.tape(seed, chain, w, n) for w in range(sweeps)))
-    cport.load()
+    k, u = np.concatenate(ks), np.concatenate(us)
+    run = cport.tu_phy_update if model.kind == 0 else cport.tv_phy_update
     t0 = time.perf_counter()
-    cport.tv_phy_update(model, s, sweeps, np.concatenate(ks), np.concatenate(us), record=True)
-    return time.perf_counter() - t0
+    s, _, _ = run(model, _CPU["s"], sweeps, k, u, record=True)
+    dt = time.perf_counter() - t0
+    _CPU["s"] = s
+    return dt
 
 
 CPU_KIND = "port"
-CPU_SWEEPS = 10          # per chain in the GPU arm's cpu_baseline sample (about 10 s of CPU work)
-CPU_SAMPLE = ("C restatement of the reference t-V sweep (dense bond-rotation GEMMs as the reference; "
-              "OpenBLAS/LAPACK from numpy, 1 thread each), one chain per host core")
+
+
+def cpu_sample_desc():
+    what = ("C restatement of the reference t-U sweep (complex eK and complex GEMMs as the reference)"
+            if make_model().kind == 0 else
+            "C restatement of the reference t-V sweep (dense bond-rotation GEMMs as the reference)")
+    return what + "; OpenBLAS/LAPACK from numpy, 1 thread each; one chain per host core"
 
 
 class CpuArm:
-    """The reference algorithm on the host cores: one chain per core, all busy."""
+    """The reference algorithm on the host cores: one chain per core, all busy.
+    Model, fields and proposal tapes are built outside the timed calls."""
 
     def __init__(self, cores: int):
         import multiprocessing as mp
@@ -248,23 +284,24 @@ class CpuArm:
         saved = {v: os.environ.get(v) for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
         for v in saved:                     # inherited by the workers before numpy loads
             os.environ[v] = "1"
+        ctx = mp.get_context("spawn")
+        wl = next(k for k, v in WORKLOADS.items() if v is WL)
         try:
-            self.pool = mp.get_context("spawn").Pool(cores)
+            self.pool = ctx.Pool(cores, initializer=_cpu_init, initargs=(wl, ctx.Value("i", 0)))
         finally:
             for v, x in saved.items():
                 if x is None:
                     os.environ.pop(v, None)
                 else:
                     os.environ[v] = x
-        self.pool.map(_cpu_worker, [(7, c, 0) for c in range(cores)])      # load in every worker
         self.calls = 0
 
     def step(self, sweeps_per_chain: int = 1) -> float:
-        """Wall time of sweeps_per_chain sweeps of `cores` chains run concurrently."""
+        """Seconds for `cores` chains to run sweeps_per_chain sweeps concurrently:
+        the slowest worker's C-call time (all workers start together)."""
         self.calls += 1
-        t0 = time.perf_counter()
-        self.pool.map(_cpu_worker, [(7 + self.calls, c, sweeps_per_chain) for c in range(self.cores)])
-        return time.perf_counter() - t0
+        times = self.pool.map(_cpu_worker, [(7 + self.calls, sweeps_per_chain)] * self.cores, chunksize=1)
+        return max(times)
 
     def close(self):
         self.pool.close()
@@ -280,35 +317,99 @@ def cpu_chain_sweeps_per_s(cores: int, sweeps_per_chain: int = 1):
     return cores * sweeps_per_chain / wall, wall
 
 
-def run_tau(args):
-    """Long run of the plain sweep: τ_int(E_kin) with a binning cross-check.
+OBS_NAMES = {0: ("Ek", "Eu", "CDW0", "CDW1", "SDW0", "SDW1", "S_charge_full", "S_charge_full_q1",
+                 "S_spin_full", "S_spin_full_q1"),
+             1: ("Ek", "Ev", "R0_AA", "R0_BB", "R0_BA", "R0_AB", "R1_AA", "R1_BB", "R1_BA", "R1_AB"),
+             2: ("Ek", "Eu", "Ev", "CDW0", "CDW1", "SDW0", "SDW1", "S_charge_full", "S_charge_full_q1",
+                 "S_spin_full", "S_spin_full_q1")}
+SPIN_COL = {0: 8, 2: 9}     # corrected AF spin structure factor (staggered, full measurement)
 
-    Prints the JSON that is committed as the workload's τ_int (both bench arms
-    run the same Markov chain algorithm, so they share it)."""
-    from kapdqmc_gb300 import Initial_s
+
+def full_measurement(model) -> bool:
+    return model.kind == 0 or (model.kind == 2 and model.is_complex)
+
+
+def new_sweeper(model, prec, fields, seed, device=0):
     from kapdqmc_gb300.sweep import Sweeper
-    model = make_model()
-    sw = Sweeper(model, NCHAINS)
-    sw.set_precision(PRECISION)
-    sw.set_fields(np.stack([Initial_s(model, 5000 + c) for c in range(NCHAINS)]))
-    sw.set_rng(424242)
-    sw.init()
-    burn = 20
-    sw.sweep(burn + args.tau_run, record=RECORD)
-    sw.synchronize()
-    ek = sw.get_obs(burn + args.tau_run)[:, burn:, 0]
-    tau = tau_int(ek)
-    # binning: τ_int ≈ var(bin means) * B / (2 var)
-    var = ek.var()
+    sw = Sweeper(model, len(fields), device=device)
+    sw.set_precision(prec)
+    if full_measurement(model):
+        sw.set_measure_full(True)
+    sw.set_fields(fields)
+    sw.set_rng(seed)
+    return sw
+
+
+def obs_summary(model, obs):
+    """Mean and standard error (over independent chains) of every column;
+    obs is (chains, sweeps, n_obs) of equilibrated sweeps."""
+    names = OBS_NAMES[model.kind]
+    cm = obs.mean(axis=1)
+    out = {}
+    for q in range(obs.shape[2]):
+        if not np.any(obs[:, :, q]):
+            continue
+        out[names[q]] = [float(cm[:, q].mean()), float(cm[:, q].std(ddof=1) / math.sqrt(cm.shape[0]))]
+    if "Eu" in out and model.kind == 0:     # double occupancy per site
+        out["double_occupancy"] = [out["Eu"][0] / model.Ns, out["Eu"][1] / model.Ns]
+    return out
+
+
+def binned_tau(x):
+    """τ_int from binning: var(bin means) * B / (2 var), B = 1 .. 16."""
+    var = x.var()
     bins = {}
     for B in (1, 2, 4, 8, 16):
-        T = ek.shape[1] // B
-        m = ek[:, :T * B].reshape(ek.shape[0], T, B).mean(axis=2)
-        bins[B] = float(m.var() * B / (2 * var))
-    out = {"workload": config()["workload"], "chains": NCHAINS, "sweeps": args.tau_run, "burn_in": burn,
-           "observable": "kinetic energy (first measurement column)", "estimator": "Sokal window c=5",
-           "tau_int": tau, "tau_int_binning": bins, "energy_mean": float(ek.mean()),
-           "energy_err": float(ek.mean(axis=1).std() / math.sqrt(NCHAINS))}
+        T = x.shape[1] // B
+        if T < 2:
+            break
+        m = x[:, :T * B].reshape(x.shape[0], T, B).mean(axis=2)
+        bins[B] = float(m.var() * B / (2 * var)) if var > 0 else 0.5
+    return bins
+
+
+def run_tau(args):
+    """Long runs of the bench's two arms: τ_int of the energy (and of the AF
+    spin structure factor where it is measured), binning cross-checks, and
+    every observable's mean and error per arm with the mixed-vs-FP64
+    difference in units of its combined error.  The mixed arm equilibrates
+    from random fields; the FP64 arm starts from its final fields.  Prints
+    the JSON that is committed as profiles/tau_int_<workload>.json."""
+    from kapdqmc_gb300 import Initial_s
+    model = make_model()
+    fields = np.stack([Initial_s(model, 5000 + c) for c in range(NCHAINS)])
+    arms = [("mixed", args.tau_burn, args.tau_run)] if model.is_complex else []
+    arms.append(("fp64", args.tau_burn if not arms else max(5, args.tau_burn // 3),
+                 args.tau_run_fp64 or max(20, args.tau_run // 3)))
+    out = {"workload": config()["workload"], "chains": NCHAINS, "record": RECORD,
+           "estimator": "Sokal window c=5 on the chain-pooled autocovariance; binning as a check",
+           "errors": "standard error over independent chains of the per-chain means"}
+    for prec, burn, sweeps in arms:
+        sw = new_sweeper(model, prec, fields, 424242 + len(out))
+        sw.init()
+        t0 = time.perf_counter()
+        sw.sweep(burn + sweeps, record=RECORD)
+        sw.synchronize()
+        wall = time.perf_counter() - t0
+        obs = sw.get_obs(burn + sweeps)[:, burn:, :]
+        fields = sw.get_fields()
+        st = sw.stats()
+        sw.close()
+        arm = {"burn_in": burn, "sweeps": sweeps, "wall_s": wall,
+               "chain_sweeps_per_s": NCHAINS * (burn + sweeps) / wall,
+               "tau_int": tau_int(obs[:, :, 0]), "tau_int_binning": binned_tau(obs[:, :, 0]),
+               "acceptance": st["accepted"] / max(st["proposals"], 1), "max_drift": st["max_drift"],
+               "obs": obs_summary(model, obs)}
+        if model.kind in SPIN_COL and obs.shape[2] > SPIN_COL[model.kind] and np.any(obs[:, :, SPIN_COL[model.kind]]):
+            x = obs[:, :, SPIN_COL[model.kind]]
+            arm["tau_int_af_spin_sf"] = tau_int(x)
+            arm["tau_int_af_spin_sf_binning"] = binned_tau(x)
+        out[prec] = arm
+        print(json.dumps({prec: {k: v for k, v in arm.items() if k != "obs"}}), file=sys.stderr, flush=True)
+    if "mixed" in out and "fp64" in out:
+        a, b = out["mixed"]["obs"], out["fp64"]["obs"]
+        out["z_mixed_vs_fp64"] = {k: (a[k][0] - b[k][0]) / math.hypot(a[k][1], b[k][1])
+                                  for k in a if k in b and math.hypot(a[k][1], b[k][1]) > 0}
     print(json.dumps(out))
 
 
@@ -325,13 +426,14 @@ def run_reference(args):
     finally:
         arm.close()
     cs = cores * len(walls) / sum(walls)
-    tau = args.tau_int or reference_tau_int() or 1.0
-    value = cs / tau
-    sample = (f"{CPU_SAMPLE}; {cores} chains x 1 sweep per step; tau_int={tau:.3g} "
-              f"(the workload's committed long-run value)")
+    tau = args.tau_int or committed_tau("fp64") or 0.5
+    value = cs / (2 * tau)
+    sample = (f"{cpu_sample_desc()}; {cores} chains x 1 sweep per step (model, fields and proposal tapes "
+              f"built outside the timed calls); tau_int={tau:.3g} (the plain FP64 sweep's committed long-run value)")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": float(np.mean(walls)) * 1e3,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "c128" if make_model().is_complex else "f64",
            "data": "synthetic (seeded HS fields and Philox proposal stream)", "config": config(),
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": CPU_KIND, "sample": sample,
@@ -341,11 +443,41 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU arm
+def timed_arm(torch, dist, dev, model, prec, fields, seed, warmup, steps, autotune=True, clocks=False, rank=0):
+    """One arm of the bench: `warmup` untimed sweeps, then `steps` sweeps timed
+    with CUDA events on the library's stream between barriers."""
+    sw = new_sweeper(model, prec, fields, seed, device=dev.index)
+    stream = torch.cuda.ExternalStream(sw.stream, device=dev)
+    tiles, tile_ms = sw.autotune() if autotune else (sw.tiles, {})
+    sw.init()
+    sw.sweep(warmup, record=RECORD)
+    sw.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    cproc = cfile = clk_path = None
+    if clocks:
+        clk_dir = os.environ.get("KDQ_CLOCKS_DIR")   # keep the raw clock samples there when set
+        clk_path = os.path.join(clk_dir, f"clocks_rank{rank}.csv") if clk_dir else \
+            os.path.join(tempfile.gettempdir(), f"kdq_clocks_{os.getpid()}.csv")
+        cproc, cfile = clocks_start(clk_path)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sw.sweep(steps, record=RECORD)
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks_stop(cproc, cfile, clk_path, dev.index) if clocks else None
+    sw.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = sw.stats()
+    obs = sw.get_obs(warmup + steps)[:, warmup:, :]
+    return dict(sw=sw, ms=ms, stats=st, obs=obs, tiles=tiles, tile_ms=tile_ms, clocks=clk)
+
+
 def run_gpu(args):
     import torch
     from kapdqmc_gb300 import Initial_s
     from kapdqmc_gb300.flops import sweep_flops
-    from kapdqmc_gb300.sweep import Sweeper
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -358,44 +490,19 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
 
     model = make_model()
-    sw = Sweeper(model, NCHAINS, device=local)
-    sw.set_precision(PRECISION)
     fields = np.stack([Initial_s(model, 1000 + NCHAINS * rank + c) for c in range(NCHAINS)])
     seed = 20261203 + rank
-    stream = torch.cuda.ExternalStream(sw.stream, device=dev)
+    prec = PRECISION if model.is_complex else "fp64"
 
-    # ---- device-resident throughput
-    sw.set_fields(fields)
-    sw.set_rng(seed)
-    # tile class: one timed sweep per class that covers the lattice (fields
-    # and random-stream positions restored; leaves the handle initialised)
-    tiles, tile_ms = sw.autotune() if not args.no_autotune else (sw.tiles, {})
-    sw.init()
-    sw.sweep(args.warmup, record=RECORD)
-    sw.synchronize()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clk_dir = os.environ.get("KDQ_CLOCKS_DIR")   # keep the raw clock samples there when set
-    clk_path = os.path.join(clk_dir, f"clocks_rank{rank}.csv") if clk_dir else \
-        os.path.join(tempfile.gettempdir(), f"kdq_clocks_{os.getpid()}.csv")
-    cproc, cfile = clocks_start(clk_path)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    sw.sweep(args.steps, record=RECORD)
-    e1.record(stream)
-    e1.synchronize()
-    clocks = clocks_stop(cproc, cfile, clk_path, local)
-    sw.synchronize()
-    ms = e0.elapsed_time(e1)
-    st = sw.stats()
-    obs = sw.get_obs(args.warmup + args.steps)
-    ek = obs[:, args.warmup:, 0]
+    # ---- the headline arm, device-resident
+    A = timed_arm(torch, dist, dev, model, prec, fields, seed, args.warmup, args.steps,
+                  autotune=not args.no_autotune, clocks=True, rank=rank)
+    sw, ms, st = A["sw"], A["ms"], A["stats"]
+    ek = A["obs"][:, :, 0]
     tau_live = tau_int(ek)
-    tau = args.tau_int or (reference_tau_int() if WL is WORKLOADS["c2"] and PRECISION == "fp64" else None) \
-        or tau_live
+    tau = args.tau_int or committed_tau(prec) or tau_live
     cs_per_s, t_max = replica_throughput(dist, ms, NCHAINS * args.steps, dev)
-    value = cs_per_s / tau
+    value = cs_per_s / (2 * tau)
 
     # ---- roofline of the sweep kernel (the only kernel of the timed region)
     acc_per_chain_sweep = st["accepted"] / (NCHAINS * args.steps)
@@ -406,7 +513,7 @@ def run_gpu(args):
     peak = fp64_peak_tflops(torch, dev)
     kc = bool(np.any(np.imag(np.asarray(model.eK)) != 0))
     fl = sweep_flops(model, acc_per_chain_sweep, record=RECORD, k_complex=kc)
-    if PRECISION == "fp64":
+    if prec == "fp64":
         flops_per_launch = fl["total"] * per_launch
         pipe = "FP64 DFMA (CUDA cores)"
     else:   # the FP64 part (QR, LU, G recompute) is what the mixed sweep is bound by
@@ -416,12 +523,12 @@ def run_gpu(args):
     roof = {"bound": "fp64", "pipe": pipe, "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
-            "traffic": traffic_per_launch() if WL is WORKLOADS["c2"] and PRECISION == "fp64" else None,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean over the sweep's "
-                              "k_block launches of the same workload (profiles/k_block_tv6x6_launches.md)",
+            "traffic": traffic_per_launch(),
+            "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum per k_block launch "
+                              f"(profiles/k_block_{WL['tag']}_{prec}_traffic.json)",
             "flops_per_launch": flops_per_launch,
             "flops_per_chain_sweep": fl}
-    if PRECISION == "mixed":
+    if prec == "mixed":
         roof["fp32_achieved_tflops"] = (fl["total"] - fl["stabilise_qr_lu"]) * per_launch / avg_launch_s / 1e12
 
     if args.phases:
@@ -457,53 +564,78 @@ def run_gpu(args):
                  "estimator": "e^-S2 = <|det(2 G1 G2 - G1 - G2 + I)_A|^2>, pair means over sweeps"}
 
     # ---- end to end through kdq_phy_update with host buffers
-    e2e_steps = max(2, min(args.steps, 5))
+    e2e_steps = max(2, min(args.steps, 3))
     cur = sw.get_fields()
     h2d = cur.nbytes
     d2h = cur.nbytes + NCHAINS * model_nobs(sw) * 8
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    e2e_rows = []
     for _ in range(e2e_steps):
         sw.set_fields(cur)
-        o = sw.phy_update(1, record=RECORD)
+        sw.phy_update(1, record=RECORD)
         cur = sw.get_fields()
-        e2e_rows.append(o[:, 0, 0])
     wall = time.perf_counter() - t0
     e2e_cs, _ = replica_throughput(dist, wall * 1e3, NCHAINS * e2e_steps, dev)
     wall = dist_max(dist, wall, dev)
-    e2e_value = e2e_cs / tau
+    e2e_value = e2e_cs / (2 * tau)
+    eq_fields = cur
+    sw.close()
+
+    # ---- the plain FP64 GPU sweep on the same fields: the metric's baseline
+    base = None
+    if prec == "mixed" and not args.no_fp64_arm:
+        n64 = max(2, args.steps // 5)
+        B = timed_arm(torch, dist, dev, model, "fp64", eq_fields, seed + 7, args.warmup, n64, autotune=False)
+        B["sw"].close()
+        cs64, _ = replica_throughput(dist, B["ms"], NCHAINS * n64, dev)
+        tau64 = args.tau_int or committed_tau("fp64") or tau_int(B["obs"][:, :, 0])
+        base = {"chain_sweeps_per_s": cs64, "tau_int": tau64, "eff_samples_per_s": cs64 / (2 * tau64),
+                "steps": n64, "warmup": args.warmup, "ms_per_step": B["ms"] / n64,
+                "max_drift": B["stats"]["max_drift"]}
 
     if rank == 0:
+        committed = {}
+        try:
+            committed = json.loads(tau_file().read_text())
+        except Exception:
+            pass
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None,
-               "dtype": "f64" if PRECISION == "fp64" else "f32 bulk products and updates, f64 ratios/QR/recompute",
+               "scaling": "weak",
+               "vs_baseline": value / base["eff_samples_per_s"] if base else None,
+               "vs_baseline_what": "mixed arm's effective samples/s over the plain FP64 GPU sweep's, same run, "
+                                   "same fields (no published number exists for this metric)",
+               "dtype": "c128" if prec == "fp64" and model.is_complex else (
+                   "f64" if prec == "fp64" else "c64 bulk products and updates, c128 ratios/QR/recompute"),
                "data": "synthetic (seeded HS fields and Philox proposal stream)",
-               "config": dict(config(), parallelism=f"replicas x{world}"),
+               "config": config(),
                "chain_sweeps_per_s": cs_per_s, "tau_int": tau, "tau_int_live": tau_live,
                "tau_int_source": "committed long run" if tau != tau_live else "this run",
                "acceptance": st["accepted"] / max(st["proposals"], 1),
                "max_drift": st["max_drift"],
-               "energy_mean": float(ek.mean()), "energy_err": float(ek.mean(axis=1).std() / math.sqrt(NCHAINS)),
+               "obs_this_run": obs_summary(model, A["obs"]),
+               "obs_long_run_z_mixed_vs_fp64": committed.get("z_mixed_vs_fp64"),
+               "fp64_arm": base,
                "gpu_launches": args.steps * launches_per_sweep,
-               "tiles": {"class": tiles, "autotune_sweep_ms": tile_ms},
+               "tiles": {"class": A["tiles"], "autotune_sweep_ms": A["tile_ms"]},
                **({"renyi2": renyi} if renyi else {}),
-               "roofline": roof, "clocks": clocks,
+               "roofline": roof, "clocks": A["clocks"],
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-                       "ms_per_step": wall / e2e_steps * 1e3}}
+                       "ms_per_step": wall / e2e_steps * 1e3,
+                       "what": "kdq_phy_update per step: fields host->device, chain rebuilt, one sweep, "
+                               "fields and rows device->host"}}
         print(json.dumps(out), file=sys.stderr, flush=True)
-        if not args.no_cpu and world == 1 and WL is WORKLOADS["c2"]:
+        if not args.no_cpu and world == 1 and model.kind in (0, 1) and WL is not WORKLOADS["c1"]:
             cores = os.cpu_count() or 1
-            cs_cpu, wall_cpu = cpu_chain_sweeps_per_s(cores, sweeps_per_chain=CPU_SWEEPS)
-            out["cpu_baseline"] = {"value": cs_cpu / tau, "unit": UNIT, "cores": cores, "kind": CPU_KIND,
+            cs_cpu, wall_cpu = cpu_chain_sweeps_per_s(cores, sweeps_per_chain=args.cpu_sweeps)
+            tau_cpu = committed_tau("fp64") or tau
+            out["cpu_baseline"] = {"value": cs_cpu / (2 * tau_cpu), "unit": UNIT, "cores": cores, "kind": CPU_KIND,
                                    "chain_sweeps_per_s": cs_cpu,
-                                   "sample": f"{CPU_SAMPLE}; {cores} chains x {CPU_SWEEPS} sweeps of the same workload, "
-                                             f"{wall_cpu:.1f} s"}
+                                   "sample": f"{cpu_sample_desc()}; {cores} chains x {args.cpu_sweeps} sweeps of the "
+                                             f"same workload, {wall_cpu:.1f} s; tau_int {tau_cpu:.3g}"}
         print(json.dumps(out))
-    sw.close()
     if dist:
         dist.destroy_process_group()
 
@@ -780,10 +912,14 @@ def model_nobs(sw):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-sweeps", type=int, default=2,
+                    help="sweeps per chain of the CPU baseline leg (one chain per host core)")
+    ap.add_argument("--no-fp64-arm", action="store_true",
+                    help="skip the plain FP64 GPU sweep timed beside the mixed arm")
     ap.add_argument("--group", action="store_true",
                     help="lattices of several configurations swept as one CUDA graph vs one after another")
     ap.add_argument("--renyi-sweeps", type=int, default=10,
@@ -794,14 +930,16 @@ def main():
                     help="τ_int used to convert chain-sweeps/s (default: the committed long-run value)")
     ap.add_argument("--phases", action="store_true",
                     help="print the per-stage clock shares of one untimed sweep to stderr")
+    ap.add_argument("--tau-burn", type=int, default=30, help="burn-in sweeps of --tau-run")
+    ap.add_argument("--tau-run-fp64", type=int, default=0, help="FP64 sweeps of --tau-run (default a third)")
     ap.add_argument("--tau-run", type=int, default=0,
                     help="long run of this many sweeps; prints the workload's τ_int JSON and exits")
     ap.add_argument("--chains", type=int, default=None,
                     help="chains per GPU (profiling of small cases only; bench lines use the workload's)")
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS),
-                    help="configuration (default c2, the metric's; the CPU arm exists for c2 only)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
-                    help="arithmetic of the sweep (mixed: complex sweeps only)")
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS),
+                    help="configuration (default c3 at 256 chains, the metric's)")
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="arithmetic of the headline arm (mixed: complex sweeps only; t-V runs fp64)")
     ap.add_argument("--slmc", action="store_true",
                     help="self-learning cluster moves against local updates (t-U workloads; prints its own line)")
     ap.add_argument("--scee", action="store_true",
@@ -819,21 +957,16 @@ def main():
     global WL, NCHAINS, PRECISION
     WL = WORKLOADS[args.workload]
     NCHAINS = args.chains or WL["chains"]
-    PRECISION = args.precision
-    if args.impl == "reference" and args.workload != "c2":
-        print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement covers the t-V workload only"}))
+    PRECISION = args.precision if make_model().is_complex else "fp64"
+    if args.impl == "reference" and args.workload == "c4":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement covers the t-U and t-V sweeps; "
+                                                              "the t-UV 8x8 square workload is not in it"}))
         return
     if args.group:
         run_group(args)
     elif args.scee:
-        if args.workload == "c2":
-            WL = WORKLOADS["c5"]
-            NCHAINS = args.chains or WL["chains"]
         run_scee(args)
     elif args.slmc:
-        if args.workload == "c2":
-            WL = WORKLOADS["c5"]
-            NCHAINS = args.chains or WL["chains"]
         run_slmc(args)
     elif args.tau_run:
         run_tau(args)

@@ -142,12 +142,16 @@ int kdq_sweep(kdq_handle* h, int32_t sweeps, int32_t record);
 int kdq_get_obs(kdq_handle* h, double* obs, size_t obs_len);
 int kdq_synchronize(kdq_handle* h);
 
-/* t-U and complex t-UV: append to every measurement row the honeycomb
- * structure factors CDW0, CDW1, SDW0, SDW1 with all terms of each correlator
- * (the reference's columns keep only the first term: its `+adjoint(...)`
- * continuation lines are discarded statements, src/tU/phy_update.jl:194-235,
- * src/tUV/phy_update.jl:306-323), making 10 (t-U) or 11 (t-UV) columns; 0
- * restores the reference's 6 or 7.  Drops rows recorded so far.  No
+/* t-U and complex t-UV: append 4 columns to every measurement row, making
+ * 10 (t-U) or 11 (t-UV); 0 restores the reference's 6 or 7.  Honeycomb
+ * lattices: the structure factors CDW0, CDW1, SDW0, SDW1 with all terms of
+ * each correlator (the reference's columns keep only the first term: its
+ * `+adjoint(...)` continuation lines are discarded statements,
+ * src/tU/phy_update.jl:194-235, src/tUV/phy_update.jl:306-323).  Square
+ * lattices (where the reference measures no structure factor): the
+ * staggered charge structure factor at (pi, pi), 0, the staggered spin
+ * structure factor at (pi, pi), 0, i.e. sum_ij e_i e_j <rho_i rho_j> / Ns^2
+ * with e the lattice's two-colouring.  Drops rows recorded so far.  No
  * counterpart in the reference. */
 int kdq_set_measure_full(kdq_handle* h, int32_t enable);
 
@@ -240,13 +244,10 @@ int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32
 int kdq_set_precision(kdq_handle* h, int32_t mode);
 
 /* Per-stage clock counts of the sweep (SM clock cycles, summed over chains):
- * cycles[0] wraps, [1] G updates of accepted proposals and the proposals'
- * bookkeeping, [2] measurements, [3] block products of the stabilisation
- * chain, [4] Householder QR, [5] G recompute, [6] self-learning cluster
- * moves, [7] acceptance ratios of the mixed-precision sweep (the serial part
- * of each local proposal, up to the barrier that publishes its decision; the
- * FP64 sweep evaluates them in windows of proposals and counts them in [1]);
- * cycles has 8 entries.  Enabling resets the counters and adds a barrier
+ * cycles[0] wraps, [1] local updates (the windows of acceptance ratios and
+ * the G updates of accepted proposals), [2] measurements, [3] block products
+ * of the stabilisation chain, [4] Householder QR, [5] G recompute, [6]
+ * self-learning cluster moves, [7] unused (0); cycles has 8 entries.  Enabling resets the counters and adds a barrier
  * per stage.  No counterpart in the reference (which has no tracing). */
 int kdq_enable_phase_timing(kdq_handle* h, int32_t enable);
 int kdq_get_phase_cycles(kdq_handle* h, double* cycles);

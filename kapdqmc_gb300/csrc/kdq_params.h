@@ -52,6 +52,7 @@ struct SweepParams {
   const double* gratio;         // 16: gamma[new]/gamma[old], index old*4+new
   const double* xtab;           // 16: tUV real-type extra weight
   const double* cosr;           // L1*L2 structure-factor phases
+  const double* stag;           // Ns: +1 / -1 two-colouring of a bipartite lattice (all 0 if not bipartite)
   const double* eta;            // 4
   double a, Ht, U, V;
   const int* bx;                // 0-based bond ends

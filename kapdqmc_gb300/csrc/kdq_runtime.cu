@@ -74,7 +74,7 @@ struct kdq_handle {
   std::string err;
   SweepParams P{};
   // model buffers
-  DevBuf nodes, rtab, dtab, vtab, gratio, xtab, cosr, eta, bx, by, site_bonds, dtv;
+  DevBuf nodes, rtab, dtab, vtab, gratio, xtab, cosr, stag, eta, bx, by, site_bonds, dtv;
   DevBuf eK, eKinv, HalfeK, HalfeKinv, K, Pt, PtH;
   // chain buffers
   DevBuf G, W1, W2, Y, Y2, Mss, X, piv, BLs, BRs, s, ctl;
@@ -444,6 +444,38 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
     for (int rx = 1; rx <= L1; ++rx)
       cr[(rx - 1) + (size_t)(ry - 1) * L1] = std::cos(2 * M_PI / L1 * rx + 2 * M_PI / L2 * ry);
   KDQ_CK(upload(h->cosr, cr));
+  // two-colouring of the hopping graph (nonzero K entries): the staggered
+  // sign of the (pi, pi) structure factors on the square lattices
+  {
+    std::vector<double> sg(N, 0.0);
+    auto kabs = [&](int i, int j) {
+      const size_t e = i + (size_t)j * N;
+      return h->kc ? std::hypot(m->K[2 * e], m->K[2 * e + 1]) : std::fabs(m->K[e]);
+    };
+    bool bip = true;
+    std::vector<int> stack;
+    for (int root = 0; root < N && bip; ++root) {
+      if (sg[root] != 0.0) continue;
+      sg[root] = 1.0;
+      stack.assign(1, root);
+      while (!stack.empty() && bip) {
+        const int i = stack.back();
+        stack.pop_back();
+        for (int j = 0; j < N; ++j) {
+          if (j == i || !(kabs(i, j) > 1e-12)) continue;
+          if (sg[j] == 0.0) {
+            sg[j] = -sg[i];
+            stack.push_back(j);
+          } else if (sg[j] == sg[i]) {
+            bip = false;
+            break;
+          }
+        }
+      }
+    }
+    if (!bip) std::fill(sg.begin(), sg.end(), 0.0);
+    KDQ_CK(upload(h->stag, sg));
+  }
   // bonds (0-based) and the tUV per-site bond lists
   int site_nb = 0;
   if (m->kind != KDQ_TU) {
@@ -517,7 +549,7 @@ int kdq_create(kdq_handle** out, const kdq_model_desc* m, int32_t nchains, int32
   P.nodes = h->nodes.as<int64_t>(); P.rtab = h->rtab.as<double>();
   P.dtv = h->dtv.as<double>(); P.dtab = h->dtab.as<double>();
   P.vtab = h->vtab.as<double>(); P.gratio = h->gratio.as<double>(); P.xtab = h->xtab.as<double>();
-  P.cosr = h->cosr.as<double>(); P.eta = h->eta.as<double>();
+  P.cosr = h->cosr.as<double>(); P.stag = h->stag.as<double>(); P.eta = h->eta.as<double>();
   P.a = m->a; P.Ht = m->Ht; P.U = m->U; P.V = m->V;
   P.bx = h->bx.as<int>(); P.by = h->by.as<int>(); P.site_bonds = h->site_bonds.as<int>();
   P.eK = h->eK.p; P.eKinv = h->eKinv.p; P.HalfeK = h->HalfeK.p; P.HalfeKinv = h->HalfeKinv.p;

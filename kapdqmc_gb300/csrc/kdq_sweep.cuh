@@ -67,11 +67,10 @@ __device__ inline void gemm_thin(int M, int N, int K, const TA* A, int lda, cons
 
 // ------------------------------------------------------------ phase timing
 // Optional per-chain clock counts of the sweep's phases (thread 0, between
-// barriers): 0 wraps, 1 G updates and the proposals' bookkeeping, 2
-// measurements, 3 block products of the stabilisation chain, 4 Householder
-// QR, 5 G recompute, 6 cluster moves, 7 acceptance ratios of the FP32
-// working-precision sweep (the FP64 sweep evaluates them in windows of
-// proposals and counts them in 1).
+// barriers): 0 wraps, 1 local updates (windows of acceptance ratios and the
+// G updates of accepted proposals), 2 measurements, 3 block products of the
+// stabilisation chain, 4 Householder QR, 5 G recompute, 6 cluster moves,
+// 7 unused.
 struct PhaseClock {
   unsigned long long* acc;
   long long t;
@@ -352,97 +351,6 @@ __device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G
     }
   }
   return p;
-}
-
-// Local update with the FP32 working-precision G (the FP64 sweep uses
-// propose_window).  Warp 0 evaluates the acceptance ratio (get_r!) and, on
-// acceptance, u' = G[:,S] r into shared memory while the other warps stage
-// the rows G[S,:]; then every thread applies G -= u' (E_S - G[S,:])
-// (Gupdate!, src/public/Gupdate.jl:5-11).
-template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
-__device__ void propose(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int x, int y, uint8_t* sfield,
-                        uint8_t tk, double tu, int logpos, int par) {
-  const SweepParams& P = c.P;
-  const int N = P.Ns;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  constexpr int RK = (KIND == KDQ_TU) ? 1 : 2;
-  Smem<TW>& sm = c.sm;
-  if (warp == 0) {
-    const int sold = *sfield;
-    const int sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
-    const int o = sold - 1, nv = sx - 1;
-    T r00, r01, r10, r11;
-    const double p = ratio(c, G, lt, x, y, o, nv, tu, r00, r01, r10, r11);
-    int acc = tu < p;
-    if (!isfinite(p)) {
-      acc = 0;
-      if (lane == 0) atomicOr(&c.ctl->err, KDQ_FLAG_NAN);
-    }
-    if (acc) {
-      // u' = G[:,S] r (working precision)
-      const TW w00 = cvt<TW>(r00), w01 = cvt<TW>(r01), w10 = cvt<TW>(r10), w11 = cvt<TW>(r11);
-      for (int a = lane; a < N; a += 32) {
-        const TW gx = G[a + (size_t)x * N];
-        if constexpr (RK == 1) {
-          sm.ucol[0][a] = gx * w00;
-        } else {
-          const TW gy = G[a + (size_t)y * N];
-          sm.ucol[0][a] = gx * w00 + gy * w10;
-          sm.ucol[1][a] = gx * w01 + gy * w11;
-        }
-      }
-    }
-    if (lane == 0) {
-      sm.accept[par] = acc;
-      sm.newv = sx;
-      if (c.P.acc_log && logpos >= 0 && logpos < c.P.acc_log_cap)
-        c.P.acc_log[(size_t)c.chain * c.P.acc_log_cap + logpos] = (uint8_t)acc;
-      c.ctl->n_prop += 1;
-      c.ctl->n_acc += acc;
-    }
-  } else {
-    // w = E_S - G[S,:]
-    for (int b = tid - 32; b < N; b += blockDim.x - 32) {
-      sm.wrow[0][b] = (b == x ? one<TW>() : zero<TW>()) - G[x + (size_t)b * N];
-      if constexpr (RK == 2) sm.wrow[1][b] = (b == y ? one<TW>() : zero<TW>()) - G[y + (size_t)b * N];
-    }
-  }
-  __syncthreads();
-  c.clk.lap(7);   // the acceptance ratio: the serial part of a proposal
-  if (sm.accept[par]) {
-    // FP32: memory latency, not arithmetic, bounds the update; warps own
-    // columns, lanes own rows (coalesced), -u' stays in registers across the
-    // columns and the row chunks are unrolled so their loads overlap
-    TW u0[MAXRM], u1[MAXRM];
-#pragma unroll
-    for (int r = 0; r < MAXRM; ++r) {
-      const int a = min(lane + 32 * r, N - 1);
-      u0[r] = -sm.ucol[0][a];
-      if constexpr (RK == 2) u1[r] = -sm.ucol[1][a];
-    }
-    const int nw = blockDim.x >> 5;
-    for (int b = warp; b < N; b += nw) {
-      TW* col = G + (size_t)b * N;
-      const TW w0 = sm.wrow[0][b];
-      TW w1;
-      if constexpr (RK == 2) w1 = sm.wrow[1][b];
-      TW v[MAXRM];
-#pragma unroll
-      for (int r = 0; r < MAXRM; ++r)
-        if (lane + 32 * r < N) v[r] = col[lane + 32 * r];
-#pragma unroll
-      for (int r = 0; r < MAXRM; ++r) {
-        if (lane + 32 * r < N) {
-          madd(v[r], u0[r], w0);
-          if constexpr (RK == 2) madd(v[r], u1[r], w1);
-          col[lane + 32 * r] = v[r];
-        }
-      }
-    }
-    if (tid == 0) *sfield = (uint8_t)sm.newv;
-    __syncthreads();
-  }
-  c.clk.lap(1);
 }
 
 // ------------------------------------------------- self-learning moves (t-U)
@@ -729,7 +637,7 @@ __device__ __forceinline__ void proposal_sites(const SweepParams& P, int jd, int
   }
 }
 
-// FP64 local updates, a window of proposals at a time.  A rejected proposal
+// Local updates, a window of proposals at a time.  A rejected proposal
 // leaves G unchanged, so the acceptance ratios of proposals m0, m0+1, ...
 // are those a one-by-one sweep computes until the first acceptance: lane k
 // of warp 0 evaluates proposal m0+k (get_r!) from the current G, the first
@@ -802,7 +710,39 @@ __device__ int propose_window(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int jd
   __syncthreads();
   const int next = sm.nxt[par];
   if (sm.accept[par]) {
-    rank_update<RK>(G, N, sm.ucol[0], sm.ucol[1], sm.wrow[0], sm.wrow[1], tid, blockDim.x, false, 0, 0);
+    if constexpr (std::is_same_v<T, TW>) {
+      rank_update<RK>(G, N, sm.ucol[0], sm.ucol[1], sm.wrow[0], sm.wrow[1], tid, blockDim.x, false, 0, 0);
+    } else {
+      // FP32: memory latency, not arithmetic, bounds the update; warps own
+      // columns, lanes own rows (coalesced), -u' stays in registers across
+      // the columns and the row chunks are unrolled so their loads overlap
+      TW u0[MAXRM], u1[MAXRM];
+#pragma unroll
+      for (int r = 0; r < MAXRM; ++r) {
+        const int a = min(lane + 32 * r, N - 1);
+        u0[r] = -sm.ucol[0][a];
+        if constexpr (RK == 2) u1[r] = -sm.ucol[1][a];
+      }
+      const int nw = blockDim.x >> 5;
+      for (int b = warp; b < N; b += nw) {
+        TW* col = G + (size_t)b * N;
+        const TW w0 = sm.wrow[0][b];
+        TW w1;
+        if constexpr (RK == 2) w1 = sm.wrow[1][b];
+        TW v[MAXRM];
+#pragma unroll
+        for (int r = 0; r < MAXRM; ++r)
+          if (lane + 32 * r < N) v[r] = col[lane + 32 * r];
+#pragma unroll
+        for (int r = 0; r < MAXRM; ++r) {
+          if (lane + 32 * r < N) {
+            madd(v[r], u0[r], w0);
+            if constexpr (RK == 2) madd(v[r], u1[r], w1);
+            col[lane + 32 * r] = v[r];
+          }
+        }
+      }
+    }
     __syncthreads();
   }
   c.clk.lap(1);
@@ -826,16 +766,8 @@ __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fw
   }
   load_tape(c, qs + off, n);
   const int logbase = (int)(c.ctl->log_pos);
-  if constexpr (std::is_same_v<T, TW>) {
-    int par = 0;
-    for (int m = 0; m < n; par ^= 1) m = propose_window<MAXRM>(c, c.G, lt, j, n, m, logbase, sl, par);
-  } else {
-    for (int m = 0; m < n; ++m) {
-      int x, y, f;
-      proposal_sites<KIND>(P, j, n, m, x, y, f);
-      propose<MAXRM>(c, c.G, lt, x, y, sl + f, c.tk[m], c.tu[m], logbase + m, m & 1);
-    }
-  }
+  int par = 0;
+  for (int m = 0; m < n; par ^= 1) m = propose_window<MAXRM>(c, c.G, lt, j, n, m, logbase, sl, par);
   if (threadIdx.x == 0) c.ctl->log_pos += n;
   finish_tape(c, n);
   __syncthreads();
@@ -1232,6 +1164,26 @@ __device__ void observables(Ctx<KIND, T, KT, TW, KW>& c, const TW* G0) {
         sf[1] += ph * (t1 + t2);
         sf[2] += t1 - t2;
         sf[3] += ph * (t1 - t2);
+      }
+    }
+  } else if constexpr (KIND != KDQ_TV) {
+    // square lattices (t-U, complex t-UV, full measurement only): the
+    // staggered charge and spin structure factors at (pi, pi),
+    // sum_ij e_i e_j <rho_i rho_j> with every term of the honeycomb
+    // correlators above (no counterpart in the reference, whose square
+    // branch measures none); e = the lattice's two-colouring
+    if (P.meas_full && P.stag[0] != 0.0) {
+      const T o = one<T>();
+      for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+        const int i = e % N, j = e / N;
+        const double w = P.stag[i] * P.stag[j];
+        const T gii = cvt<T>(G0[i + (size_t)i * N]), gjj = cvt<T>(G0[j + (size_t)j * N]);
+        const T gij = cvt<T>(G0[e]), gji = cvt<T>(G0[j + (size_t)i * N]);
+        const T del = i == j ? o : zero<T>();
+        const double same = re((o - gii) * (o - gjj) + (del - gij) * gji) + re(conjg(gii * gjj + gij * (del - gji)));
+        const double opp = re((o - gii) * conjg(gjj)) + re(conjg(gii) * (o - gjj));
+        sf[4] += w * (same + opp);
+        sf[6] += w * (same - opp);
       }
     }
   }

@@ -310,8 +310,10 @@ class Sweeper:
         return (out.view(np.complex128) if cplx else out).reshape(N, N, order="F")
 
     def set_measure_full(self, enable: bool = True):
-        """t-U and complex t-UV: also measure the honeycomb structure factors
-        with all terms (4 more columns after the reference's 6 or 7)."""
+        """t-U and complex t-UV: 4 more columns after the reference's 6 or 7:
+        honeycomb, CDW0, CDW1, SDW0, SDW1 with all terms; square lattices,
+        the staggered charge structure factor at (pi, pi), 0, the staggered
+        spin structure factor at (pi, pi), 0."""
         self._ck(self.lib.kdq_set_measure_full(self.h, int(bool(enable))))
         self.n_obs = self.lib.kdq_n_obs(self.h)
 

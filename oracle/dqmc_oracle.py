@@ -298,7 +298,7 @@ class _TUSweep(_Sweep):
         if "HoneyComb" in m.Lattice:
             out[2:] = _honeycomb_sf_quirk(m.site, G0, m.Ns, spinful_real=False)
         if self.full_sf:
-            out += _honeycomb_sf_full(m.site, G0, m.Ns) if "HoneyComb" in m.Lattice else [0.0] * 4
+            out += _honeycomb_sf_full(m.site, G0, m.Ns) if "HoneyComb" in m.Lattice else _square_sf_full(m, G0)
         return np.array(out)
 
     def run(self, sweeps):
@@ -536,7 +536,7 @@ class _TUVSweep(_Sweep):
         if "HoneyComb" in m.Lattice:
             out[3:] = _honeycomb_sf_quirk(m.site, G0, m.Ns, spinful_real=not m.is_complex)
         if self.full_sf:
-            out += _honeycomb_sf_full(m.site, G0, m.Ns) if "HoneyComb" in m.Lattice else [0.0] * 4
+            out += _honeycomb_sf_full(m.site, G0, m.Ns) if "HoneyComb" in m.Lattice else _square_sf_full(m, G0)
         return np.array(out)
 
     def run(self, sweeps):
@@ -655,6 +655,51 @@ def _honeycomb_sf_full(site, G0, Ns):
             SDW1 += ph * (t1 - t2)
     n2 = Ns ** 2
     return [float(np.real(v)) / n2 for v in (CDW0, CDW1, SDW0, SDW1)]
+
+
+def staggered_signs(K):
+    """+1 / -1 per site of a two-colouring of the hopping graph (nonzero K
+    entries), site 0 on +1; all zeros when the graph is not bipartite."""
+    K = np.asarray(K)
+    N = K.shape[0]
+    adj = np.abs(K) > 1e-12
+    sign = np.zeros(N, dtype=np.int64)
+    for root in range(N):
+        if sign[root]:
+            continue
+        sign[root] = 1
+        stack = [root]
+        while stack:
+            i = stack.pop()
+            for j in np.nonzero(adj[i])[0]:
+                if j == i:
+                    continue
+                if sign[j] == 0:
+                    sign[j] = -sign[i]
+                    stack.append(j)
+                elif sign[j] == sign[i]:
+                    return np.zeros(N, dtype=np.int64)
+    return sign
+
+
+def _square_sf_full(model, G0):
+    """The square lattices' counterpart of the corrected honeycomb structure
+    factors (no counterpart in the reference, whose square branch measures
+    none): the staggered charge and spin structure factors at (pi, pi),
+    sum_ij e_i e_j <(rho_i)(rho_j)> / Ns^2 with rho = n_up + n_dn (charge)
+    or n_up - n_dn (spin) and e the two-colouring of the lattice, every term
+    of the correlators as in the honeycomb form; the two shifted-momentum
+    columns stay 0."""
+    eps = staggered_signs(model.K).astype(np.float64)
+    g, c = G0, np.conj
+    d = np.diag(g)
+    same = (1 - d)[:, None] * (1 - d)[None, :] - g * g.T + c(d[:, None] * d[None, :] - g * g.T)
+    same = same + np.diag(d + c(d))            # the delta_ij terms: G_ii + conj(G_ii)
+    opp = (1 - d)[:, None] * c(d)[None, :] + c(d)[:, None] * (1 - d)[None, :]
+    w = eps[:, None] * eps[None, :]
+    n2 = model.Ns ** 2
+    return [float(np.real(np.sum(w * (same + opp)))) / n2, 0.0,
+            float(np.real(np.sum(w * (same - opp)))) / n2, 0.0]
 
 
 def _tv_density_sf(site, G0, Ns):

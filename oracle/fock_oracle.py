@@ -500,3 +500,39 @@ def tu_structure_factors(model):
                     s1 += np.cos(2 * np.pi / L1_ * rx + 2 * np.pi / L2_ * ry) * v
         out += [float(np.real(s0)) / Ns ** 2, float(np.real(s1)) / Ns ** 2]
     return out[0], out[1], out[2], out[3]
+
+
+def tu_staggered_structure_factors(model):
+    """Exact staggered charge and spin structure factors at (pi, pi) of the
+    t-U sweep's measurement on a bipartite (square) lattice, the columns
+    kdq_set_measure_full adds there: sum_ij e_i e_j <rho_i rho_j> / Ns^2 with
+    e the two-colouring of the lattice, rho = n_up + n_dn (charge) or
+    n_up - n_dn (spin), n_up = n_a, n_dn = 1 - n_b as in
+    ``tu_structure_factors``.  Returns (charge, spin)."""
+    import dqmc_oracle as O
+    Ns = model.Ns
+    if Ns > 12:
+        raise ValueError(f"Fock-space sum needs Ns <= 12, got {Ns}")
+    eps = O.staggered_signs(model.K).astype(np.float64)
+    basis = _basis(Ns, Ns // 2)
+    occ = _occupations(basis, Ns)
+    m = occ[:, None, :] - occ[None, :, :]
+    γ, η = np.asarray(model.γ), np.asarray(model.η)
+
+    def V(l):
+        f = {d: np.sum(γ * np.exp(1j * model.α[l - 1] * η * d)) for d in (-1, 0, 1)}
+        return np.prod(np.select([m == -1, m == 0, m == 1], [f[-1], f[0], f[1]]), axis=2)
+
+    R, L, _ = tu_states(model, V)
+    Ha, Hb = gamma_op(model.HalfeK, basis), gamma_op(model.HalfeK.conj(), basis)
+    Hia, Hib = gamma_op(model.HalfeKinv, basis), gamma_op(model.HalfeKinv.conj(), basis)
+    R1 = Ha @ R @ Hb.T
+    L1 = Hia.conj().T @ L @ Hib.conj()
+    norm = np.vdot(L1, R1)
+    nup = occ[:, None, :]
+    ndn = 1.0 - occ[None, :, :]
+    out = []
+    for sgn in (1.0, -1.0):
+        D = np.sum((nup + sgn * ndn) * eps, axis=2)     # sum_i e_i rho_i, (Sa, Sb)
+        out.append(float(np.real(np.vdot(L1, D * D * R1) / norm)) / Ns ** 2)
+    return out[0], out[1]

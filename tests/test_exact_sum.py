@@ -215,3 +215,27 @@ def test_full_structure_factors_converge_to_exact_correlations():
     mu, se = means.mean(0), means.std(0, ddof=1) / np.sqrt(len(means))
     assert np.all(np.abs(mu - exact) < 5 * se), (mu, se, exact)
     assert np.all(se < 0.1 * np.abs(exact))
+
+
+def test_square_staggered_structure_factors_converge_to_exact_correlations():
+    """On a square lattice the full-measurement columns 6 and 8 are the
+    staggered charge and spin structure factors at (pi, pi) (no counterpart
+    in the reference, whose square branch measures none): the oracle's
+    chains average to the exact sum_ij e_i e_j <rho_i rho_j> / Ns^2 of the
+    8-site torus."""
+    m = cases.tu_sq8()
+    exact = np.array(F.tu_staggered_structure_factors(m))
+    n = O.proposals_per_sweep(m)
+    means = []
+    for c in range(12):
+        sweeps = 150
+        ks, us = zip(*(philox.tape(78, c, w, n) for w in range(sweeps)))
+        sw = O.phy_update(m, Initial_s(m, 710 + c), sweeps, O.Tape(np.concatenate(ks), np.concatenate(us)),
+                          True, full_sf=True)
+        rows = np.array(sw.obs_rows)
+        assert np.all(rows[:, 7] == 0) and np.all(rows[:, 9] == 0)
+        means.append(rows[20:, [6, 8]].mean(0))
+    means = np.array(means)
+    mu, se = means.mean(0), means.std(0, ddof=1) / np.sqrt(len(means))
+    assert np.all(np.abs(mu - exact) < 5 * se), (mu, se, exact)
+    assert np.all(se < 0.1 * np.abs(exact))

@@ -77,3 +77,23 @@ def test_cluster_moves_keep_the_distribution():
     mu, se, st = _run(model, 256, "fp64", slmc_args=(params, 1, 4, 16))
     assert st["proposed"] > 0 and 0 < st["accepted"] < st["proposed"]
     _check(model, mu, se)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_square_staggered_structure_factors_reproduce_exact_sum(precision):
+    """Full-measurement columns 6 and 8 on the 8-site square torus: the
+    staggered charge and spin structure factors at (pi, pi)."""
+    model = cases.tu_sq8()
+    exact = np.array(F.tu_staggered_structure_factors(model))
+    fields = np.stack([Initial_s(model, 9100 + c) for c in range(512)])
+    with Sweeper(model, 512) as sw:
+        sw.set_precision(precision)
+        sw.set_measure_full(True)
+        sw.set_fields(fields)
+        sw.set_rng(2468)
+        obs = sw.phy_update(SWEEPS, True)
+    chain_means = obs[:, WARM:, [6, 8]].mean(axis=1)
+    mu = chain_means.mean(axis=0)
+    se = chain_means.std(axis=0, ddof=1) / np.sqrt(len(chain_means))
+    assert np.all(np.abs(mu - exact) < 5 * se), (mu, se, exact)
+    assert np.all(se < 0.05 * np.abs(exact))

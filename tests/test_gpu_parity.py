@@ -257,10 +257,12 @@ def test_grover_det_at_middle_slice():
 
 
 @pytest.mark.parametrize("record", [1, 2])
-@pytest.mark.parametrize("make,ncol", [(cases.tu_honeycomb, 10), (cases.tuv_honeycomb, 11)])
+@pytest.mark.parametrize("make,ncol", [(cases.tu_honeycomb, 10), (cases.tuv_honeycomb, 11),
+                                      (cases.tu_square, 10), (cases.tuv_square, 11)])
 def test_full_structure_factors(record, make, ncol):
     # honeycomb t-U and complex t-UV with the structure factors' discarded
-    # adjoint terms restored (4 columns after the reference's)
+    # adjoint terms restored (4 columns after the reference's); on the square
+    # lattices the staggered (pi, pi) charge and spin structure factors
     model = make()
     nch, sweeps, seed = 2, 2, 77
     fields = np.stack([Initial_s(model, 300 + c) for c in range(nch)])
