@@ -60,27 +60,142 @@ __device__ inline float re(float a) { return a; }
 __device__ inline double abs2(cf a) { return (double)a.x * a.x + (double)a.y * a.y; }
 __device__ inline double abs2(float a) { return (double)a * a; }
 
+// ----------------------------------------------------------- double-float
+// hi + lo, two floats with |lo| <= ulp(hi)/2: a 48-bit significand carried
+// on the FP32 pipe (Dekker, "A floating-point technique for extending the
+// available precision", Numer. Math. 18, 1971; error-free sums after Knuth,
+// TAOCP vol. 2, 4.2.2; error-free products with a fused multiply-add).  The
+// stabilisation type of the mixed-precision sweep: on GB300 the FP32 pipe
+// is ~67x the FP64 pipe, so ~15 FP32 operations per multiply-add still run
+// several times faster than one DFMA.  The intrinsics keep every rounding
+// step explicit (no contraction into FMAs).
+struct df {
+  float hi, lo;
+};
+__device__ __forceinline__ df df_fast2(float s, float e) {   // |s| >= |e|
+  const float h = __fadd_rn(s, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ df df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ df df_from(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - (double)h)};
+}
+__device__ __forceinline__ double df_to(df a) { return (double)a.hi + (double)a.lo; }   // exact
+__device__ __forceinline__ df operator+(df a, df b) {
+  const df s = df_two_sum(a.hi, b.hi);
+  return df_fast2(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df operator-(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
+__device__ __forceinline__ df operator*(df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_fast2(p, e);
+}
+__device__ __forceinline__ df operator*(df a, double b) { return a * df_from(b); }
+__device__ __forceinline__ df operator*(double a, df b) { return df_from(a) * b; }
+__device__ __forceinline__ df operator/(df a, double b) { return df_from(df_to(a) / b); }
+__device__ __forceinline__ df operator/(df a, df b) { return df_from(df_to(a) / df_to(b)); }
+// acc += a * b in one renormalisation (15 FP32 operations)
+__device__ __forceinline__ void madd(df& acc, df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const df s = df_two_sum(acc.hi, p);
+  acc = df_fast2(s.hi, __fadd_rn(s.lo, __fadd_rn(e, acc.lo)));
+}
+__device__ __forceinline__ df conjg(df a) { return a; }
+__device__ __forceinline__ double re(df a) { return df_to(a); }
+__device__ __forceinline__ double abs2(df a) { const double v = df_to(a); return v * v; }
+
+// complex double-float
+struct cdf {
+  df x, y;
+};
+__device__ __forceinline__ cdf operator+(cdf a, cdf b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ cdf operator-(cdf a, cdf b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ cdf operator-(cdf a) { return {-a.x, -a.y}; }
+__device__ __forceinline__ cdf operator*(cdf a, cdf b) {
+  df re_ = a.x * b.x, im_ = a.x * b.y;
+  madd(re_, -a.y, b.y);
+  madd(im_, a.y, b.x);
+  return {re_, im_};
+}
+__device__ __forceinline__ cdf operator*(cdf a, double b) { const df d = df_from(b); return {a.x * d, a.y * d}; }
+__device__ __forceinline__ cdf operator*(double a, cdf b) { return b * a; }
+__device__ __forceinline__ cdf operator/(cdf a, double b) { return {a.x / b, a.y / b}; }
+__device__ __forceinline__ cdf conjg(cdf a) { return {a.x, -a.y}; }
+// quotients are rare (pivots, reflector scalars): through complex128
+__device__ inline cdf cdf_from(cd v) { return {df_from(v.x), df_from(v.y)}; }
+__device__ inline cdf operator/(cdf a, cdf b) {
+  return cdf_from(cd{df_to(a.x), df_to(a.y)} / cd{df_to(b.x), df_to(b.y)});
+}
+__device__ __forceinline__ double re(cdf a) { return df_to(a.x); }
+__device__ __forceinline__ double abs2(cdf a) {
+  const double u = df_to(a.x), v = df_to(a.y);
+  return u * u + v * v;
+}
+__device__ __forceinline__ void madd(cdf& acc, cdf a, cdf b) {
+  madd(acc.x, a.x, b.x);
+  madd(acc.x, -a.y, b.y);
+  madd(acc.y, a.x, b.y);
+  madd(acc.y, a.y, b.x);
+}
+__device__ __forceinline__ void madd(cdf& acc, cdf a, df b) {
+  madd(acc.x, a.x, b);
+  madd(acc.y, a.y, b);
+}
+__device__ __forceinline__ void madd(cdf& acc, df a, cdf b) {
+  madd(acc.x, a, b.x);
+  madd(acc.y, a, b.y);
+}
+
 // conversions between the FP64 and the working types
 template <class To> struct cvt_t;
 template <> struct cvt_t<double> {
   __device__ static double f(double v) { return v; }
   __device__ static double f(float v) { return v; }
+  __device__ static double f(df v) { return df_to(v); }
 };
 template <> struct cvt_t<float> {
   __device__ static float f(double v) { return (float)v; }
   __device__ static float f(float v) { return v; }
+  __device__ static float f(df v) { return __fadd_rn(v.hi, v.lo); }
 };
 template <> struct cvt_t<cd> {
   __device__ static cd f(cd v) { return v; }
   __device__ static cd f(cf v) { return {v.x, v.y}; }
   __device__ static cd f(double v) { return {v, 0.0}; }
   __device__ static cd f(float v) { return {v, 0.0}; }
+  __device__ static cd f(cdf v) { return {df_to(v.x), df_to(v.y)}; }
+  __device__ static cd f(df v) { return {df_to(v), 0.0}; }
 };
 template <> struct cvt_t<cf> {
   __device__ static cf f(cf v) { return v; }
   __device__ static cf f(cd v) { return {(float)v.x, (float)v.y}; }
   __device__ static cf f(double v) { return {(float)v, 0.0f}; }
   __device__ static cf f(float v) { return {v, 0.0f}; }
+  __device__ static cf f(cdf v) { return {__fadd_rn(v.x.hi, v.x.lo), __fadd_rn(v.y.hi, v.y.lo)}; }
+};
+template <> struct cvt_t<df> {
+  __device__ static df f(df v) { return v; }
+  __device__ static df f(double v) { return df_from(v); }
+  __device__ static df f(float v) { return {v, 0.0f}; }
+};
+template <> struct cvt_t<cdf> {
+  __device__ static cdf f(cdf v) { return v; }
+  __device__ static cdf f(cd v) { return {df_from(v.x), df_from(v.y)}; }
+  __device__ static cdf f(cf v) { return {{v.x, 0.0f}, {v.y, 0.0f}}; }
+  __device__ static cdf f(double v) { return {df_from(v), {0.0f, 0.0f}}; }
+  __device__ static cdf f(float v) { return {{v, 0.0f}, {0.0f, 0.0f}}; }
 };
 template <class To, class From> __device__ inline To cvt(From v) { return cvt_t<To>::f(v); }
 
@@ -89,17 +204,28 @@ template <class T> struct low_t;
 template <> struct low_t<double> { using type = float; };
 template <> struct low_t<cd> { using type = cf; };
 
+// the double-float type standing in for an FP64 type
+template <class T> struct dfl_t;
+template <> struct dfl_t<double> { using type = df; };
+template <> struct dfl_t<cd> { using type = cdf; };
+
 template <class T> __device__ inline T zero();
+template <> __device__ inline df zero<df>() { return {0.0f, 0.0f}; }
+template <> __device__ inline cdf zero<cdf>() { return {{0.0f, 0.0f}, {0.0f, 0.0f}}; }
 template <> __device__ inline double zero<double>() { return 0.0; }
 template <> __device__ inline cd zero<cd>() { return {0.0, 0.0}; }
 template <> __device__ inline float zero<float>() { return 0.0f; }
 template <> __device__ inline cf zero<cf>() { return {0.0f, 0.0f}; }
 template <class T> __device__ inline T one();
+template <> __device__ inline df one<df>() { return {1.0f, 0.0f}; }
+template <> __device__ inline cdf one<cdf>() { return {{1.0f, 0.0f}, {0.0f, 0.0f}}; }
 template <> __device__ inline double one<double>() { return 1.0; }
 template <> __device__ inline cd one<cd>() { return {1.0, 0.0}; }
 template <> __device__ inline float one<float>() { return 1.0f; }
 template <> __device__ inline cf one<cf>() { return {1.0f, 0.0f}; }
 template <class T> __device__ inline T from_real(double v);
+template <> __device__ inline df from_real<df>(double v) { return df_from(v); }
+template <> __device__ inline cdf from_real<cdf>(double v) { return {df_from(v), {0.0f, 0.0f}}; }
 template <> __device__ inline double from_real<double>(double v) { return v; }
 template <> __device__ inline cd from_real<cd>(double v) { return {v, 0.0}; }
 template <> __device__ inline float from_real<float>(double v) { return (float)v; }
@@ -148,6 +274,15 @@ __device__ inline float warp_sum(float v) {
   return v;
 }
 __device__ inline cf warp_sum(cf v) { return {warp_sum(v.x), warp_sum(v.y)}; }
+__device__ inline df warp_sum(df v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const df w = {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = v + w;
+  }
+  return v;
+}
+__device__ inline cdf warp_sum(cdf v) { return {warp_sum(v.x), warp_sum(v.y)}; }
 
 // Block-wide sum; `red` is shared scratch of >= 32 doubles.  All threads
 // receive the result.

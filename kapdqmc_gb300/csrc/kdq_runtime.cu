@@ -83,6 +83,7 @@ struct kdq_handle {
   int precision = KDQ_PREC_FP64;
   size_t esz_w = 16;       // bytes per working-precision G element
   DevBuf Yw, Y2w, Gd, eKw, eKinvw, HalfeKw, HalfeKinvw;
+  DevBuf Pts, PtHs;   // mixed: Pt and Pt^H in the double-float stabilisation type
   DevBuf phase;            // per-chain phase clocks when enabled
   DevBuf gmid;             // per-chain G at tau = Nt/2 when enabled
   DevBuf lw;               // per-chain log|det| of the dropped QR factors per node
@@ -196,6 +197,16 @@ __global__ void k_seed_chains(void* BRs, void* BLs, const void* Pt, const void* 
   for (size_t i = threadIdx.x; i < bytes; i += blockDim.x) {
     br[i] = pt[i];
     bl[i] = ph[i];
+  }
+}
+
+// FP64 -> double-float pairs (hi, lo): the mixed sweep's stabilisation type
+__global__ void k_to_dfl(const double* src, float* dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double v = src[i];
+    const float hi = __double2float_rn(v);
+    dst[2 * i] = hi;
+    dst[2 * i + 1] = __double2float_rn(v - (double)hi);
   }
 }
 
@@ -654,8 +665,10 @@ int kdq_init(kdq_handle* h) {
   if (!h) return KDQ_ERR_ARG;
   KDQ_CUDA(h, cudaSetDevice(h->device));
   const size_t fs = (size_t)h->Ns * h->ns;
-  k_seed_chains<<<h->nchains, 256, 0, h->stream>>>(h->BRs.p, h->BLs.p, h->Pt.p, h->PtH.p, fs,
-                                                   h->P.sz_chainB, h->NN, h->esz, h->P.lw);
+  const bool dfl = h->precision == KDQ_PREC_MIXED;
+  k_seed_chains<<<h->nchains, 256, 0, h->stream>>>(h->BRs.p, h->BLs.p, dfl ? h->Pts.p : h->Pt.p,
+                                                   dfl ? h->PtHs.p : h->PtH.p, fs, h->P.sz_chainB, h->NN,
+                                                   h->esz, h->P.lw);
   KDQ_CUDA(h, cudaGetLastError());
   k_reset_ctl<<<(h->nchains + 127) / 128, 128, 0, h->stream>>>(h->ctl.as<ChainCtl>(), h->nchains, 1);
   KDQ_CUDA(h, cudaGetLastError());
@@ -901,6 +914,13 @@ int kdq_set_precision(kdq_handle* h, int32_t mode) {
       k_to_float<<<64, 256, 0, h->stream>>>(src[q]->as<double>(), dst[q]->as<float>(), kn);
       KDQ_CUDA(h, cudaGetLastError());
     }
+    const size_t pn = Nn * (h->gc ? 2 : 1);   // doubles per trial-state matrix
+    KDQ_CUDA(h, h->Pts.alloc(pn * 2 * sizeof(float)));
+    KDQ_CUDA(h, h->PtHs.alloc(pn * 2 * sizeof(float)));
+    k_to_dfl<<<64, 256, 0, h->stream>>>(h->Pt.as<double>(), h->Pts.as<float>(), pn);
+    KDQ_CUDA(h, cudaGetLastError());
+    k_to_dfl<<<64, 256, 0, h->stream>>>(h->PtH.as<double>(), h->PtHs.as<float>(), pn);
+    KDQ_CUDA(h, cudaGetLastError());
     P.Yw = h->Yw.p;
     P.Y2w = h->Y2w.p;
     P.Gd = h->Gd.p;
@@ -912,6 +932,8 @@ int kdq_set_precision(kdq_handle* h, int32_t mode) {
     h->Yw.alloc(0);
     h->Y2w.alloc(0);
     h->Gd.alloc(0);
+    h->Pts.alloc(0);
+    h->PtHs.alloc(0);
     P.Yw = h->Y.p;
     P.Y2w = h->Y2.p;
     P.Gd = h->W1.p;

@@ -21,6 +21,7 @@
 #include "kdq_cnn.cuh"
 #include "kdq_device.cuh"
 #include "kdq_params.h"
+#include "kdq_tc.cuh"
 
 namespace kdq {
 
@@ -53,6 +54,9 @@ template <class T> struct Tiles<6, T> { static constexpr int SM = 3, SN = 6, TM 
 template <> struct Tiles<6, cd> { static constexpr int SM = 2, SN = 6, TM = 2, TN = 6; };
 template <> struct Tiles<3, float> { static constexpr int SM = 3, SN = 9, TM = 3, TN = 4; };
 template <> struct Tiles<3, cf> { static constexpr int SM = 2, SN = 8, TM = 2, TN = 4; };
+template <> struct Tiles<3, df> : Tiles<3, double> {};
+template <> struct Tiles<3, cdf> : Tiles<3, cd> {};
+template <> struct Tiles<6, cdf> : Tiles<6, cd> {};
 
 template <int MAXRM, class T, class TA, class TB, class TC, class TS = double>
 __device__ inline void gemm_sq(int M, int N, int K, const TA* A, int lda, const TB* B, int ldb, TC* C,
@@ -63,6 +67,34 @@ template <int MAXRM, class T, class TA, class TB, class TC, class TS = double>
 __device__ inline void gemm_thin(int M, int N, int K, const TA* A, int lda, const TB* B, int ldb, TC* C,
                                  int ldc, const TS* rs = nullptr, const TS* cs = nullptr) {
   bgemm_t<Tiles<MAXRM, T>::TM, Tiles<MAXRM, T>::TN>(M, N, K, A, lda, B, ldb, C, ldc, rs, cs);
+}
+
+// Products with a kinetic matrix kin (eK, eKinv, HalfeK, HalfeKinv):
+// C = rs .* (kin X) .* cs (kmul_left) or rs .* (X kin) .* cs (kmul_right).
+// The mixed sweep with a real kinetic matrix (no flux) runs them as 3xTF32
+// tensor tiles (kdq_tc.cuh); the FP64 sweep and complex kinetic matrices use
+// the register-tiled CUDA-core GEMM (THIN: the N x ns / ns x N tile shape).
+template <int MAXRM, bool THIN, class TW, class KW>
+__device__ inline void kmul_left(int M, int N, int K, const KW* kin, int ldk, const TW* X, int ldx, TW* C, int ldc,
+                                 const TW* rs = nullptr, const TW* cs = nullptr) {
+  if constexpr (std::is_same_v<TW, cf> && std::is_same_v<KW, float>) {
+    tc_cgemm<true>(M, N, K, kin, ldk, reinterpret_cast<const float*>(X), ldx, C, ldc, rs, cs);
+  } else if constexpr (THIN) {
+    gemm_thin<MAXRM, TW>(M, N, K, kin, ldk, X, ldx, C, ldc, rs, cs);
+  } else {
+    gemm_sq<MAXRM, TW>(M, N, K, kin, ldk, X, ldx, C, ldc, rs, cs);
+  }
+}
+template <int MAXRM, bool THIN, class TW, class KW>
+__device__ inline void kmul_right(int M, int N, int K, const TW* X, int ldx, const KW* kin, int ldk, TW* C, int ldc,
+                                  const TW* rs = nullptr, const TW* cs = nullptr) {
+  if constexpr (std::is_same_v<TW, cf> && std::is_same_v<KW, float>) {
+    tc_cgemm<false>(M, N, K, reinterpret_cast<const float*>(X), ldx, kin, ldk, C, ldc, rs, cs);
+  } else if constexpr (THIN) {
+    gemm_thin<MAXRM, TW>(M, N, K, X, ldx, kin, ldk, C, ldc, rs, cs);
+  } else {
+    gemm_sq<MAXRM, TW>(M, N, K, X, ldx, kin, ldk, C, ldc, rs, cs);
+  }
 }
 
 // ------------------------------------------------------------ phase timing
@@ -108,6 +140,9 @@ struct Smem {
 
 template <int KIND, class T, class KT, class TW, class KW>
 struct Ctx {
+  // arithmetic of the stabilisation (QR, inverse, G recompute): T in the
+  // plain sweep, its double-float counterpart in the mixed one
+  using TS = std::conditional_t<std::is_same_v<T, TW>, T, typename dfl_t<T>::type>;
   const SweepParams& P;
   Smem<TW>& sm;
   uint8_t* tk;     // tape slice: choice index
@@ -119,11 +154,11 @@ struct Ctx {
   TW* W2;          // N x N work (measurement)
   TW* Yw;          // thin factors in working precision (N x ns)
   TW* Y2w;
-  T* Y;            // thin factors in FP64 (alias Yw, Y2w in plain mode)
-  T* Y2;
-  T* Gd;           // N x N FP64 recompute product (alias W1 in plain mode)
-  T* Mss;
-  T* X;
+  TS* Y;           // thin factors in the stabilisation type (alias Yw, Y2w in plain mode)
+  TS* Y2;
+  TS* Gd;          // N x N recompute product (alias W1 in plain mode)
+  TS* Mss;         // ns x ns (the cluster moves borrow it as T)
+  TS* X;
   int* piv;
   uint8_t* s;      // this chain's field, Nt x n_field
   const KW* eK;    // kinetic matrices in working precision
@@ -213,8 +248,8 @@ template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void wrap_fwd_kv(Ctx<KIND, T, KT, TW, KW>& c, TW* G, TW* W, int lt) {
   const int N = c.P.Ns;
   slice_diag(c, lt, +1);
-  gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, G, N, W, N);                       // eK G
-  gemm_sq<MAXRM, TW>(N, N, N, W, N, c.eKinv, N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
+  kmul_left<MAXRM, false>(N, N, N, c.eK, N, G, N, W, N);                         // eK G
+  kmul_right<MAXRM, false>(N, N, N, W, N, c.eKinv, N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
 }
 
 // G <- B_lt^{-1} G B_lt: WrapKV!("Backward","B"), src/tU/GreenMatrix.jl:78-83.
@@ -224,8 +259,8 @@ __device__ void wrap_bwd_kv(Ctx<KIND, T, KT, TW, KW>& c, TW* G, TW* W, int lt) {
   slice_diag(c, lt, -1);
   for (Walk w(N, N); w.ok(); w.next()) G[w.e] = (c.sm.dvec[w.i] * G[w.e]) * c.sm.dinv[w.j];
   __syncthreads();
-  gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, G, N, W, N);
-  gemm_sq<MAXRM, TW>(N, N, N, W, N, c.eK, N, G, N);
+  kmul_left<MAXRM, false>(N, N, N, c.eKinv, N, G, N, W, N);
+  kmul_right<MAXRM, false>(N, N, N, W, N, c.eK, N, G, N);
 }
 
 // tV bond rotation of direction j on both sides of G:
@@ -516,7 +551,7 @@ __device__ void slmc_moves(Ctx<KIND, T, KT, TW, KW>& c, int lt, int visit) {
     __syncthreads();
     const int m = s_m;
     if (!m) continue;
-    T* M = c.Mss;   // m x m, free between recomputes
+    T* M = reinterpret_cast<T*>(c.Mss);   // m x m, free between recomputes (same size as TS)
     for (int e = tid; e < m * m; e += blockDim.x) {
       const int a = e % m, b = e / m;
       const int ja = wrapi(i0 + sidx[a], N), jb = wrapi(i0 + sidx[b], N);
@@ -801,7 +836,7 @@ __device__ TW* apply_slice_left(Ctx<KIND, T, KT, TW, KW>& c, TW* Y, TW* Y2, int 
     }
   } else {
     slice_diag(c, lt, +1);
-    gemm_thin<MAXRM, TW>(N, ns, N, c.eK, N, Y, N, Y2, N, c.sm.dvec, (const TW*)nullptr);
+    kmul_left<MAXRM, true>(N, ns, N, c.eK, N, Y, N, Y2, N, c.sm.dvec);
   }
   return Y2;
 }
@@ -833,7 +868,7 @@ __device__ TW* apply_slice_right(Ctx<KIND, T, KT, TW, KW>& c, TW* Z, TW* Z2, int
       Z[e] = Z[e] * c.sm.dvec[col];
     }
     __syncthreads();
-    gemm_thin<MAXRM, TW>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
+    kmul_right<MAXRM, true>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
   }
   return Z2;
 }
@@ -851,11 +886,13 @@ __device__ inline double* lw_at(const SweepParams& P, int chain, int side, int k
 // fields, kept in ChainCtl (no counterpart in the reference, which discards
 // the R factors).
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
-__device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, bool drift, int node) {
+__device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const typename Ctx<KIND, T, KT, TW, KW>::TS* BL,
+                      const typename Ctx<KIND, T, KT, TW, KW>::TS* BR, bool drift, int node) {
+  using TS = typename Ctx<KIND, T, KT, TW, KW>::TS;
   const int N = c.P.Ns, ns = N / 2;
-  gemm_thin<MAXRM, T>(ns, ns, N, BL, ns, BR, N, c.Mss, ns);
+  gemm_thin<MAXRM, TS>(ns, ns, N, BL, ns, BR, N, c.Mss, ns);
   __shared__ int bad;
-  __shared__ T fcol[KDQ_MAX_NS / 2];
+  __shared__ TS fcol[KDQ_MAX_NS / 2];
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   // (BL BR)^-1 by Gauss-Jordan, then X = (BL BR)^-1 BL and BR X as block GEMMs
@@ -871,14 +908,14 @@ __device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, boo
     c.ctl->det_re = ph.x;
     c.ctl->det_im = ph.y;
   }
-  gemm_thin<MAXRM, T>(ns, N, ns, c.Mss, ns, BL, ns, c.X, ns);
-  gemm_sq<MAXRM, T>(N, N, ns, BR, N, c.X, ns, c.Gd, N);
+  gemm_thin<MAXRM, TS>(ns, N, ns, c.Mss, ns, BL, ns, c.X, ns);
+  gemm_sq<MAXRM, TS>(N, N, ns, BR, N, c.X, ns, c.Gd, N);
   double d2 = 0.0, n2 = 0.0;
   for (Walk w(N, N); w.ok(); w.next()) {
-    T g = zero<T>() - c.Gd[w.e];
-    if (w.i == w.j) g = g + one<T>();
+    TS g = zero<TS>() - c.Gd[w.e];
+    if (w.i == w.j) g = g + one<TS>();
     if (drift) {
-      d2 += abs2(cvt<T>(c.G[w.e]) - g);
+      d2 += abs2(cvt<TS>(c.G[w.e]) - g);
       n2 += abs2(g);
     }
     c.G[w.e] = cvt<TW>(g);
@@ -902,11 +939,12 @@ __device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const T* BL, const T* BR, boo
 // BRs[k+1] = orth_cols(BM(k) BRs[k]) then G recompute at node k+1.
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
+  using TS = typename Ctx<KIND, T, KT, TW, KW>::TS;
   const SweepParams& P = c.P;
   const int N = P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
-  T* BRk = P.BRs<T>(c.chain) + (size_t)(k - 1) * fs;
-  T* BRn = BRk + fs;
+  TS* BRk = P.BRs<TS>(c.chain) + (size_t)(k - 1) * fs;
+  TS* BRn = BRk + fs;
   for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Yw[e] = cvt<TW>(BRk[e]);
   __syncthreads();
   TW* cur = c.Yw;
@@ -916,11 +954,11 @@ __device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
     oth = cur;
     cur = res;
   }
-  T* src;
+  TS* src;
   if constexpr (std::is_same_v<T, TW>) {
     src = cur;
-  } else {   // the block product in working precision, its QR in FP64
-    for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Y[e] = cvt<T>(cur[e]);
+  } else {   // the block product in working precision, its QR in double-float
+    for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Y[e] = cvt<TS>(cur[e]);
     __syncthreads();
     src = c.Y;
   }
@@ -937,7 +975,7 @@ __device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
     b[2] = ph.y;
   }
   c.clk.lap(4);
-  const T* BLn = P.BLs<T>(c.chain) + (size_t)k * fs;
+  const TS* BLn = P.BLs<TS>(c.chain) + (size_t)k * fs;
   get_G<MAXRM>(c, BLn, BRn, true, k + 1);
   c.clk.lap(5);
   if (threadIdx.x == 0) c.ctl->idx = k + 1;
@@ -946,11 +984,12 @@ __device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
 // BLs[k] = orth_rows(BLs[k+1] BM(k)) then (optionally) G recompute.
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute, bool drift) {
+  using TS = typename Ctx<KIND, T, KT, TW, KW>::TS;
   const SweepParams& P = c.P;
   const int N = P.Ns, ns = N / 2;
   const size_t fs = (size_t)N * ns;
-  T* BLk = P.BLs<T>(c.chain) + (size_t)(k - 1) * fs;
-  const T* BLn = BLk + fs;
+  TS* BLk = P.BLs<TS>(c.chain) + (size_t)(k - 1) * fs;
+  const TS* BLn = BLk + fs;
   for (size_t e = threadIdx.x; e < fs; e += blockDim.x) c.Yw[e] = cvt<TW>(BLn[e]);
   __syncthreads();
   TW* cur = c.Yw;
@@ -960,9 +999,9 @@ __device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute
     oth = cur;
     cur = res;
   }
-  // orth_rows: QR of Z^H (N x ns) in FP64, BL = Q^H
-  T* A;
-  T* Q;
+  // orth_rows: QR of Z^H (N x ns) in the stabilisation type, BL = Q^H
+  TS* A;
+  TS* Q;
   if constexpr (std::is_same_v<T, TW>) {
     A = oth;
     Q = cur;
@@ -972,7 +1011,7 @@ __device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute
   }
   for (size_t e = threadIdx.x; e < fs; e += blockDim.x) {
     const int r = e % ns, col = e / ns;
-    A[col + (size_t)r * N] = conjg(cvt<T>(cur[e]));
+    A[col + (size_t)r * N] = conjg(cvt<TS>(cur[e]));
   }
   __syncthreads();
   c.clk.lap(3);
@@ -993,7 +1032,7 @@ __device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute
   }
   __syncthreads();
   c.clk.lap(4);
-  if (recompute) get_G<MAXRM>(c, BLk, P.BRs<T>(c.chain) + (size_t)(k - 1) * fs, drift, k);
+  if (recompute) get_G<MAXRM>(c, BLk, P.BRs<TS>(c.chain) + (size_t)(k - 1) * fs, drift, k);
   c.clk.lap(5);
   if (threadIdx.x == 0) c.ctl->idx = k;
 }
@@ -1055,8 +1094,8 @@ __device__ void measure(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
       }
     }
   }
-  gemm_sq<MAXRM, TW>(N, N, N, c.HalfeK, N, G0, N, W, N);
-  gemm_sq<MAXRM, TW>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
+  kmul_left<MAXRM, false>(N, N, N, c.HalfeK, N, G0, N, W, N);
+  kmul_right<MAXRM, false>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
   observables(c, G0);
 }
 
@@ -1276,15 +1315,15 @@ __device__ void mul_slice(Ctx<KIND, T, KT, TW, KW>& c, TW* X, TW* W, int lt, con
     if (right && !inv) {          // X D eK
       for (Walk w(N, N); w.ok(); w.next()) X[w.e] = X[w.e] * d[w.j];
       __syncthreads();
-      gemm_sq<MAXRM, TW>(N, N, N, X, N, c.eK, N, W, N);
+      kmul_right<MAXRM, false>(N, N, N, X, N, c.eK, N, W, N);
     } else if (right) {           // X eKinv D^-1
-      gemm_sq<MAXRM, TW>(N, N, N, X, N, c.eKinv, N, W, N, (const TW*)nullptr, d);
+      kmul_right<MAXRM, false>(N, N, N, X, N, c.eKinv, N, W, N, (const TW*)nullptr, d);
     } else if (!inv) {            // D eK X
-      gemm_sq<MAXRM, TW>(N, N, N, c.eK, N, X, N, W, N, d, (const TW*)nullptr);
+      kmul_left<MAXRM, false>(N, N, N, c.eK, N, X, N, W, N, d, (const TW*)nullptr);
     } else {                      // eKinv D^-1 X
       for (Walk w(N, N); w.ok(); w.next()) X[w.e] = d[w.i] * X[w.e];
       __syncthreads();
-      gemm_sq<MAXRM, TW>(N, N, N, c.eKinv, N, X, N, W, N);
+      kmul_left<MAXRM, false>(N, N, N, c.eKinv, N, X, N, W, N);
     }
     for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = W[e];
     __syncthreads();
@@ -1360,6 +1399,7 @@ template <int KIND, class T, class KT, int MAXRM, bool MIXED>
 __global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, int mode, int k) {
   using TW = std::conditional_t<MIXED, typename low_t<T>::type, T>;
   using KW = std::conditional_t<MIXED, typename low_t<KT>::type, KT>;
+  using TS = typename Ctx<KIND, T, KT, TW, KW>::TS;
   extern __shared__ double dyn_d[];
   __shared__ Smem<TW> sm;
   const int chain = blockIdx.x;
@@ -1379,11 +1419,11 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, i
                              static_cast<TW*>(P.W2) + cNN,
                              static_cast<TW*>(P.Yw) + cNn,
                              static_cast<TW*>(P.Y2w) + cNn,
-                             static_cast<T*>(P.Y) + cNn,
-                             static_cast<T*>(P.Y2) + cNn,
-                             static_cast<T*>(P.Gd) + cNN,
-                             static_cast<T*>(P.Mss) + (size_t)chain * P.sz_nn,
-                             static_cast<T*>(P.X) + cNn,
+                             static_cast<TS*>(P.Y) + cNn,
+                             static_cast<TS*>(P.Y2) + cNn,
+                             static_cast<TS*>(P.Gd) + cNN,
+                             static_cast<TS*>(P.Mss) + (size_t)chain * P.sz_nn,
+                             static_cast<TS*>(P.X) + cNn,
                              P.piv + (size_t)chain * (N / 2),
                              P.s + (size_t)chain * P.Nt * P.n_field,
                              static_cast<const KW*>(P.eK),

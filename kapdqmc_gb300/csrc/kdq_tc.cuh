@@ -1,0 +1,194 @@
+// Split-precision (3xTF32) products of the mixed-precision sweep on the
+// tensor pipe: complex FP32 matrices times the real FP32 kinetic matrices
+// (eK, eKinv, HalfeK, HalfeKinv of a hopping matrix without flux).
+//
+// Every FP32 operand x is split into two TF32 values, hi = tf32(x) and
+// lo = tf32(x - hi) (x - hi is exact in FP32), and each product A B is
+// accumulated in FP32 as A_lo B_hi + A_hi B_lo + A_hi B_hi (the A_lo B_lo
+// term, ~2^-22 relative, is dropped): about FP32 accuracy from TF32 tensor
+// operations.  Tiles are mma.sync.m16n8k8 (TF32 inputs, FP32 accumulators);
+// the whole CTA computes one product, each warp a 3 x 4 block of 16 x 8
+// tiles, operands read through L1 (the kinetic matrix is shared by every
+// chain of the launch and stays in L2).
+//
+// A complex matrix is used through a real view of its interleaved (re, im)
+// floats, arranged so that the real and imaginary part of one complex entry
+// land in the same thread's accumulators:
+//   left  C = A_real B_cplx: real view of B and C has 2N columns, column
+//         2j + r = part r of complex column j (an 8-column tile = 4 complex
+//         columns; accumulators c0/c1 are re/im of one entry);
+//   right C = A_cplx B_real: real view of A and C has 2M rows, tile rows
+//         0..7 = re and 8..15 = im of 8 complex rows (c0/c2 and c1/c3).
+// The epilogue applies the optional complex row and column scalings
+// C = rs[i] (A B)[i,j] cs[j] of the slice wraps and block products.
+//
+// Reference products (KAPDQMC): WrapKV! src/tU/GreenMatrix.jl:56-86 (and
+// src/tUV/GreenMatrix.jl:92-122), BM_F! src/tU/GreenMatrix.jl:10-27, and the
+// measurement wraps of phy_measure src/tU/phy_update.jl:154-182.
+#pragma once
+#include <cstdint>
+
+#include "kdq_device.cuh"
+
+namespace kdq {
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
+  hi = tf32_rna(x);
+  lo = tf32_rna(__fsub_rn(x, __uint_as_float(hi)));
+}
+
+// d += a b for one m16n8k8 TF32 tile (FP32 accumulators)
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+constexpr int TC_WM = 3;   // m16 tiles per warp
+constexpr int TC_WN = 4;   // n8 tiles per warp
+
+// C (M x N complex) = rs .* (A B) .* cs with A real (M x K, lda) and B complex
+// (K x N, ldb complex elements) when LEFT, A complex (M x K, lda) and B real
+// (K x N, ldb) otherwise.  C must not alias A or B.  rs (M) and cs (N) may be
+// NULL.  All threads of the CTA call it; it ends with __syncthreads().
+template <bool LEFT>
+__device__ __noinline__ void tc_cgemm(int M, int N, int K, const float* __restrict__ A, int lda,
+                                      const float* __restrict__ B, int ldb, cf* __restrict__ C, int ldc,
+                                      const cf* rs, const cf* cs) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  // real-view extents in m16 / n8 tiles
+  const int MT = LEFT ? (M + 15) / 16 : (M + 7) / 8;
+  const int NT = LEFT ? (N + 3) / 4 : (N + 7) / 8;
+  const int KT = (K + 7) / 8;
+  const int WMT = (MT + TC_WM - 1) / TC_WM, WNT = (NT + TC_WN - 1) / TC_WN;
+  float* Cf = reinterpret_cast<float*>(C);
+  for (int wt = warp; wt < WMT * WNT; wt += nwarps) {
+    const int mt0 = (wt % WMT) * TC_WM, nt0 = (wt / WMT) * TC_WN;
+    float acc[TC_WM][TC_WN][4];
+#pragma unroll
+    for (int i = 0; i < TC_WM; ++i)
+#pragma unroll
+      for (int j = 0; j < TC_WN; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.0f;
+    // element offsets of this thread's fragment rows / columns (-1: outside)
+    int arow[TC_WM][2];   // A: real-view rows g and g + 8 of each m tile
+#pragma unroll
+    for (int i = 0; i < TC_WM; ++i)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int mt = mt0 + i;
+        if (LEFT) {
+          const int m = mt * 16 + g + 8 * h;
+          arow[i][h] = (mt < MT && m < M) ? m : -1;
+        } else {   // complex row 8 mt + g, part h
+          const int m = mt * 8 + g;
+          arow[i][h] = (mt < MT && m < M) ? 2 * m + h : -1;
+        }
+      }
+    int bcol[TC_WN];   // B: real-view column g of each n tile
+#pragma unroll
+    for (int j = 0; j < TC_WN; ++j) {
+      const int nt = nt0 + j;
+      if (LEFT) {   // complex column 4 nt + g / 2, part g & 1
+        const int n = nt * 4 + (g >> 1);
+        bcol[j] = (nt < NT && n < N) ? 2 * n * ldb + (g & 1) : -1;
+      } else {
+        const int n = nt * 8 + g;
+        bcol[j] = (nt < NT && n < N) ? n * ldb : -1;
+      }
+    }
+    for (int kt = 0; kt < KT; ++kt) {
+      const int k0 = kt * 8 + t, k1 = k0 + 4;
+      const bool kin0 = k0 < K, kin1 = k1 < K;
+      uint32_t ah[TC_WM][4], al[TC_WM][4];
+#pragma unroll
+      for (int i = 0; i < TC_WM; ++i) {
+        float v[4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int r = arow[i][h];
+          if (LEFT) {
+            v[h] = (r >= 0 && kin0) ? A[r + (size_t)k0 * lda] : 0.0f;
+            v[2 + h] = (r >= 0 && kin1) ? A[r + (size_t)k1 * lda] : 0.0f;
+          } else {
+            v[h] = (r >= 0 && kin0) ? A[r + (size_t)k0 * 2 * lda] : 0.0f;
+            v[2 + h] = (r >= 0 && kin1) ? A[r + (size_t)k1 * 2 * lda] : 0.0f;
+          }
+        }
+        // fragment order: a0 (row g, col t), a1 (row g+8, col t), a2 (row g, col t+4), a3 (row g+8, col t+4)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tf32_split(v[q], ah[i][q], al[i][q]);
+      }
+      uint32_t bh[TC_WN][2], bl[TC_WN][2];
+#pragma unroll
+      for (int j = 0; j < TC_WN; ++j) {
+        const int c = bcol[j];
+        float v0, v1;
+        if (LEFT) {
+          v0 = (c >= 0 && kin0) ? B[c + 2 * k0] : 0.0f;
+          v1 = (c >= 0 && kin1) ? B[c + 2 * k1] : 0.0f;
+        } else {
+          v0 = (c >= 0 && kin0) ? B[c + k0] : 0.0f;
+          v1 = (c >= 0 && kin1) ? B[c + k1] : 0.0f;
+        }
+        tf32_split(v0, bh[j][0], bl[j][0]);
+        tf32_split(v1, bh[j][1], bl[j][1]);
+      }
+#pragma unroll
+      for (int i = 0; i < TC_WM; ++i)
+#pragma unroll
+        for (int j = 0; j < TC_WN; ++j) {
+          mma_tf32(acc[i][j], al[i][0], al[i][1], al[i][2], al[i][3], bh[j][0], bh[j][1]);
+          mma_tf32(acc[i][j], ah[i][0], ah[i][1], ah[i][2], ah[i][3], bl[j][0], bl[j][1]);
+          mma_tf32(acc[i][j], ah[i][0], ah[i][1], ah[i][2], ah[i][3], bh[j][0], bh[j][1]);
+        }
+    }
+    // epilogue: complex entries, optional scalings
+#pragma unroll
+    for (int i = 0; i < TC_WM; ++i)
+#pragma unroll
+      for (int j = 0; j < TC_WN; ++j) {
+        const int mt = mt0 + i, nt = nt0 + j;
+        if (mt >= MT || nt >= NT) continue;
+        cf e[2];
+        int row[2], col[2];
+        if (LEFT) {   // entries (16 mt + g, 4 nt + t) and (16 mt + g + 8, 4 nt + t)
+          e[0] = cf{acc[i][j][0], acc[i][j][1]};
+          e[1] = cf{acc[i][j][2], acc[i][j][3]};
+          row[0] = mt * 16 + g;
+          row[1] = row[0] + 8;
+          col[0] = col[1] = nt * 4 + t;
+        } else {      // entries (8 mt + g, 8 nt + 2t) and (8 mt + g, 8 nt + 2t + 1)
+          e[0] = cf{acc[i][j][0], acc[i][j][2]};
+          e[1] = cf{acc[i][j][1], acc[i][j][3]};
+          row[0] = row[1] = mt * 8 + g;
+          col[0] = nt * 8 + 2 * t;
+          col[1] = col[0] + 1;
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          if (row[q] >= M || col[q] >= N) continue;
+          cf v = e[q];
+          if (rs) v = rs[row[q]] * v;
+          if (cs) v = v * cs[col[q]];
+          const size_t o = 2 * (row[q] + (size_t)col[q] * ldc);
+          Cf[o] = v.x;
+          Cf[o + 1] = v.y;
+        }
+      }
+  }
+  __syncthreads();
+}
+
+}  // namespace kdq
