@@ -132,6 +132,7 @@ struct Smem {
   T ucol[4][KDQ_MAX_NS];   // update vectors: [2 buf + r], two buffers of rank 2
   T wrow[4][KDQ_MAX_NS];
   T rr[4];
+  int site[2];     // the accepted proposal's sites (delayed updates)
   int accept[2];
   int nxt[2];      // next proposal of a layer after a window (FP64)
   int newv;
@@ -320,14 +321,11 @@ __device__ void tv_rotate(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int j, int
 
 // ---------------------------------------------------------- local updates
 // Proposal decision and rank-k update (k = 1 for tU, 2 for tV and tUV).
-// Acceptance ratio p of the proposal sold -> sx (0-based o, nv) on the
-// sites S = {x} (t-U) or {x, y} at slice lt, from G[S,S] (get_r!), and, when
-// tu < p, r = (I + Delta (I - G_SS))^-1 Delta for the update.
+// ratio_ss: acceptance ratio from the entries G[S,S] (get_r!).
 template <int KIND, class T, class KT, class TW, class KW>
-__device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G, int lt, int x, int y, int o,
-                                        int nv, double tu, T& r00, T& r01, T& r10, T& r11) {
+__device__ __forceinline__ double ratio_ss(Ctx<KIND, T, KT, TW, KW>& c, int lt, int o, int nv, double tu, T gxx,
+                                           T gxy, T gyx, T gyy, T& r00, T& r01, T& r10, T& r11) {
   const SweepParams& P = c.P;
-  const int N = P.Ns;
   double p;
   r01 = zero<T>();
   r10 = zero<T>();
@@ -335,7 +333,7 @@ __device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G
   if constexpr (KIND == KDQ_TU) {
     // get_r!, src/tU/GreenMatrix.jl:49-54; γ ratio src/tU/phy_update.jl:261
     const cd Δ = reinterpret_cast<const cd*>(P.rtab)[(size_t)(lt - 1) * 16 + o * 4 + nv];
-    const cd g = cvt<cd>(G[x + (size_t)x * N]);
+    const cd g = cvt<cd>(gxx);
     const cd pc = cd{1.0, 0.0} + Δ * (cd{1.0, 0.0} - g);
     p = abs2(pc) * P.gratio[o * 4 + nv];
     if constexpr (std::is_same_v<T, TW>) {
@@ -352,11 +350,10 @@ __device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G
     // proposal starts at the G-dependent products.
     const double* dt = P.dtv + ((size_t)(lt - 1) * 16 + o * 4 + nv) * 3;
     const double dd = dt[0], do_ = dt[1], dp = dt[2];
-    const double gxx = re(G[x + (size_t)x * N]), gxy = re(G[x + (size_t)y * N]);
-    const double gyx = re(G[y + (size_t)x * N]), gyy = re(G[y + (size_t)y * N]);
+    const double Gxx = re(gxx), Gxy = re(gxy), Gyx = re(gyx), Gyy = re(gyy);
     // r = I + Δ - Δ G_SS
-    const double a00 = dp - (dd * gxx + do_ * gyx), a01 = do_ - (dd * gxy + do_ * gyy);
-    const double a10 = do_ - (do_ * gxx + dd * gyx), a11 = dp - (do_ * gxy + dd * gyy);
+    const double a00 = dp - (dd * Gxx + do_ * Gyx), a01 = do_ - (dd * Gxy + do_ * Gyy);
+    const double a10 = do_ - (do_ * Gxx + dd * Gyx), a11 = dp - (do_ * Gxy + dd * Gyy);
     const double det = a00 * a11 - a01 * a10;
     p = det * P.gratio[o * 4 + nv];
     if (tu < p) {   // r = r^-1 Δ = adj(r) Δ / det, needed only for the update
@@ -369,8 +366,6 @@ __device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G
   } else {
     // get_r!, src/tUV/GreenMatrix.jl:73-89; weight src/tUV/phy_update.jl:193-197
     const T* t2 = reinterpret_cast<const T*>(P.rtab) + (size_t)(o * 4 + nv) * 2;
-    const T gxx = cvt<T>(G[x + (size_t)x * N]), gxy = cvt<T>(G[x + (size_t)y * N]);
-    const T gyx = cvt<T>(G[y + (size_t)x * N]), gyy = cvt<T>(G[y + (size_t)y * N]);
     T a00 = t2[0] - t2[0] * gxx, a01 = zero<T>() - t2[0] * gxy;
     T a10 = zero<T>() - t2[1] * gyx, a11 = t2[1] - t2[1] * gyy;
     a00 = a00 + one<T>();
@@ -386,6 +381,23 @@ __device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G
     }
   }
   return p;
+}
+
+// Acceptance ratio p of the proposal sold -> sx (0-based o, nv) on the
+// sites S = {x} (t-U) or {x, y} at slice lt, from G[S,S] (get_r!), and, when
+// tu < p, r = (I + Delta (I - G_SS))^-1 Delta for the update.
+template <int KIND, class T, class KT, class TW, class KW>
+__device__ __forceinline__ double ratio(Ctx<KIND, T, KT, TW, KW>& c, const TW* G, int lt, int x, int y, int o,
+                                        int nv, double tu, T& r00, T& r01, T& r10, T& r11) {
+  const int N = c.P.Ns;
+  const T gxx = cvt<T>(G[x + (size_t)x * N]);
+  T gxy = zero<T>(), gyx = zero<T>(), gyy = zero<T>();
+  if constexpr (KIND != KDQ_TU) {
+    gxy = cvt<T>(G[x + (size_t)y * N]);
+    gyx = cvt<T>(G[y + (size_t)x * N]);
+    gyy = cvt<T>(G[y + (size_t)y * N]);
+  }
+  return ratio_ss(c, lt, o, nv, tu, gxx, gxy, gyx, gyy, r00, r01, r10, r11);
 }
 
 // ------------------------------------------------- self-learning moves (t-U)
@@ -672,7 +684,7 @@ __device__ __forceinline__ void proposal_sites(const SweepParams& P, int jd, int
   }
 }
 
-// Local updates, a window of proposals at a time.  A rejected proposal
+// FP64 local updates, a window of proposals at a time.  A rejected proposal
 // leaves G unchanged, so the acceptance ratios of proposals m0, m0+1, ...
 // are those a one-by-one sweep computes until the first acceptance: lane k
 // of warp 0 evaluates proposal m0+k (get_r!) from the current G, the first
@@ -745,40 +757,143 @@ __device__ int propose_window(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int jd
   __syncthreads();
   const int next = sm.nxt[par];
   if (sm.accept[par]) {
-    if constexpr (std::is_same_v<T, TW>) {
-      rank_update<RK>(G, N, sm.ucol[0], sm.ucol[1], sm.wrow[0], sm.wrow[1], tid, blockDim.x, false, 0, 0);
-    } else {
-      // FP32: memory latency, not arithmetic, bounds the update; warps own
-      // columns, lanes own rows (coalesced), -u' stays in registers across
-      // the columns and the row chunks are unrolled so their loads overlap
-      TW u0[MAXRM], u1[MAXRM];
+    rank_update<RK>(G, N, sm.ucol[0], sm.ucol[1], sm.wrow[0], sm.wrow[1], tid, blockDim.x, false, 0, 0);
+    __syncthreads();
+  }
+  c.clk.lap(1);
+  return next;
+}
+
+// Delayed updates of the mixed-precision sweep (Alvarez, Loh, Scalapino,
+// Comput. Phys. Commun. 179, 2008; no counterpart in the reference, which
+// updates G after every acceptance, src/public/Gupdate.jl:5-11).  The rank-1
+// (t-U) or rank-2 (t-V, t-UV) changes of accepted proposals are kept as
+// vector pairs u_q = (G[:,S] r)_q, w_q = (E_S - G[S,:])_q in shared memory,
+// the current Green's function being G - sum_q u_q w_q^T; a proposal's
+// ratio and an accepted proposal's new vectors read G through that sum, and
+// G itself is rewritten once per KDQ_DELAY vectors (delayed_flush) instead
+// of once per acceptance: the N x N matrix streams through L2 KDQ_DELAY / k
+// times less often.  Decisions use the same windows as the FP64 sweep.
+#define KDQ_DELAY 8
+template <class TW>
+struct Delay {
+  TW U[KDQ_DELAY][KDQ_MAX_NS];
+  TW W[KDQ_DELAY][KDQ_MAX_NS];
+};
+
+// G -= sum_{q < kd} U[q] W[q]^T; warps own columns, lanes rows.
+template <class TW>
+__device__ void delayed_flush(TW* G, int N, const Delay<TW>& db, int kd) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int b = warp; b < N; b += nw) {
+    TW wb[KDQ_DELAY];
 #pragma unroll
-      for (int r = 0; r < MAXRM; ++r) {
-        const int a = min(lane + 32 * r, N - 1);
-        u0[r] = -sm.ucol[0][a];
-        if constexpr (RK == 2) u1[r] = -sm.ucol[1][a];
+    for (int q = 0; q < KDQ_DELAY; ++q) wb[q] = q < kd ? db.W[q][b] : zero<TW>();
+    TW* col = G + (size_t)b * N;
+    for (int a = lane; a < N; a += 32) {
+      TW v = col[a];
+#pragma unroll
+      for (int q = 0; q < KDQ_DELAY; ++q)
+        if (q < kd) madd(v, -db.U[q][a], wb[q]);
+      col[a] = v;
+    }
+  }
+  __syncthreads();
+}
+
+// (G - U W)[i, j] for the kd pending vector pairs
+template <class TW>
+__device__ __forceinline__ TW delayed_entry(const TW* G, int N, const Delay<TW>& db, int kd, int i, int j) {
+  TW v = G[i + (size_t)j * N];
+  for (int q = 0; q < kd; ++q) madd(v, -db.U[q][i], db.W[q][j]);
+  return v;
+}
+
+// One window of proposals with delayed updates; kd (uniform over the CTA)
+// is the number of pending vector pairs.  Returns the next proposal index.
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ int propose_window_delayed(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int jd, int n, int m0,
+                                      int logbase, uint8_t* sl, int par, Delay<TW>& db, int& kd) {
+  const SweepParams& P = c.P;
+  const int N = P.Ns;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int RK = (KIND == KDQ_TU) ? 1 : 2;
+  Smem<TW>& sm = c.sm;
+  if (warp == 0) {
+    const int W = min(32, n - m0);
+    const int m = m0 + lane;
+    const bool valid = lane < W;
+    int x = 0, y = 0, f = 0, sx = 0, acc = 0;
+    bool bad = false;
+    T r00 = zero<T>(), r01 = zero<T>(), r10 = zero<T>(), r11 = zero<T>();
+    if (valid) {
+      proposal_sites<KIND>(P, jd, n, m, x, y, f);
+      const int sold = sl[f];
+      const int tk = c.tk[m];
+      sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
+      const T gxx = cvt<T>(delayed_entry(G, N, db, kd, x, x));
+      T gxy = zero<T>(), gyx = zero<T>(), gyy = zero<T>();
+      if constexpr (RK == 2) {
+        gxy = cvt<T>(delayed_entry(G, N, db, kd, x, y));
+        gyx = cvt<T>(delayed_entry(G, N, db, kd, y, x));
+        gyy = cvt<T>(delayed_entry(G, N, db, kd, y, y));
       }
-      const int nw = blockDim.x >> 5;
-      for (int b = warp; b < N; b += nw) {
-        TW* col = G + (size_t)b * N;
-        const TW w0 = sm.wrow[0][b];
-        TW w1;
-        if constexpr (RK == 2) w1 = sm.wrow[1][b];
-        TW v[MAXRM];
-#pragma unroll
-        for (int r = 0; r < MAXRM; ++r)
-          if (lane + 32 * r < N) v[r] = col[lane + 32 * r];
-#pragma unroll
-        for (int r = 0; r < MAXRM; ++r) {
-          if (lane + 32 * r < N) {
-            madd(v[r], u0[r], w0);
-            if constexpr (RK == 2) madd(v[r], u1[r], w1);
-            col[lane + 32 * r] = v[r];
-          }
-        }
+      const double p = ratio_ss(c, lt, sold - 1, sx - 1, c.tu[m], gxx, gxy, gyx, gyy, r00, r01, r10, r11);
+      bad = !isfinite(p);
+      acc = !bad && c.tu[m] < p;
+    }
+    const unsigned amask = __ballot_sync(0xffffffffu, acc);
+    const int ja = amask ? __ffs(amask) - 1 : W;   // first accepting lane, W if none
+    const int nres = ja < W ? ja + 1 : W;          // proposals decided by this window
+    if (lane < nres && bad) atomicOr(&c.ctl->err, KDQ_FLAG_NAN);
+    if (lane < nres) {
+      const int logpos = logbase + m;
+      if (P.acc_log && logpos >= 0 && logpos < P.acc_log_cap)
+        P.acc_log[(size_t)c.chain * P.acc_log_cap + logpos] = (uint8_t)(lane == ja);
+    }
+    if (ja < W && lane == ja) {
+      sl[f] = (uint8_t)sx;   // lane W (no acceptance) holds no proposal
+      sm.site[0] = x;
+      sm.site[1] = y;
+      sm.rr[0] = cvt<TW>(r00);
+      sm.rr[1] = cvt<TW>(r01);
+      sm.rr[2] = cvt<TW>(r10);
+      sm.rr[3] = cvt<TW>(r11);
+    }
+    if (lane == 0) {
+      sm.accept[par] = ja < W;
+      sm.nxt[par] = m0 + nres;
+      c.ctl->n_prop += nres;
+      c.ctl->n_acc += (ja < W) ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  const int next = sm.nxt[par];
+  if (sm.accept[par]) {
+    // the accepted proposal's vectors from the current G (= G - U W)
+    const int xa = sm.site[0], ya = sm.site[1];
+    const TW w00 = sm.rr[0], w01 = sm.rr[1], w10 = sm.rr[2], w11 = sm.rr[3];
+    for (int a = tid; a < N; a += blockDim.x) {
+      const TW gx = delayed_entry(G, N, db, kd, a, xa);
+      const TW rx = delayed_entry(G, N, db, kd, xa, a);
+      if constexpr (RK == 1) {
+        db.U[kd][a] = gx * w00;
+        db.W[kd][a] = (a == xa ? one<TW>() : zero<TW>()) - rx;
+      } else {
+        const TW gy = delayed_entry(G, N, db, kd, a, ya);
+        const TW ry = delayed_entry(G, N, db, kd, ya, a);
+        db.U[kd][a] = gx * w00 + gy * w10;
+        db.U[kd + 1][a] = gx * w01 + gy * w11;
+        db.W[kd][a] = (a == xa ? one<TW>() : zero<TW>()) - rx;
+        db.W[kd + 1][a] = (a == ya ? one<TW>() : zero<TW>()) - ry;
       }
     }
     __syncthreads();
+    kd += RK;
+    if (kd + RK > KDQ_DELAY) {   // no room for another acceptance
+      delayed_flush(G, N, db, kd);
+      kd = 0;
+    }
   }
   c.clk.lap(1);
   return next;
@@ -802,7 +917,14 @@ __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fw
   load_tape(c, qs + off, n);
   const int logbase = (int)(c.ctl->log_pos);
   int par = 0;
-  for (int m = 0; m < n; par ^= 1) m = propose_window<MAXRM>(c, c.G, lt, j, n, m, logbase, sl, par);
+  if constexpr (std::is_same_v<T, TW>) {
+    for (int m = 0; m < n; par ^= 1) m = propose_window<MAXRM>(c, c.G, lt, j, n, m, logbase, sl, par);
+  } else {
+    __shared__ Delay<TW> db;
+    int kd = 0;
+    for (int m = 0; m < n; par ^= 1) m = propose_window_delayed<MAXRM>(c, c.G, lt, j, n, m, logbase, sl, par, db, kd);
+    if (kd) delayed_flush(c.G, P.Ns, db, kd);
+  }
   if (threadIdx.x == 0) c.ctl->log_pos += n;
   finish_tape(c, n);
   __syncthreads();
