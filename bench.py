@@ -184,22 +184,33 @@ def clocks_stop(proc, f, path, device):
             "samples": len(sm)}
 
 
-def fp64_peak_tflops(torch, dev):
-    """Measured FP64 ceiling: cuBLAS DGEMM 4096^3, best of 5 (CUDA events)."""
-    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
-    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
-    for _ in range(2):
-        torch.matmul(a, b)
-    best = 0.0
-    for _ in range(5):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        torch.matmul(a, b)
-        e1.record()
-        e1.synchronize()
-        best = max(best, 2 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
-    del a, b
+def gemm_peak_tflops(torch, dev, dtype, tf32=False):
+    """Measured pipe ceiling: a cuBLAS GEMM 4096^3 of `dtype`, best of 5
+    (CUDA events); FP32 with TF32 disabled is the CUDA-core FP32 pipe, with
+    TF32 enabled the TF32 tensor pipe."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = tf32
+    try:
+        a = torch.randn(4096, 4096, dtype=dtype, device=dev)
+        b = torch.randn(4096, 4096, dtype=dtype, device=dev)
+        for _ in range(2):
+            torch.matmul(a, b)
+        best = 0.0
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = max(best, 2 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+        del a, b
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
     return best
+
+
+def fp64_peak_tflops(torch, dev):
+    return gemm_peak_tflops(torch, dev, torch.float64)
 
 
 def traffic_per_launch():
@@ -477,7 +488,7 @@ def timed_arm(torch, dist, dev, model, prec, fields, seed, warmup, steps, autotu
 def run_gpu(args):
     import torch
     from kapdqmc_gb300 import Initial_s
-    from kapdqmc_gb300.flops import sweep_flops
+    from kapdqmc_gb300.flops import mixed_roofline, sweep_flops
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -510,26 +521,41 @@ def run_gpu(args):
     block_launches = args.steps * 2 * (len(model.nodes) - 1)
     per_launch = NCHAINS / (2 * (len(model.nodes) - 1))
     avg_launch_s = ms * 1e-3 / block_launches
-    peak = fp64_peak_tflops(torch, dev)
     kc = bool(np.any(np.imag(np.asarray(model.eK)) != 0))
     fl = sweep_flops(model, acc_per_chain_sweep, record=RECORD, k_complex=kc)
+    traffic = {"traffic": traffic_per_launch(),
+               "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum per k_block launch, per chain, "
+                                 f"times the chains of a launch (profiles/k_block_{WL['tag']}_{prec}_traffic.json)"}
     if prec == "fp64":
+        peak = fp64_peak_tflops(torch, dev)
         flops_per_launch = fl["total"] * per_launch
-        pipe = "FP64 DFMA (CUDA cores)"
-    else:   # the FP64 part (QR, LU, G recompute) is what the mixed sweep is bound by
-        flops_per_launch = fl["stabilise_qr_lu"] * per_launch
-        pipe = "FP64 DFMA for QR, LU and the G recompute (the FP32 bulk products are reported apart)"
-    achieved = flops_per_launch / avg_launch_s / 1e12
-    roof = {"bound": "fp64", "pipe": pipe, "achieved": achieved, "peak": peak,
-            "unit": "TFLOP/s", "frac": achieved / peak,
-            "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
-            "traffic": traffic_per_launch(),
-            "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum per k_block launch "
-                              f"(profiles/k_block_{WL['tag']}_{prec}_traffic.json)",
-            "flops_per_launch": flops_per_launch,
-            "flops_per_chain_sweep": fl}
-    if prec == "mixed":
-        roof["fp32_achieved_tflops"] = (fl["total"] - fl["stabilise_qr_lu"]) * per_launch / avg_launch_s / 1e12
+        achieved = flops_per_launch / avg_launch_s / 1e12
+        roof = {"bound": "fp64", "pipe": "FP64 DFMA (CUDA cores)", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
+                **traffic, "flops_per_launch": flops_per_launch, "flops_per_chain_sweep": fl}
+    else:
+        # time roofline over the pipes the mixed sweep's stages run on
+        p_tf32 = gemm_peak_tflops(torch, dev, torch.float32, tf32=True)
+        p_fp32 = gemm_peak_tflops(torch, dev, torch.float32, tf32=False)
+        work = mixed_roofline(fl)                                  # pipe flops per chain-sweep
+        t_pipe = {"tensor": work["tensor"] * per_launch / (p_tf32 * 1e12),
+                  "fp32": work["fp32"] * per_launch / (p_fp32 * 1e12)}
+        t_roof = sum(t_pipe.values())
+        flops_per_launch = fl["total"] * per_launch                # algorithmic flops
+        achieved = flops_per_launch / avg_launch_s / 1e12
+        peak = flops_per_launch / t_roof / 1e12
+        roof = {"bound": max(t_pipe, key=t_pipe.get), "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak,
+                "what": "algorithmic flops of a launch over its measured time (achieved) and over its roofline "
+                        "time (peak): sum over pipes of the pipe work at the pipe's measured rate, with the "
+                        "3xTF32 kinetic products as 3 TF32 products each and the double-float stabilisation "
+                        "at 15 FP32 operations per real multiply-add",
+                "pipe_roofline_s_per_launch": t_pipe, "launch_s": avg_launch_s,
+                "peaks_tflops": {"tf32_tensor": p_tf32, "fp32_cuda_core": p_fp32},
+                "peak_source": "cuBLAS TF32 and FP32 (TF32 off) GEMM 4096^3 measured in this run",
+                **traffic, "flops_per_launch": flops_per_launch, "flops_per_chain_sweep": fl,
+                "pipe_work_per_chain_sweep": work}
 
     if args.phases:
         sw.enable_phase_timing(True)

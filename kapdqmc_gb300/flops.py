@@ -48,17 +48,39 @@ def sweep_flops(model, accepted: float, record, k_complex: bool = False) -> dict
     hh = 2 * (2 * N * ns * ns - 2 * ns ** 3 // 3) * (mgg // 2)   # geqrf + orgqr (mgg/2 per op pair)
     getg = (ns * ns * N + ns ** 3 // 3 + ns * ns * N + N * N * ns) * mgg
     out["stabilise"] = thin + n_cross * (hh + getg)
-    out["stabilise_qr_lu"] = n_cross * (hh + getg)     # FP64 in both precisions
+    out["stabilise_qr_lu"] = n_cross * (hh + getg)     # FP64 (plain) or double-float (mixed)
     if record == 2:
         # fast form: two products per measurement plus the factor pushes/pops
         # (each a slice matrix applied to L and to R)
-        out["measure"] = (fast_factor_ops(model) * (wrap + rot) + measured_slices(model) * 2 * N ** 3 * mgg)
+        out["measure_kinetic"] = fast_factor_ops(model) * (wrap + rot)
+        out["measure"] = out["measure_kinetic"] + measured_slices(model) * 2 * N ** 3 * mgg
     elif record:
-        out["measure"] = measure_wraps(model) * (wrap + rot) + measured_slices(model) * 2 * N ** 3 * mgk
+        out["measure_kinetic"] = measure_wraps(model) * (wrap + rot) + measured_slices(model) * 2 * N ** 3 * mgk
+        out["measure"] = out["measure_kinetic"]
     else:
-        out["measure"] = 0
-    out["total"] = sum(v for k, v in out.items() if k != "stabilise_qr_lu")
+        out["measure"] = out["measure_kinetic"] = 0
+    out["total"] = sum(v for k, v in out.items() if k not in ("stabilise_qr_lu", "measure_kinetic"))
     return out
+
+
+# FP32-pipe instructions per algorithmic flop of the double-float
+# arithmetic of the mixed sweep's stabilisation: a real multiply-add (2
+# flops) takes 15 FP32 operations (kdq_device.cuh, madd(df&, df, df)).
+DF_OPS_PER_FLOP = 7.5
+# TF32 tensor products per FP32 product of the 3xTF32 split
+TF32_PRODUCTS = 3
+
+
+def mixed_roofline(fl: dict) -> dict:
+    """Work of one mixed-precision chain-sweep per pipe, in the units the
+    pipe's peak is measured in: 'tensor' = TF32 tensor flops of the 3xTF32
+    kinetic products (wraps, thin block products, measurement factors),
+    'fp32' = FP32-pipe flops of the double-float stabilisation (QR, inverse,
+    recompute; 2 * DF_OPS_PER_FLOP per algorithmic flop counted as FMA
+    pairs) plus the FP32 local updates and measurement products."""
+    tensor = TF32_PRODUCTS * (fl["wrap"] + (fl["stabilise"] - fl["stabilise_qr_lu"]) + fl["measure_kinetic"])
+    fp32 = 2 * DF_OPS_PER_FLOP * fl["stabilise_qr_lu"] + fl["update"] + (fl["measure"] - fl["measure_kinetic"])
+    return {"tensor": tensor, "fp32": fp32}
 
 
 def _window(model):
