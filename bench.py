@@ -783,6 +783,61 @@ def run_slmc(args):
     print(json.dumps(out))
 
 
+def run_slmc_scan(args):
+    """Local updates against learned cluster moves on a small t-U lattice
+    over a range of couplings: per U, the local sweep's acceptance and
+    tau_int of the energy and of the AF spin structure factor, an effective
+    model trained on the chains' configurations (held-out residual), and
+    the same chains with one cluster move per slice of the largest and of
+    half that cluster length.  One JSON line per U."""
+    from kapdqmc_gb300 import Initial_s, slmc, tU_Hubbard_Para
+    site = [int(v) for v in args.scan_site.split(",")]
+    nch = args.chains or 256
+
+    def arm(model, fields, seed, burn, sweeps, slmc_args=None):
+        sw = new_sweeper(model, "mixed", fields, seed)
+        if slmc_args is not None:
+            sw.slmc_enable(*slmc_args)
+        sw.init()
+        sw.sweep(burn, record=0)
+        sw.synchronize()
+        t0 = time.perf_counter()
+        sw.sweep(sweeps, record=RECORD)
+        sw.synchronize()
+        wall = time.perf_counter() - t0
+        obs = sw.get_obs(sweeps)
+        st, stats, s = (sw.slmc_stats() if slmc_args is not None else None), sw.stats(), sw.get_fields()
+        sw.close()
+        return {"chain_sweeps_per_s": len(fields) * sweeps / wall, "acceptance": stats["accepted"] / max(1, stats["proposals"]),
+                "tau_int_energy": tau_int(obs[:, :, 0]), "tau_int_af_sf": tau_int(obs[:, :, 8]),
+                "tau_int_binning_energy": binned_tau(obs[:, :, 0]), "tau_int_binning_af_sf": binned_tau(obs[:, :, 8]),
+                "obs": obs_summary(model, obs), "cluster_moves": st}, s
+
+    for U in (float(u) for u in args.scan_u.split(",")):
+        model = tU_Hubbard_Para(Ht=1.0, Hu1=U, Hu2=U, Δt=0.1, Θrelax=5.0, Θquench=0.0, Lattice="SQUARE45",
+                                site=site, BatchSize=10, Initial="H0")
+        fields = np.stack([Initial_s(model, 100 + c) for c in range(nch)])
+        local, s_eq = arm(model, fields, 1, 100, args.steps)
+        sw = new_sweeper(model, "mixed", s_eq, 5)
+        sw.init()
+        X, Y = [], []
+        for _ in range(40):
+            sw.sweep(1, record=0)
+            X.append(slmc.cnn_fields(sw.get_fields()))
+            Y.append(sw.log_det()[0])
+        sw.close()
+        X, Y = np.concatenate(X), np.concatenate(Y)
+        ntr = int(0.9 * len(X))
+        params, loss, _ = slmc.fit_effective_model(X[:ntr], Y[:ntr], epochs=10, batch=64, lr=2e-3, seed=1)
+        held = float(np.std(slmc.cnn_forward(X[ntr:], params) - 2 * Y[ntr:]) / np.std(2 * Y[ntr:]))
+        out = {"U": U, "Ns": model.Ns, "Nt": model.Nt, "chains": nch, "sweeps": args.steps, "local": local,
+               "heldout_residual_over_sd": held, "loss_first_last": [float(loss[0]), float(loss[-1])]}
+        lmax = min(32, model.Ns // 2, model.Ns - 8)
+        for L, steps in ((lmax, 64), (max(1, lmax // 2), 32)):
+            out[f"cluster_L{L}_steps{steps}"], _ = arm(model, s_eq, 2, 20, args.steps, (params, 1, L, steps))
+        print(json.dumps(out), flush=True)
+
+
 # Members of the group line: (workload, chains, precision); every configuration
 # with a quarter of its batch, so that no member fills the GPU alone.
 GROUP = [("c1", 64, "fp64"), ("c2", 64, "fp64"), ("c4", 64, "mixed"), ("c5", 64, "mixed")]
@@ -970,6 +1025,10 @@ def main():
                     help="self-learning cluster moves against local updates (t-U workloads; prints its own line)")
     ap.add_argument("--scee", action="store_true",
                     help="coupled SCEE sweep of replica pairs (t-U workloads; prints its own line)")
+    ap.add_argument("--slmc-scan", action="store_true",
+                    help="local updates vs learned cluster moves on a small t-U lattice over --scan-u")
+    ap.add_argument("--scan-site", default="2,4", help="SQUARE45 site of --slmc-scan (2,4: the 4x4 torus)")
+    ap.add_argument("--scan-u", default="4,8,12,16", help="couplings U/t of --slmc-scan")
     ap.add_argument("--slmc-burn", type=int, default=10)
     ap.add_argument("--slmc-train-sweeps", type=int, default=80,
                     help="sweeps of configurations collected for training (x chains configurations)")
@@ -994,6 +1053,8 @@ def main():
         run_scee(args)
     elif args.slmc:
         run_slmc(args)
+    elif args.slmc_scan:
+        run_slmc_scan(args)
     elif args.tau_run:
         run_tau(args)
     elif args.impl == "reference":
