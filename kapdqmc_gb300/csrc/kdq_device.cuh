@@ -112,6 +112,19 @@ __device__ __forceinline__ void madd(df& acc, df a, df b) {
   const df s = df_two_sum(acc.hi, p);
   acc = df_fast2(s.hi, __fadd_rn(s.lo, __fadd_rn(e, acc.lo)));
 }
+// acc += a * b without the final renormalisation (12 FP32 operations):
+// acc.hi is the rounded running sum, acc.lo collects the rounding errors;
+// normalise(acc) before acc is used as an operand.
+__device__ __forceinline__ void madd_lazy(df& acc, df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const df s = df_two_sum(acc.hi, p);
+  acc.hi = s.hi;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(s.lo, e));
+}
+__device__ __forceinline__ df normalise(df a) { return df_two_sum(a.hi, a.lo); }
 __device__ __forceinline__ df conjg(df a) { return a; }
 __device__ __forceinline__ double re(df a) { return df_to(a); }
 __device__ __forceinline__ double abs2(df a) { const double v = df_to(a); return v * v; }
@@ -143,12 +156,15 @@ __device__ __forceinline__ double abs2(cdf a) {
   const double u = df_to(a.x), v = df_to(a.y);
   return u * u + v * v;
 }
+// complex multiply-add, lazily accumulated (see madd_lazy): normalise the
+// accumulator before it is used as an operand
 __device__ __forceinline__ void madd(cdf& acc, cdf a, cdf b) {
-  madd(acc.x, a.x, b.x);
-  madd(acc.x, -a.y, b.y);
-  madd(acc.y, a.x, b.y);
-  madd(acc.y, a.y, b.x);
+  madd_lazy(acc.x, a.x, b.x);
+  madd_lazy(acc.x, -a.y, b.y);
+  madd_lazy(acc.y, a.x, b.y);
+  madd_lazy(acc.y, a.y, b.x);
 }
+__device__ __forceinline__ cdf normalise(cdf a) { return {normalise(a.x), normalise(a.y)}; }
 __device__ __forceinline__ void madd(cdf& acc, cdf a, df b) {
   madd(acc.x, a.x, b);
   madd(acc.y, a.y, b);
@@ -298,6 +314,12 @@ __device__ inline double block_sum(double v, double* red) {
   return t;
 }
 
+// accumulators of the FP64, FP32 and complex types need no normalisation
+__device__ __forceinline__ double normalise(double a) { return a; }
+__device__ __forceinline__ float normalise(float a) { return a; }
+__device__ __forceinline__ cd normalise(cd a) { return a; }
+__device__ __forceinline__ cf normalise(cf a) { return a; }
+
 // ------------------------------------------------------------------- GEMM
 // C[M x N] = A[M x K] * B[K x N] (column-major, C must not alias A or B),
 // with an optional epilogue C[i,j] = rs[i] * acc * cs[j]; with SUB the
@@ -346,7 +368,7 @@ __device__ void bgemm_t(int M, int N, int K, const TA* __restrict__ A, int lda,
       for (int n = 0; n < TN; ++n) {
         const int j = c0 + CS * n;
         if (j >= N) continue;
-        TC v = acc[m][n];
+        TC v = normalise(acc[m][n]);
         if (rs) v = rs[i] * v;
         if (cs) v = v * cs[j];
         if constexpr (SUB) v = C[i + (size_t)j * ldc] - v;   // C -= A B
@@ -358,6 +380,41 @@ __device__ void bgemm_t(int M, int N, int K, const TA* __restrict__ A, int lda,
 }
 
 // ------------------------------------------------ Householder QR (thin Q)
+// Columns c0 <= c < n of A (ld N): A[j:,c] -= s w (w^H A[j:,c]) with the
+// reflector w = x[j:] and s = 2 / (w^H w).  Warp `warp` of nw takes columns
+// c0 + warp, c0 + warp + nw, ... three at a time: the three dot products and
+// their warp reductions are independent chains, so they overlap; each
+// column's own arithmetic is the same as one column at a time.
+template <class T>
+__device__ __forceinline__ void reflect_columns(int N, int c0, int n, int j, const T* x, double s, T* A, int warp,
+                                                int nw, int lane) {
+  for (int c = c0 + warp; c < n; c += 3 * nw) {
+    const int cb = c + nw, cc = c + 2 * nw;
+    T* ya = A + (size_t)c * N;
+    T* yb = A + (size_t)min(cb, n - 1) * N;
+    T* yc = A + (size_t)min(cc, n - 1) * N;
+    T ta = zero<T>(), tb = zero<T>(), tc = zero<T>();
+    for (int i = j + lane; i < N; i += 32) {
+      const T xi = conjg(x[i]);
+      madd(ta, xi, ya[i]);
+      if (cb < n) madd(tb, xi, yb[i]);
+      if (cc < n) madd(tc, xi, yc[i]);
+    }
+    ta = warp_sum(normalise(ta));
+    tb = warp_sum(normalise(tb));
+    tc = warp_sum(normalise(tc));
+    ta = ta * s;
+    tb = tb * s;
+    tc = tc * s;
+    for (int i = j + lane; i < N; i += 32) {
+      const T xi = x[i];
+      ya[i] = ya[i] - xi * ta;
+      if (cb < n) yb[i] = yb[i] - xi * tb;
+      if (cc < n) yc[i] = yc[i] - xi * tc;
+    }
+  }
+}
+
 // Overwrites Q (N x n, column-major, ld N) with an orthonormal basis of the
 // column space of Y (N x n, ld N), destroying Y.  Reflectors
 // H = I - w w^H * (2 / w^H w) with w = x + e^{i arg x0} |x| e1 (Householder
@@ -392,14 +449,7 @@ __device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red,
     }
     __syncthreads();
     // trailing columns c > j: A[:,c] -= (2/ww) w (w^H A[:,c])
-    for (int c = j + 1 + warp; c < n; c += nw) {
-      T* y = Y + (size_t)c * N;
-      T t = zero<T>();
-      for (int i = j + lane; i < N; i += 32) madd(t, conjg(x[i]), y[i]);
-      t = warp_sum(t);
-      t = t * wn[j];
-      for (int i = j + lane; i < N; i += 32) y[i] = y[i] - x[i] * t;
-    }
+    reflect_columns(N, j + 1, n, j, x, wn[j], Y, warp, nw, lane);
     __syncthreads();
   }
   // Q = H_0 H_1 ... H_{n-1} [I; 0]
@@ -410,20 +460,72 @@ __device__ void householder_q(int N, int n, T* Y, T* Q, double* wn, double* red,
   __syncthreads();
   for (int j = n - 1; j >= 0; --j) {
     const T* x = Y + (size_t)j * N;
-    for (int c = j + warp; c < n; c += nw) {
-      T* q = Q + (size_t)c * N;
-      T t = zero<T>();
-      for (int i = j + lane; i < N; i += 32) madd(t, conjg(x[i]), q[i]);
-      t = warp_sum(t);
-      t = t * wn[j];
-      for (int i = j + lane; i < N; i += 32) q[i] = q[i] - x[i] * t;
-    }
+    reflect_columns(N, j, n, j, x, wn[j], Q, warp, nw, lane);
     __syncthreads();
   }
   if (tid == 0) {
     if (log_out) *log_out = lgs;
     if (phase_out) *phase_out = phs;
   }
+}
+
+// ------------------------------------------------------- Cholesky QR (thin Q)
+// W = R^H R for the n x n Hermitian positive definite W (ld n), in place: R
+// in the upper triangle (real positive diagonal), the strictly lower part
+// left as it was.  Sets *bad when a pivot falls to <= tol times the largest
+// diagonal entry (W too ill-conditioned for the caller's purpose).  When
+// given, log_out receives sum_k log R_kk.  rinv (n entries, shared memory)
+// receives 1 / R_kk.
+template <class T>
+__device__ void chol_upper(int n, T* W, double tol, double* rinv, int* bad, double* log_out = nullptr) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ double dmax;
+  if (tid == 0) {
+    double m = 0.0;
+    for (int k = 0; k < n; ++k) m = fmax(m, re(W[k + (size_t)k * n]));
+    dmax = m;
+  }
+  __syncthreads();
+  double lgs = 0.0;   // thread 0
+  for (int k = 0; k < n; ++k) {
+    if (tid == 0) {
+      double d = re(W[k + (size_t)k * n]);
+      if (!(d > tol * dmax)) {
+        *bad = 1;
+        d = dmax > 0.0 ? dmax : 1.0;   // keep the arithmetic finite; the caller discards the result
+      }
+      const double r = sqrt(d);
+      W[k + (size_t)k * n] = from_real<T>(r);
+      rinv[k] = 1.0 / r;
+      lgs += log(r);
+    }
+    __syncthreads();
+    const double s = rinv[k];
+    for (int c = k + 1 + tid; c < n; c += nt) W[k + (size_t)c * n] = W[k + (size_t)c * n] * s;   // row k of R
+    __syncthreads();
+    const int m = n - k - 1;
+    for (int e = tid; e < m * m; e += nt) {   // W[i,j] -= conj(R[k,i]) R[k,j], i, j > k
+      const int i = k + 1 + e % m, j = k + 1 + e / m;
+      W[i + (size_t)j * n] = W[i + (size_t)j * n] - conjg(W[k + (size_t)i * n]) * W[k + (size_t)j * n];
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && log_out) *log_out = lgs;
+}
+
+// Q (N x n, ld N) = A R^-1 with R upper triangular (ld n, from chol_upper) and
+// rinv = 1 / diag(R): one thread per row, forward substitution along the
+// columns.  Q must not alias A.
+template <class T>
+__device__ void trsm_right_upper(int N, int n, const T* A, const T* R, const double* rinv, T* Q) {
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    for (int c = 0; c < n; ++c) {
+      T acc = A[i + (size_t)c * N];
+      for (int k = 0; k < c; ++k) madd(acc, -Q[i + (size_t)k * N], R[k + (size_t)c * n]);
+      Q[i + (size_t)c * N] = normalise(acc) * rinv[c];
+    }
+  }
+  __syncthreads();
 }
 
 // --------------------------------------------------------- LU and solves

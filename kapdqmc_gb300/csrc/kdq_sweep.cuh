@@ -1058,6 +1058,43 @@ __device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const typename Ctx<KIND, T, K
   __syncthreads();
 }
 
+// Thin Q of the N x ns block product A (destroyed) into Q, and the log|det|
+// and phase of the dropped triangle.  Plain sweep: Householder (the
+// reference's ?geqrf + ?orgqr).  Mixed sweep: one-pass Cholesky QR in
+// double-float arithmetic, W = A^H A = R^H R, Q = A R^-1 (GEMM-shaped, about a
+// third of the Householder's operations): the mixed sweep's slice matrices
+// D eK have unitary D, so cond(A) <= cond(eK)^n_wrap and the loss of
+// orthogonality, ~cond(A)^2 2^-48, stays far below the FP32 G it feeds (2e-12
+// at t-U 12x12, n_wrap 8); when a pivot reveals cond(A)^2 > 1e8 the
+// Householder form runs instead.  The span, and so G, is the same either way
+// (Q differs by a unitary column rotation).  scratch: N x ns (TS).
+template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
+__device__ void thin_q(Ctx<KIND, T, KT, TW, KW>& c, typename Ctx<KIND, T, KT, TW, KW>::TS* A,
+                       typename Ctx<KIND, T, KT, TW, KW>::TS* Q, typename Ctx<KIND, T, KT, TW, KW>::TS* scratch,
+                       double* qlg, cd* qph) {
+  using TS = typename Ctx<KIND, T, KT, TW, KW>::TS;
+  const int N = c.P.Ns, ns = N / 2;
+  if constexpr (!std::is_same_v<T, TW>) {
+    __shared__ int bad;
+    __shared__ double rinv[KDQ_MAX_NS / 2];
+    if (threadIdx.x == 0) bad = 0;
+    for (size_t e = threadIdx.x; e < (size_t)N * ns; e += blockDim.x) {   // A^H (ns x N)
+      const int i = e % N, col = e / N;
+      scratch[col + (size_t)i * ns] = conjg(A[e]);
+    }
+    __syncthreads();
+    gemm_thin<MAXRM, TS>(ns, ns, N, scratch, ns, A, N, c.Mss, ns);
+    chol_upper(ns, c.Mss, 1e-8, rinv, &bad, qlg);
+    if (!bad) {
+      trsm_right_upper(N, ns, A, c.Mss, rinv, Q);
+      if (threadIdx.x == 0) *qph = mkc(1.0, 0.0);
+      __syncthreads();
+      return;
+    }
+  }
+  householder_q(N, ns, A, Q, c.sm.wn, c.sm.red, qlg, qph);
+}
+
 // BRs[k+1] = orth_cols(BM(k) BRs[k]) then G recompute at node k+1.
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
@@ -1087,7 +1124,7 @@ __device__ void node_forward(Ctx<KIND, T, KT, TW, KW>& c, int k) {
   c.clk.lap(3);
   __shared__ double qlg;   // written and read by thread 0 only
   __shared__ cd qph;
-  householder_q(N, ns, src, BRn, c.sm.wn, c.sm.red, &qlg, &qph);
+  thin_q<MAXRM>(c, src, BRn, c.Y2, &qlg, &qph);
   if (threadIdx.x == 0) {   // B(tau_{k+1}, 0) P = BRs[k+1] R_{k+1} ... R_1
     const double* a = lw_at(P, c.chain, 1, k);
     double* b = lw_at(P, c.chain, 1, k + 1);
@@ -1139,7 +1176,7 @@ __device__ void node_backward(Ctx<KIND, T, KT, TW, KW>& c, int k, bool recompute
   c.clk.lap(3);
   __shared__ double qlg;   // written and read by thread 0 only
   __shared__ cd qph;
-  householder_q(N, ns, A, Q, c.sm.wn, c.sm.red, &qlg, &qph);
+  thin_q<MAXRM>(c, A, Q, c.X, &qlg, &qph);
   for (size_t e = threadIdx.x; e < fs; e += blockDim.x) {
     const int r = e % ns, col = e / ns;
     BLk[e] = conjg(Q[col + (size_t)r * N]);

@@ -65,8 +65,9 @@ def sweep_flops(model, accepted: float, record, k_complex: bool = False) -> dict
 
 # FP32-pipe instructions per algorithmic flop of the double-float
 # arithmetic of the mixed sweep's stabilisation: a real multiply-add (2
-# flops) takes 15 FP32 operations (kdq_device.cuh, madd(df&, df, df)).
-DF_OPS_PER_FLOP = 7.5
+# flops) of its GEMMs and reflector dot products takes 12 FP32 operations
+# (kdq_device.cuh, madd_lazy; 15 with a renormalisation per step).
+DF_OPS_PER_FLOP = 6.0
 # TF32 tensor products per FP32 product of the 3xTF32 split
 TF32_PRODUCTS = 3
 
@@ -76,8 +77,8 @@ def mixed_roofline(fl: dict) -> dict:
     pipe's peak is measured in: 'tensor' = TF32 tensor flops of the 3xTF32
     kinetic products (wraps, thin block products, measurement factors),
     'fp32' = FP32-pipe flops of the double-float stabilisation (QR, inverse,
-    recompute; 2 * DF_OPS_PER_FLOP per algorithmic flop counted as FMA
-    pairs) plus the FP32 local updates and measurement products."""
+    recompute; 2 * DF_OPS_PER_FLOP per algorithmic flop, the peak counting
+    an FMA as 2) plus the FP32 local updates and measurement products."""
     tensor = TF32_PRODUCTS * (fl["wrap"] + (fl["stabilise"] - fl["stabilise_qr_lu"]) + fl["measure_kinetic"])
     fp32 = 2 * DF_OPS_PER_FLOP * fl["stabilise_qr_lu"] + fl["update"] + (fl["measure"] - fl["measure_kinetic"])
     return {"tensor": tensor, "fp32": fp32}

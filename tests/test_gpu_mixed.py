@@ -93,3 +93,53 @@ def test_mixed_energy_within_error_bars_of_fp64():
         means[prec] = (ek.mean(), ek.std(ddof=1) / np.sqrt(nch))
     (m1, e1), (m2, e2) = means["fp64"], means["mixed"]
     assert abs(m1 - m2) < 3 * np.hypot(e1, e2), means
+
+
+def _cholesky_pivot_ratios(model, s):
+    """min_k R_kk^2 / max_k W_kk of the Cholesky W = R^H R of W = Z Z^H for the
+    init chain's block products Z = BL_{k+1} BM_k (the mixed sweep's Cholesky
+    QR rejects a block when this falls to 1e-8)."""
+    sw = O._TUSweep(model, s, O.Tape(np.zeros(1, np.uint8), np.zeros(1)), False)
+    sw.init_chain()
+    out = []
+    for idx in range(sw.NN - 1, 0, -1):
+        Z = sw.BLs[idx + 1] @ sw.BM(idx)
+        W = Z @ Z.conj().T
+        try:
+            R = np.linalg.cholesky(W)
+        except np.linalg.LinAlgError:      # not positive definite in FP64 either
+            out.append(0.0)
+            continue
+        out.append(float(np.min(np.abs(np.diag(R)) ** 2) / np.max(np.real(np.diag(W)))))
+    return np.array(out)
+
+
+def test_mixed_falls_back_to_householder_for_ill_conditioned_blocks():
+    """dt = 0.5 and n_wrap = 10 on the 4x4 square lattice make the block
+    products so ill-conditioned that the mixed sweep's Cholesky QR rejects
+    them (pivot ratio below 1e-8, checked here on the oracle's blocks) and the
+    Householder form runs.  FP32 wraps are too coarse to follow the FP64
+    oracle's decisions at this dt (each slice's eK has condition number e^4),
+    so the check is on the stabilisation itself: after the sweep, G at
+    tau = 0 is recomputed from the chain's stabilised B-chains, and it must
+    equal the oracle's G built from the same final fields, to the ~3e-3 that
+    FP32 block products through such slices allow (1e-4 at the configured
+    dt, test_mixed_tracks_fp64_oracle)."""
+    from kapdqmc_gb300 import tU_Hubbard_Para
+    model = tU_Hubbard_Para(Ht=1.0, Hu1=4.0, Hu2=4.0, Δt=0.5, Θrelax=5.0, Θquench=0.0,
+                            Lattice="SQUARE45", site=[2, 4], BatchSize=10, Initial="H0")
+    nch = 2
+    fields = np.stack([Initial_s(model, 310 + c) for c in range(nch)])
+    assert np.any(_cholesky_pivot_ratios(model, fields[0]) < 1e-8)
+    with Sweeper(model, nch) as sw:
+        sw.set_precision("mixed")
+        sw.set_fields(fields)
+        sw.set_rng(78)
+        sw.phy_update(1, 0)
+        s_end = sw.get_fields()
+        G = [sw.green(c) for c in range(nch)]
+    for c in range(nch):
+        ref = O._TUSweep(model, s_end[c], O.Tape(np.zeros(1, np.uint8), np.zeros(1)), False)
+        ref.init_chain()
+        err = np.linalg.norm(G[c] - ref.G) / np.linalg.norm(ref.G)
+        assert err < 1e-2, err
