@@ -244,10 +244,12 @@ int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32
 int kdq_set_precision(kdq_handle* h, int32_t mode);
 
 /* Per-stage clock counts of the sweep (SM clock cycles, summed over chains):
- * cycles[0] wraps, [1] local updates (the windows of acceptance ratios and
- * the G updates of accepted proposals), [2] measurements, [3] block products
- * of the stabilisation chain, [4] Householder QR, [5] G recompute, [6]
- * self-learning cluster moves, [7] unused (0); cycles has 8 entries.  Enabling resets the counters and adds a barrier
+ * cycles[0] wraps, [1] local updates (FP64 sweep: the windows of
+ * acceptance ratios and the G updates of accepted proposals; mixed sweep:
+ * the accepted proposals' update vectors and the flushes of the delayed
+ * updates), [2] measurements, [3] block products of the stabilisation chain,
+ * [4] QR, [5] G recompute, [6] self-learning cluster moves, [7] the mixed
+ * sweep's windows of acceptance ratios; cycles has 8 entries.  Enabling resets the counters and adds a barrier
  * per stage.  No counterpart in the reference (which has no tracing). */
 int kdq_enable_phase_timing(kdq_handle* h, int32_t enable);
 int kdq_get_phase_cycles(kdq_handle* h, double* cycles);

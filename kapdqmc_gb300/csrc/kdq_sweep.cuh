@@ -99,10 +99,11 @@ __device__ inline void kmul_right(int M, int N, int K, const TW* X, int ldx, con
 
 // ------------------------------------------------------------ phase timing
 // Optional per-chain clock counts of the sweep's phases (thread 0, between
-// barriers): 0 wraps, 1 local updates (windows of acceptance ratios and the
-// G updates of accepted proposals), 2 measurements, 3 block products of the
-// stabilisation chain, 4 Householder QR, 5 G recompute, 6 cluster moves,
-// 7 unused.
+// barriers): 0 wraps, 1 local updates (the FP64 sweep's windows of
+// acceptance ratios and G updates; the mixed sweep's new update vectors and
+// flushes of the delayed updates), 2 measurements, 3 block products of the
+// stabilisation chain, 4 QR, 5 G recompute, 6 cluster moves, 7 the mixed
+// sweep's windows of acceptance ratios.
 struct PhaseClock {
   unsigned long long* acc;
   long long t;
@@ -868,6 +869,7 @@ __device__ int propose_window_delayed(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt
     }
   }
   __syncthreads();
+  c.clk.lap(7);   // the window's decision (ratios, ballot, publication)
   const int next = sm.nxt[par];
   if (sm.accept[par]) {
     // the accepted proposal's vectors from the current G (= G - U W)

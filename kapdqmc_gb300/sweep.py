@@ -175,7 +175,7 @@ class Sweeper:
         self._ck(self.lib.kdq_set_precision(self.h, code))
         self.precision = mode
 
-    PHASES = ("wrap", "update", "measure", "block_product", "qr", "recompute", "cluster_moves", "ratio")
+    PHASES = ("wrap", "update", "measure", "block_product", "qr", "recompute", "cluster_moves", "ratio_windows")
 
     def enable_phase_timing(self, enable: bool = True):
         self._ck(self.lib.kdq_enable_phase_timing(self.h, int(bool(enable))))
