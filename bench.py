@@ -1017,8 +1017,8 @@ def main():
                     help="long run of this many sweeps; prints the workload's τ_int JSON and exits")
     ap.add_argument("--chains", type=int, default=None,
                     help="chains per GPU (profiling of small cases only; bench lines use the workload's)")
-    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS),
-                    help="configuration (default c3 at 256 chains, the metric's)")
+    ap.add_argument("--workload", default=None, choices=sorted(WORKLOADS),
+                    help="configuration (default: c3 at 256 chains, the metric's; c5 for --scee and --slmc)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="arithmetic of the headline arm (mixed: complex sweeps only; t-V runs fp64)")
     ap.add_argument("--slmc", action="store_true",
@@ -1040,6 +1040,8 @@ def main():
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     global WL, NCHAINS, PRECISION
+    if args.workload is None:
+        args.workload = "c5" if (args.scee or args.slmc) else "c3"
     WL = WORKLOADS[args.workload]
     NCHAINS = args.chains or WL["chains"]
     PRECISION = args.precision if make_model().is_complex else "fp64"
