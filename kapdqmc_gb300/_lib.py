@@ -50,6 +50,7 @@ _SIGS = {
                                 C.c_float, C.c_uint64, C.c_void_p, C.c_void_p, C.c_int32]),
     "kdq_stream": (C.c_void_p, [C.c_void_p]),
     "kdq_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kdq_set_sweep_launch": (C.c_int, [C.c_void_p, C.c_int32]),
     "kdq_set_tiles": (C.c_int, [C.c_void_p, C.c_int32]),
     "kdq_get_tiles": (C.c_int, [C.c_void_p]),
     "kdq_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),

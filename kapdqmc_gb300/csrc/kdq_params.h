@@ -15,7 +15,8 @@
 #define KDQ_FLAG_SINGULAR 2     // zero pivot in the G recompute
 #define KDQ_FLAG_TAPE 4         // explicit tape exhausted
 
-enum { KDQ_MODE_INIT = 0, KDQ_MODE_FWD = 1, KDQ_MODE_BWD = 2 };
+// KDQ_MODE_SWEEP: every block of one sweep (forward then backward) in one launch
+enum { KDQ_MODE_INIT = 0, KDQ_MODE_FWD = 1, KDQ_MODE_BWD = 2, KDQ_MODE_SWEEP = 3 };
 
 struct ChainCtl {
   int idx;              // current stabilisation index (1-based, as the reference)

@@ -109,6 +109,7 @@ struct kdq_handle {
   // one sweep (2 (NN-1) block launches) captured as a CUDA graph, replayed
   // while the launch parameters stay the same
   bool use_graphs = true;
+  bool sweep_launch = false;  // one launch per sweep (else, the default, one per stabilisation block)
   cudaGraphExec_t graph = nullptr;
   SweepParams graph_P{};
   ~kdq_handle() {
@@ -750,8 +751,11 @@ int sweep_prepare(kdq_handle* h, int32_t sweeps, int32_t record) {
   return KDQ_OK;
 }
 
-// The 2 (NN-1) block launches of one sweep on the handle's stream.
+// One sweep on the handle's stream: 2 (NN-1) block launches, or (per-sweep
+// shape) a single launch in which every CTA runs its chain's blocks
+// (chains are independent, so no CTA waits for another between blocks).
 cudaError_t sweep_launches(kdq_handle* h) {
+  if (h->sweep_launch) return launch(h, KDQ_MODE_SWEEP, 0);
   cudaError_t ce = cudaSuccess;
   for (int k = 1; k <= h->NN - 1 && ce == cudaSuccess; ++k) ce = launch(h, KDQ_MODE_FWD, k);
   for (int k = h->NN - 1; k >= 1 && ce == cudaSuccess; --k) ce = launch(h, KDQ_MODE_BWD, k);
@@ -979,6 +983,17 @@ int kdq_get_phase_cycles(kdq_handle* h, double* cycles) {
 int kdq_set_graphs(kdq_handle* h, int32_t enable) {
   if (!h) return KDQ_ERR_ARG;
   h->use_graphs = enable != 0;
+  return KDQ_OK;
+}
+
+int kdq_set_sweep_launch(kdq_handle* h, int32_t per_sweep) {
+  if (!h) return KDQ_ERR_ARG;
+  if (h->sweep_launch != (per_sweep != 0) && h->graph) {   // the captured sweep has the other shape
+    KDQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    KDQ_CUDA(h, cudaGraphExecDestroy(h->graph));
+    h->graph = nullptr;
+  }
+  h->sweep_launch = per_sweep != 0;
   return KDQ_OK;
 }
 

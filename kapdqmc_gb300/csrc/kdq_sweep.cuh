@@ -1552,9 +1552,13 @@ __device__ void measure_fast(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
 }
 
 // ------------------------------------------------------------------ kernel
+template <int KIND, class T, class KT, int MAXRM, bool MIXED, class C>
+__device__ __forceinline__ void sweep_block(C& c, const SweepParams& P, int mode, int k);
+
 // mode KDQ_MODE_INIT: block k of the initial left chain (and G at k == 1);
 // KDQ_MODE_FWD: forward slices node(k)+1 .. node(k+1), then the node;
-// KDQ_MODE_BWD: backward slices node(k+1) .. node(k)+1, then the node.
+// KDQ_MODE_BWD: backward slices node(k+1) .. node(k)+1, then the node;
+// KDQ_MODE_SWEEP: all forward then all backward blocks of one sweep.
 // MIXED selects the FP32 working precision (see the header of this file).
 template <int KIND, class T, class KT, int MAXRM, bool MIXED>
 __global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, int mode, int k) {
@@ -1603,6 +1607,28 @@ __global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, i
     node_backward<MAXRM>(c, k, k == 1, false);
     return;
   }
+  // KDQ_MODE_SWEEP: the whole sweep in one launch (a chain's blocks depend
+  // only on that chain, so each CTA runs through them without waiting for
+  // the others); one call site keeps the block body inlined once
+  const int nb = mode == KDQ_MODE_SWEEP ? 2 * (P.NN - 1) : 1;
+  for (int b = 0; b < nb; ++b) {
+    int m = mode, kk = k;
+    if (mode == KDQ_MODE_SWEEP) {
+      m = b < P.NN - 1 ? KDQ_MODE_FWD : KDQ_MODE_BWD;
+      kk = b < P.NN - 1 ? b + 1 : 2 * (P.NN - 1) - b;
+    }
+    sweep_block<KIND, T, KT, MAXRM, MIXED>(c, P, m, kk);
+  }
+}
+
+// One stabilisation block of the sweep: forward slices node(k)+1 .. node(k+1)
+// then the node, or backward slices node(k+1) .. node(k)+1 then the node.
+template <int KIND, class T, class KT, int MAXRM, bool MIXED, class C>
+__device__ __forceinline__ void sweep_block(C& c, const SweepParams& P, int mode, int k) {
+  const int N = P.Ns;
+  const int chain = c.chain;
+  PhaseClock& clk = c.clk;
+  using TW = std::conditional_t<MIXED, typename low_t<T>::type, T>;
   const int Θidx = P.NN / 2 + 1;
   const int lo = (int)P.nodes[k - 1], hi = (int)P.nodes[k];
   if (mode == KDQ_MODE_FWD) {

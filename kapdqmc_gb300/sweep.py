@@ -189,6 +189,11 @@ class Sweeper:
         """Replay sweeps from a captured CUDA graph (default) or launch block by block."""
         self._ck(self.lib.kdq_set_graphs(self.h, int(bool(enable))))
 
+    def set_sweep_launch(self, per_sweep: bool):
+        """One launch per sweep (each chain's CTA runs all of the sweep's
+        blocks) or, the default, one launch per stabilisation block."""
+        self._ck(self.lib.kdq_set_sweep_launch(self.h, int(bool(per_sweep))))
+
     def set_tiles(self, rows: int):
         """Register-tile class of the sweep kernel (1, 3 or 6 row groups of 32 sites)."""
         self._ck(self.lib.kdq_set_tiles(self.h, int(rows)))
