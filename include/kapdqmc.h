@@ -231,12 +231,16 @@ int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32
                            const int32_t* index, int32_t nA, double* det, void* stream);
 
 /* Arithmetic of the sweep.  KDQ_PREC_FP64 (default): everything in FP64, the
- * reference's arithmetic.  KDQ_PREC_MIXED: the slice wraps, the block
- * products of the stabilisation chain, the measurement products and the
- * rank-k updates of G run in FP32 on the FP32 pipe (G is held in FP32),
- * while the acceptance ratios, the Householder QR, the LU and the recompute
- * of G at every node stay FP64; kdq_get_drift then reports
- * ||G_FP32-wrap - G_FP64-recompute||_F / ||G||_F.  Only the complex sweeps
+ * reference's arithmetic.  KDQ_PREC_MIXED: G is held in FP32; the products
+ * with a real kinetic matrix (slice wraps, block products of the
+ * stabilisation chain, the measurement's kinetic factors) run as 3xTF32
+ * tensor-core tiles with FP32 accumulation (FP32 CUDA-core products when
+ * the hopping is complex), the rank-k updates of G in FP32, delayed and
+ * applied in batches; the acceptance ratios stay FP64, and the thin QR
+ * (Cholesky QR, Householder when a block is ill-conditioned), the inverse
+ * and the recompute of G at every node run in double-float arithmetic (two
+ * FP32 values, 48-bit significand, ~1e-14 relative); kdq_get_drift then
+ * reports ||G_FP32-wrap - G_recompute||_F / ||G||_F.  Only the complex sweeps
  * (t-U, t-UV with U > 0) accept it: their HS factors cis(alpha eta) are
  * unitary, while the real factors exp(+-alpha eta) of t-V and real t-UV
  * amplify FP32 rounding in the wraps (KDQ_ERR_ARG).  No counterpart in the
