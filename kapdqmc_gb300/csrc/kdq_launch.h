@@ -13,7 +13,7 @@ cudaError_t launch_tv(const SweepParams& P, int mode, int k, int maxrm, int ncha
                       cudaStream_t st);
 cudaError_t launch_tuv(const SweepParams& P, int mode, int k, int maxrm, bool g_complex,
                        int nchains, size_t dyn, cudaStream_t st);
-// the same with FP32 working precision (mixed-precision sweep)
+// the same in mixed precision (FP32 working type, double-float stabilisation)
 cudaError_t launch_tu_mixed(const SweepParams& P, int mode, int k, int maxrm, bool k_complex,
                             int nchains, size_t dyn, cudaStream_t st);
 cudaError_t launch_tv_mixed(const SweepParams& P, int mode, int k, int maxrm, int nchains, size_t dyn,

@@ -7,10 +7,12 @@
 // Two precisions.  T / KT are the FP64 types of the sweep (complex128 or
 // float64 for G, float64 or complex128 for the kinetic matrices); TW / KW are
 // the working types of the bulk products (slice wraps, thin B-products,
-// measurement products) and of the rank-k updates.  Plain mode: TW = T.
-// Mixed mode: TW = FP32 (float / complex float) on the CUDA cores' FP32
-// pipe, while the acceptance ratios, the Householder QR, the LU and the G
-// recompute at every node stay FP64 (T).
+// measurement products) and of the rank-k updates; TS (Ctx::TS) is the type
+// of the stabilisation (thin QR, inverse, G recompute).  Plain mode:
+// TW = TS = T.  Mixed mode: TW = FP32 (float / complex float), the products
+// with a real kinetic matrix on the tensor pipe as 3xTF32 (kdq_tc.cuh), the
+// updates delayed; TS = double-float (df / cdf, kdq_device.cuh) on the FP32
+// pipe; the acceptance ratios stay FP64 (T).
 //
 // Reference (KAPDQMC): src/tU/phy_update.jl:3-267, src/tU/GreenMatrix.jl,
 // src/tV/phy_update.jl:1-314, src/tV/GreenMatrix.jl,
@@ -1559,7 +1561,7 @@ __device__ __forceinline__ void sweep_block(C& c, const SweepParams& P, int mode
 // KDQ_MODE_FWD: forward slices node(k)+1 .. node(k+1), then the node;
 // KDQ_MODE_BWD: backward slices node(k+1) .. node(k)+1, then the node;
 // KDQ_MODE_SWEEP: all forward then all backward blocks of one sweep.
-// MIXED selects the FP32 working precision (see the header of this file).
+// MIXED selects the mixed precision (see the header of this file).
 template <int KIND, class T, class KT, int MAXRM, bool MIXED>
 __global__ void __launch_bounds__(KDQ_THREADS, 2) k_block(const SweepParams P, int mode, int k) {
   using TW = std::conditional_t<MIXED, typename low_t<T>::type, T>;

@@ -169,8 +169,9 @@ class Sweeper:
         return obs.reshape(self.nchains, rows, self.n_obs)
 
     def set_precision(self, mode: str):
-        """"fp64" (default, the reference's arithmetic) or "mixed" (FP32 bulk
-        products and updates, FP64 ratios and stabilisation)."""
+        """"fp64" (default, the reference's arithmetic) or "mixed" (FP32 G,
+        3xTF32 tensor-core kinetic products, delayed FP32 updates, FP64
+        acceptance ratios, double-float QR and G recompute)."""
         code = {"fp64": 0, "mixed": 1}[mode]
         self._ck(self.lib.kdq_set_precision(self.h, code))
         self.precision = mode
