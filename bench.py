@@ -264,7 +264,7 @@ def _cpu_worker(args):
     n = O.proposals_per_sweep(model)
     ks, us = zip(*(philox.tape(seed, chain, w, n) for w in range(sweeps)))
     k, u = np.concatenate(ks), np.concatenate(us)
-    run = cport.tu_phy_update if model.kind == 0 else cport.tv_phy_update
+    run = (cport.tu_phy_update, cport.tv_phy_update, cport.tuv_phy_update)[model.kind]
     t0 = time.perf_counter()
     s, _, _ = run(model, _CPU["s"], sweeps, k, u, record=True)
     dt = time.perf_counter() - t0
@@ -276,9 +276,10 @@ CPU_KIND = "port"
 
 
 def cpu_sample_desc():
-    what = ("C restatement of the reference t-U sweep (complex eK and complex GEMMs as the reference)"
-            if make_model().kind == 0 else
-            "C restatement of the reference t-V sweep (dense bond-rotation GEMMs as the reference)")
+    what = ("C restatement of the reference t-U sweep (complex eK and complex GEMMs as the reference)",
+            "C restatement of the reference t-V sweep (dense bond-rotation GEMMs as the reference)",
+            "C restatement of the reference t-UV sweep (complex eK, complex GEMMs and rank-2 bond updates as "
+            "the reference)")[make_model().kind]
     return what + "; OpenBLAS/LAPACK from numpy, 1 thread each; one chain per host core"
 
 
@@ -437,10 +438,13 @@ def run_reference(args):
     finally:
         arm.close()
     cs = cores * len(walls) / sum(walls)
-    tau = args.tau_int or committed_tau("fp64") or 0.5
+    tau = args.tau_int or committed_tau("fp64")
+    tau_src = "given" if args.tau_int else "the plain FP64 sweep's committed long-run value"
+    if tau is None:
+        tau, tau_src = 0.5, "the lower bound 0.5: no committed long run for this workload"
     value = cs / (2 * tau)
     sample = (f"{cpu_sample_desc()}; {cores} chains x 1 sweep per step (model, fields and proposal tapes "
-              f"built outside the timed calls); tau_int={tau:.3g} (the plain FP64 sweep's committed long-run value)")
+              f"built outside the timed calls); tau_int={tau:.3g} ({tau_src})")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": float(np.mean(walls)) * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -653,7 +657,7 @@ def run_gpu(args):
                        "what": "kdq_phy_update per step: fields host->device, chain rebuilt, one sweep, "
                                "fields and rows device->host"}}
         print(json.dumps(out), file=sys.stderr, flush=True)
-        if not args.no_cpu and world == 1 and model.kind in (0, 1) and WL is not WORKLOADS["c1"]:
+        if not args.no_cpu and world == 1 and WL is not WORKLOADS["c1"]:
             cores = os.cpu_count() or 1
             cs_cpu, wall_cpu = cpu_chain_sweeps_per_s(cores, sweeps_per_chain=args.cpu_sweeps)
             tau_cpu = committed_tau("fp64") or tau
@@ -1045,10 +1049,6 @@ def main():
     WL = WORKLOADS[args.workload]
     NCHAINS = args.chains or WL["chains"]
     PRECISION = args.precision if make_model().is_complex else "fp64"
-    if args.impl == "reference" and args.workload == "c4":
-        print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement covers the t-U and t-V sweeps; "
-                                                              "the t-UV 8x8 square workload is not in it"}))
-        return
     if args.group:
         run_group(args)
     elif args.scee:

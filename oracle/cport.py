@@ -1,4 +1,4 @@
-"""ctypes driver of the C restatement of the t-V and t-U sweeps
+"""ctypes driver of the C restatement of the t-V, t-U and t-UV sweeps
 (oracle/cport/kdq_cpu.c).
 
 TEST INFRASTRUCTURE ONLY: the timed CPU baseline and its parity tests.  The
@@ -46,6 +46,7 @@ def load():
             raise RuntimeError("BLAS/LAPACK symbols not found in numpy's OpenBLAS")
         lib.kdq_cpu_tv_phy_update.restype = C.c_int
         lib.kdq_cpu_tu_phy_update.restype = C.c_int
+        lib.kdq_cpu_tuv_phy_update.restype = C.c_int
         _lib = lib
     return _lib
 
@@ -104,3 +105,33 @@ def tu_phy_update(model, s, sweeps, k, u, record=True, log=False):
         raise RuntimeError(f"kdq_cpu_tu_phy_update failed with {rc}")
     s_out = flat_s.reshape(model.field_shape, order="F")
     return s_out, obs.reshape(-1, 6)[:sweeps], acc
+
+
+def tuv_phy_update(model, s, sweeps, k, u, record=True, log=False):
+    """Run the C restatement of the t-UV sweep (complex or, for U < 0, the
+    real branch); returns (s, obs rows (sweeps, 7), accept log or None)."""
+    lib = load()
+    s = np.asfortranarray(np.array(s, dtype=np.uint8))
+    flat_s = np.ascontiguousarray(np.ravel(s, order="F"))
+    z = lambda m: np.ascontiguousarray(np.ravel(np.asarray(m, dtype=np.complex128), order="F")).view(np.float64)
+    mats = [z(model.eK), z(model.eKinv), z(model.HalfeK), z(model.HalfeKinv), z(model.K), z(model.Pt)]
+    nn = np.asarray(model.nnidx)
+    bonds = np.ascontiguousarray(np.stack([nn[:, :, 0].ravel(order="F"), nn[:, :, 1].ravel(order="F")], axis=1),
+                                 dtype=np.int32)
+    nodes = np.ascontiguousarray(model.nodes, dtype=np.int64)
+    gamma, eta = (np.ascontiguousarray(x, dtype=np.float64) for x in (model.γ, model.η))
+    k = np.ascontiguousarray(k, dtype=np.uint8)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    obs = np.zeros(max(sweeps, 1) * 7)
+    acc = np.zeros(len(k), dtype=np.uint8) if log else None
+    hc = int("HoneyComb" in model.Lattice)
+    rc = lib.kdq_cpu_tuv_phy_update(
+        C.c_int(model.Ns), C.c_int(model.Nt), C.c_int(len(nodes)), _p(nodes), _p(gamma), _p(eta),
+        *(_p(m) for m in mats[:5]), C.c_double(model.Ht), C.c_double(model.U), C.c_double(model.V),
+        C.c_double(model.a), C.c_int(0 if model.is_complex else 1), _p(mats[5]), _p(bonds), C.c_int(len(bonds)),
+        C.c_int(model.site[0]), C.c_int(model.site[1]), C.c_int(hc), _p(flat_s), C.c_int(sweeps),
+        C.c_int(int(record)), _p(k), _p(u), C.c_size_t(len(k)), _p(obs), _p(acc) if log else None)
+    if rc != 0:
+        raise RuntimeError(f"kdq_cpu_tuv_phy_update failed with {rc}")
+    s_out = flat_s.reshape(model.field_shape, order="F")
+    return s_out, obs.reshape(-1, 7)[:sweeps], acc

@@ -180,3 +180,22 @@ def test_c_restatement_tu_matches_numpy_oracle(make):
     np.testing.assert_array_equal(acc.astype(bool), np.array(ref.accepts))
     np.testing.assert_array_equal(s2, ref.s)
     np.testing.assert_allclose(obs, np.array(ref.obs_rows)[:, :6], rtol=1e-9, atol=1e-10)
+
+
+@pytest.mark.parametrize("make", [cases.tuv_honeycomb, cases.tuv_square, cases.tuv_hc8_real],
+                         ids=["hc", "sq", "real"])
+def test_c_restatement_tuv_matches_numpy_oracle(make):
+    """The timed t-UV CPU baseline (C, complex GEMMs and rank-2 bond updates as
+    the reference; the U < 0 real branch in complex storage) makes the
+    oracle's decisions."""
+    import cport
+    model = make()
+    s = Initial_s(model, 4)
+    n = O.proposals_per_sweep(model)
+    ks, us = zip(*(philox.tape(6, 0, w, n) for w in range(2)))
+    k, u = np.concatenate(ks), np.concatenate(us)
+    ref = O.phy_update(model, s, 2, O.Tape(k, u), True)
+    s2, obs, acc = cport.tuv_phy_update(model, s, 2, k, u, True, log=True)
+    np.testing.assert_array_equal(acc.astype(bool), np.array(ref.accepts))
+    np.testing.assert_array_equal(s2, ref.s)
+    np.testing.assert_allclose(obs, np.array(ref.obs_rows)[:, :7], rtol=1e-9, atol=1e-10)
