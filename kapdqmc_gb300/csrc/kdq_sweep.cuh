@@ -1034,17 +1034,40 @@ __device__ void get_G(Ctx<KIND, T, KT, TW, KW>& c, const typename Ctx<KIND, T, K
     c.ctl->det_re = ph.x;
     c.ctl->det_im = ph.y;
   }
-  gemm_thin<MAXRM, TS>(ns, N, ns, c.Mss, ns, BL, ns, c.X, ns);
-  gemm_sq<MAXRM, TS>(N, N, ns, BR, N, c.X, ns, c.Gd, N);
   double d2 = 0.0, n2 = 0.0;
-  for (Walk w(N, N); w.ok(); w.next()) {
-    TS g = zero<TS>() - c.Gd[w.e];
-    if (w.i == w.j) g = g + one<TS>();
-    if (drift) {
-      d2 += abs2(cvt<TS>(c.G[w.e]) - g);
-      n2 += abs2(g);
+  if constexpr (std::is_same_v<TS, cdf>) {
+    // Mixed sweep: (BL BR) and its inverse in double-float set the
+    // conditioning; the two products after them feed the FP32 G, so they run
+    // as complex 3xTF32 tensor tiles to FP32 accuracy (X and BR X in FP32,
+    // in the first halves of the X and Gd buffers).
+    cf* Xf = reinterpret_cast<cf*>(c.X);
+    cf* Gf = reinterpret_cast<cf*>(c.Gd);
+    tc_zgemm<4, 4>(ns, N, ns, reinterpret_cast<const float*>(c.Mss), ns, reinterpret_cast<const float*>(BL), ns,
+                   Xf, ns);
+    tc_zgemm<4, 2>(N, N, ns, reinterpret_cast<const float*>(BR), N, reinterpret_cast<const float*>(Xf), ns, Gf, N);
+    for (Walk w(N, N); w.ok(); w.next()) {
+      const cf p = Gf[w.e];
+      const cf g = cf{(w.i == w.j ? 1.0f : 0.0f) - p.x, -p.y};
+      if (drift) {
+        const cf o = c.G[w.e];
+        const double dx = (double)o.x - (double)g.x, dy = (double)o.y - (double)g.y;
+        d2 += dx * dx + dy * dy;
+        n2 += (double)g.x * g.x + (double)g.y * g.y;
+      }
+      c.G[w.e] = g;
     }
-    c.G[w.e] = cvt<TW>(g);
+  } else {
+    gemm_thin<MAXRM, TS>(ns, N, ns, c.Mss, ns, BL, ns, c.X, ns);
+    gemm_sq<MAXRM, TS>(N, N, ns, BR, N, c.X, ns, c.Gd, N);
+    for (Walk w(N, N); w.ok(); w.next()) {
+      TS g = zero<TS>() - c.Gd[w.e];
+      if (w.i == w.j) g = g + one<TS>();
+      if (drift) {
+        d2 += abs2(cvt<TS>(c.G[w.e]) - g);
+        n2 += abs2(g);
+      }
+      c.G[w.e] = cvt<TW>(g);
+    }
   }
   if (drift) {
     d2 = block_sum(d2, c.sm.red);

@@ -191,4 +191,125 @@ __device__ __noinline__ void tc_cgemm(int M, int N, int K, const float* __restri
   __syncthreads();
 }
 
+// One complex entry (re, im) of a cf (S = 2) or cdf (S = 4, hi + lo) array.
+template <int S>
+__device__ __forceinline__ void tc_ldc(const float* __restrict__ p, float& re, float& im) {
+  if constexpr (S == 4) {
+    re = __fadd_rn(p[0], p[1]);
+    im = __fadd_rn(p[2], p[3]);
+  } else {
+    re = p[0];
+    im = p[1];
+  }
+}
+
+// C (M x N complex FP32, ldc) = A B with A (M x K) and B (K x N) complex
+// matrices whose entries are SA (SB) floats apart: 2 for cf, 4 for cdf
+// (re.hi, re.lo, im.hi, im.lo; the FP32 value hi + lo is used).  Real view:
+// C' = A' B' with K' = 2K, real k index 2k + p,
+//   A'(re row m, 2k + p) = p ? -Ai[m,k] : Ar[m,k]
+//   A'(im row m, 2k + p) = p ?  Ar[m,k] : Ai[m,k]
+//   B'(2k + p, n)        = p ?  Bi[k,n] : Br[k,n]
+// so that the re / im rows of C' are Ar Br - Ai Bi and Ai Br + Ar Bi; tile
+// rows 0..7 = re and 8..15 = im of 8 complex rows, as in tc_cgemm<false>.
+// Same 3xTF32 split and warp blocking as tc_cgemm.  BROW: B stored by rows,
+// entry (k, n) at SB (k ldb + n).  SUB: C <- C - A B (the accumulators start
+// from C).  C must not alias A or B.  All threads of the CTA call it; it ends
+// with __syncthreads().
+template <int SA, int SB, bool BROW = false, bool SUB = false>
+__device__ __noinline__ void tc_zgemm(int M, int N, int K, const float* __restrict__ A, int lda,
+                                      const float* __restrict__ B, int ldb, cf* __restrict__ C, int ldc) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int g = lane >> 2, t = lane & 3, p = t & 1;
+  const int MT = (M + 7) / 8, NT = (N + 7) / 8, KT = (K + 3) / 4;
+  const int WMT = (MT + TC_WM - 1) / TC_WM, WNT = (NT + TC_WN - 1) / TC_WN;
+  float* Cf = reinterpret_cast<float*>(C);
+  for (int wt = warp; wt < WMT * WNT; wt += nwarps) {
+    const int mt0 = (wt % WMT) * TC_WM, nt0 = (wt / WMT) * TC_WN;
+    int arow[TC_WM];   // complex row 8 mt + g of each m tile (-1: outside)
+#pragma unroll
+    for (int i = 0; i < TC_WM; ++i) {
+      const int m = (mt0 + i) * 8 + g;
+      arow[i] = (mt0 + i < MT && m < M) ? m : -1;
+    }
+    int bcol[TC_WN];   // complex column 8 nt + g of each n tile (-1: outside)
+#pragma unroll
+    for (int j = 0; j < TC_WN; ++j) {
+      const int n = (nt0 + j) * 8 + g;
+      bcol[j] = (nt0 + j < NT && n < N) ? n : -1;
+    }
+    float acc[TC_WM][TC_WN][4];
+#pragma unroll
+    for (int i = 0; i < TC_WM; ++i)
+#pragma unroll
+      for (int j = 0; j < TC_WN; ++j)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {   // this thread's entries (8 mt + g, 8 nt + 2t + q), as in the epilogue
+          const int n = (nt0 + j) * 8 + 2 * t + q;
+          float re = 0.0f, im = 0.0f;
+          if (SUB && arow[i] >= 0 && nt0 + j < NT && n < N) {
+            const size_t o = 2 * (arow[i] + (size_t)n * ldc);
+            re = Cf[o];
+            im = Cf[o + 1];
+          }
+          acc[i][j][q] = re;
+          acc[i][j][2 + q] = im;
+        }
+    for (int kt = 0; kt < KT; ++kt) {
+      // real k columns t and t + 4 of the tile: complex k0 and k0 + 2, part p
+      const int k0 = kt * 4 + (t >> 1), k1 = k0 + 2;
+      const bool kin0 = k0 < K, kin1 = k1 < K;
+      uint32_t ah[TC_WM][4], al[TC_WM][4];
+#pragma unroll
+      for (int i = 0; i < TC_WM; ++i) {
+        const int m = arow[i];
+        float r0 = 0.0f, i0 = 0.0f, r1 = 0.0f, i1 = 0.0f;
+        if (m >= 0 && kin0) tc_ldc<SA>(A + (size_t)SA * (m + (size_t)k0 * lda), r0, i0);
+        if (m >= 0 && kin1) tc_ldc<SA>(A + (size_t)SA * (m + (size_t)k1 * lda), r1, i1);
+        // fragment order: a0 (re row, k col t), a1 (im row, t), a2 (re row, t + 4), a3 (im row, t + 4)
+        const float v[4] = {p ? -i0 : r0, p ? r0 : i0, p ? -i1 : r1, p ? r1 : i1};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tf32_split(SUB ? -v[q] : v[q], ah[i][q], al[i][q]);
+      }
+      uint32_t bh[TC_WN][2], bl[TC_WN][2];
+#pragma unroll
+      for (int j = 0; j < TC_WN; ++j) {
+        const int n = bcol[j];
+        float r0 = 0.0f, i0 = 0.0f, r1 = 0.0f, i1 = 0.0f;
+        if (n >= 0 && kin0)
+          tc_ldc<SB>(B + (size_t)SB * (BROW ? (size_t)k0 * ldb + n : k0 + (size_t)n * ldb), r0, i0);
+        if (n >= 0 && kin1)
+          tc_ldc<SB>(B + (size_t)SB * (BROW ? (size_t)k1 * ldb + n : k1 + (size_t)n * ldb), r1, i1);
+        tf32_split(p ? i0 : r0, bh[j][0], bl[j][0]);
+        tf32_split(p ? i1 : r1, bh[j][1], bl[j][1]);
+      }
+#pragma unroll
+      for (int i = 0; i < TC_WM; ++i)
+#pragma unroll
+        for (int j = 0; j < TC_WN; ++j) {
+          mma_tf32(acc[i][j], al[i][0], al[i][1], al[i][2], al[i][3], bh[j][0], bh[j][1]);
+          mma_tf32(acc[i][j], ah[i][0], ah[i][1], ah[i][2], ah[i][3], bl[j][0], bl[j][1]);
+          mma_tf32(acc[i][j], ah[i][0], ah[i][1], ah[i][2], ah[i][3], bh[j][0], bh[j][1]);
+        }
+    }
+    // entries (8 mt + g, 8 nt + 2t) and (8 mt + g, 8 nt + 2t + 1): re in c0 / c1, im in c2 / c3
+#pragma unroll
+    for (int i = 0; i < TC_WM; ++i)
+#pragma unroll
+      for (int j = 0; j < TC_WN; ++j) {
+        const int m = arow[i];
+        if (m < 0 || nt0 + j >= NT) continue;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int n = (nt0 + j) * 8 + 2 * t + q;
+          if (n >= N) continue;
+          const size_t o = 2 * (m + (size_t)n * ldc);
+          Cf[o] = acc[i][j][q];
+          Cf[o + 1] = acc[i][j][2 + q];
+        }
+      }
+  }
+  __syncthreads();
+}
+
 }  // namespace kdq
