@@ -553,8 +553,8 @@ def run_gpu(args):
                 "frac": achieved / peak,
                 "what": "algorithmic flops of a launch over its measured time (achieved) and over its roofline "
                         "time (peak): sum over pipes of the pipe work at the pipe's measured rate, with the "
-                        "3xTF32 kinetic products as 3 TF32 products each and the double-float stabilisation "
-                        "at 12 FP32 operations per real multiply-add",
+                        "3xTF32 products (kinetic, recompute X and BR X, delayed flushes) as 3 TF32 products "
+                        "each and the double-float stabilisation at 12 FP32 operations per real multiply-add",
                 "pipe_roofline_s_per_launch": t_pipe, "launch_s": avg_launch_s,
                 "peaks_tflops": {"tf32_tensor": p_tf32, "fp32_cuda_core": p_fp32},
                 "peak_source": "cuBLAS TF32 and FP32 (TF32 off) GEMM 4096^3 measured in this run",

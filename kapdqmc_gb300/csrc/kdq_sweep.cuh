@@ -784,9 +784,16 @@ struct Delay {
   TW W[KDQ_DELAY][KDQ_MAX_NS];
 };
 
-// G -= sum_{q < kd} U[q] W[q]^T; warps own columns, lanes rows.
+// G -= sum_{q < kd} U[q] W[q]^T.  Complex G: one N x N x kd product on the
+// tensor pipe (3xTF32, FP32 accumulators starting from G).  Otherwise warps
+// own columns, lanes rows, in sequential FMAs.
 template <class TW>
 __device__ void delayed_flush(TW* G, int N, const Delay<TW>& db, int kd) {
+  if constexpr (std::is_same_v<TW, cf>) {
+    tc_zgemm<2, 2, true, true>(N, N, kd, reinterpret_cast<const float*>(&db.U[0][0]), KDQ_MAX_NS,
+                               reinterpret_cast<const float*>(&db.W[0][0]), KDQ_MAX_NS, G, N);
+    return;
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int b = warp; b < N; b += nw) {
     TW wb[KDQ_DELAY];

@@ -49,6 +49,12 @@ def sweep_flops(model, accepted: float, record, k_complex: bool = False) -> dict
     getg = (ns * ns * N + ns ** 3 // 3 + ns * ns * N + N * N * ns) * mgg
     out["stabilise"] = thin + n_cross * (hh + getg)
     out["stabilise_qr_lu"] = n_cross * (hh + getg)     # FP64 (plain) or double-float (mixed)
+    # of which the two products after the inverse, X = (BL BR)^-1 BL and BR X
+    # (3xTF32 tensor tiles in the mixed sweep)
+    out["recompute_products"] = n_cross * (ns * ns * N + N * N * ns) * mgg
+    # of the local updates: the rank-k G updates themselves (the mixed sweep's
+    # delayed flushes, 3xTF32 tensor tiles for a complex G)
+    out["update_flush"] = accepted * rank * N * N * mgg
     if record == 2:
         # fast form: two products per measurement plus the factor pushes/pops
         # (each a slice matrix applied to L and to R)
@@ -59,7 +65,8 @@ def sweep_flops(model, accepted: float, record, k_complex: bool = False) -> dict
         out["measure"] = out["measure_kinetic"]
     else:
         out["measure"] = out["measure_kinetic"] = 0
-    out["total"] = sum(v for k, v in out.items() if k not in ("stabilise_qr_lu", "measure_kinetic"))
+    parts = ("stabilise_qr_lu", "measure_kinetic", "recompute_products", "update_flush")
+    out["total"] = sum(v for k, v in out.items() if k not in parts)
     return out
 
 
@@ -72,15 +79,20 @@ DF_OPS_PER_FLOP = 6.0
 TF32_PRODUCTS = 3
 
 
-def mixed_roofline(fl: dict) -> dict:
+def mixed_roofline(fl: dict, tc_flush: bool = True) -> dict:
     """Work of one mixed-precision chain-sweep per pipe, in the units the
     pipe's peak is measured in: 'tensor' = TF32 tensor flops of the 3xTF32
-    kinetic products (wraps, thin block products, measurement factors),
-    'fp32' = FP32-pipe flops of the double-float stabilisation (QR, inverse,
-    recompute; 2 * DF_OPS_PER_FLOP per algorithmic flop, the peak counting
-    an FMA as 2) plus the FP32 local updates and measurement products."""
-    tensor = TF32_PRODUCTS * (fl["wrap"] + (fl["stabilise"] - fl["stabilise_qr_lu"]) + fl["measure_kinetic"])
-    fp32 = 2 * DF_OPS_PER_FLOP * fl["stabilise_qr_lu"] + fl["update"] + (fl["measure"] - fl["measure_kinetic"])
+    products (slice wraps, thin block products, measurement factors, the
+    recompute's X and BR X products and, with tc_flush, the delayed rank-k
+    flushes of G), 'fp32' = FP32-pipe flops of the double-float
+    stabilisation (QR, BL BR and its inverse; 2 * DF_OPS_PER_FLOP per
+    algorithmic flop, the peak counting an FMA as 2) plus the rest of the
+    FP32 local updates and the measurement products."""
+    flush = fl["update_flush"] if tc_flush else 0
+    tensor = TF32_PRODUCTS * (fl["wrap"] + (fl["stabilise"] - fl["stabilise_qr_lu"]) + fl["measure_kinetic"]
+                              + fl["recompute_products"] + flush)
+    fp32 = (2 * DF_OPS_PER_FLOP * (fl["stabilise_qr_lu"] - fl["recompute_products"]) + fl["update"] - flush
+            + (fl["measure"] - fl["measure_kinetic"]))
     return {"tensor": tensor, "fp32": fp32}
 
 
