@@ -63,6 +63,11 @@ struct SweepParams {
   const void* eKinv;
   const void* HalfeK;
   const void* HalfeKinv;
+  // mixed sweep with real kinetic matrices: each of eK, eKinv, HalfeK,
+  // HalfeKinv pre-split into TF32 hi/lo words in mma fragment order, as the
+  // left (A) and the right (B) operand (kdq_tc.cuh, kin_frag_*), or NULL
+  const void* kin_frag;
+  size_t kin_frag_words;        // uint4 words per matrix and side
   const void* K;                // FP64
   const void* Pt;
   // chain state (chain-major); G, W1, W2, Yw, Y2w, Lm, Rm are in the working

@@ -14,6 +14,7 @@
 #include "kdq_cnn.cuh"
 #include "kdq_launch.h"
 #include "kdq_params.h"
+#include "kdq_tc.cuh"
 
 using cplx = std::complex<double>;
 
@@ -83,6 +84,7 @@ struct kdq_handle {
   int precision = KDQ_PREC_FP64;
   size_t esz_w = 16;       // bytes per working-precision G element
   DevBuf Yw, Y2w, Gd, eKw, eKinvw, HalfeKw, HalfeKinvw;
+  DevBuf kinfrag;     // mixed, real kinetic matrices: the pre-split tensor-core operands
   DevBuf Pts, PtHs;   // mixed: Pt and Pt^H in the double-float stabilisation type
   DevBuf phase;            // per-chain phase clocks when enabled
   DevBuf gmid;             // per-chain G at tau = Nt/2 when enabled
@@ -161,6 +163,8 @@ cudaError_t upload_mat(DevBuf& b, const double* src, size_t n, bool cplx_in, boo
 // Launch one stabilisation block for all chains.
 cudaError_t launch(kdq_handle* h, int mode, int k) {
   if (h->precision == KDQ_PREC_MIXED) {
+    // the tensor-core kinetic products read the pre-split operands
+    if (!h->kc && !h->P.kin_frag) return cudaErrorInvalidValue;
     switch (h->kind) {
       case KDQ_TU:
         return kdq::launch_tu_mixed(h->P, mode, k, h->maxrm, h->kc, h->nchains, h->dyn, h->stream);
@@ -209,6 +213,15 @@ __global__ void k_to_dfl(const double* src, float* dst, size_t n) {
     dst[2 * i] = hi;
     dst[2 * i + 1] = __double2float_rn(v - (double)hi);
   }
+}
+
+// The TF32 hi/lo fragment layouts of one real N x N kinetic matrix as the
+// left and the right tensor-core operand (kin_frag_word, kdq_tc.cuh).
+__global__ void k_kin_frag(const float* kin, int N, uint4* left, uint4* right) {
+  const size_t k8 = (N + 7) / 8, m16 = (N + 15) / 16;
+  const size_t n = (m16 > k8 ? m16 : k8) * k8 * 32;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    kdq::kin_frag_word(kin, N, e, left, right);
 }
 
 __global__ void k_to_float(const double* src, float* dst, size_t n) {
@@ -918,6 +931,22 @@ int kdq_set_precision(kdq_handle* h, int32_t mode) {
       k_to_float<<<64, 256, 0, h->stream>>>(src[q]->as<double>(), dst[q]->as<float>(), kn);
       KDQ_CUDA(h, cudaGetLastError());
     }
+    if (!h->kc) {   // real kinetic matrices: pre-split operands of the tensor-core products
+      const size_t words = kdq::kin_frag_words(h->Ns);
+      KDQ_CUDA(h, h->kinfrag.alloc(8 * words * sizeof(uint4)));
+      uint4* base = h->kinfrag.as<uint4>();
+      for (int q = 0; q < 4; ++q) {
+        k_kin_frag<<<64, 256, 0, h->stream>>>(dst[q]->as<float>(), h->Ns, base + (size_t)(2 * q) * words,
+                                              base + (size_t)(2 * q + 1) * words);
+        KDQ_CUDA(h, cudaGetLastError());
+      }
+      P.kin_frag = base;
+      P.kin_frag_words = words;
+    } else {
+      h->kinfrag.alloc(0);
+      P.kin_frag = nullptr;
+      P.kin_frag_words = 0;
+    }
     const size_t pn = Nn * (h->gc ? 2 : 1);   // doubles per trial-state matrix
     KDQ_CUDA(h, h->Pts.alloc(pn * 2 * sizeof(float)));
     KDQ_CUDA(h, h->PtHs.alloc(pn * 2 * sizeof(float)));
@@ -938,6 +967,9 @@ int kdq_set_precision(kdq_handle* h, int32_t mode) {
     h->Gd.alloc(0);
     h->Pts.alloc(0);
     h->PtHs.alloc(0);
+    h->kinfrag.alloc(0);
+    P.kin_frag = nullptr;
+    P.kin_frag_words = 0;
     P.Yw = h->Y.p;
     P.Y2w = h->Y2.p;
     P.Gd = h->W1.p;

@@ -74,13 +74,25 @@ __device__ inline void gemm_thin(int M, int N, int K, const TA* A, int lda, cons
 // Products with a kinetic matrix kin (eK, eKinv, HalfeK, HalfeKinv):
 // C = rs .* (kin X) .* cs (kmul_left) or rs .* (X kin) .* cs (kmul_right).
 // The mixed sweep with a real kinetic matrix (no flux) runs them as 3xTF32
-// tensor tiles (kdq_tc.cuh); the FP64 sweep and complex kinetic matrices use
-// the register-tiled CUDA-core GEMM (THIN: the N x ns / ns x N tile shape).
+// tensor tiles (kdq_tc.cuh) with the kinetic operand pre-split (kf, see
+// kin_frag); the FP64 sweep and complex kinetic matrices use the
+// register-tiled CUDA-core GEMM (THIN: the N x ns / ns x N tile shape).
+enum { KIN_EK = 0, KIN_EKINV = 1, KIN_HALFEK = 2, KIN_HALFEKINV = 3 };
+
+// Pre-split words of kinetic matrix kid as the left (side 0) or right
+// (side 1) operand, or NULL (then the TF32 products are not used: the
+// runtime builds the words whenever the mixed sweep has a real kinetic
+// matrix, and refuses to launch it without them).
+__device__ __forceinline__ const uint4* kin_frag(const SweepParams& P, int kid, int side) {
+  return P.kin_frag ? static_cast<const uint4*>(P.kin_frag) + (size_t)(2 * kid + side) * P.kin_frag_words
+                    : nullptr;
+}
+
 template <int MAXRM, bool THIN, class TW, class KW>
-__device__ inline void kmul_left(int M, int N, int K, const KW* kin, int ldk, const TW* X, int ldx, TW* C, int ldc,
-                                 const TW* rs = nullptr, const TW* cs = nullptr) {
+__device__ inline void kmul_left(int M, int N, int K, const KW* kin, const uint4* kf, int ldk, const TW* X, int ldx,
+                                 TW* C, int ldc, const TW* rs = nullptr, const TW* cs = nullptr) {
   if constexpr (std::is_same_v<TW, cf> && std::is_same_v<KW, float>) {
-    tc_cgemm<true>(M, N, K, kin, ldk, reinterpret_cast<const float*>(X), ldx, C, ldc, rs, cs);
+    tc_cgemm<true>(M, N, K, kf, reinterpret_cast<const float*>(X), ldx, C, ldc, rs, cs);
   } else if constexpr (THIN) {
     gemm_thin<MAXRM, TW>(M, N, K, kin, ldk, X, ldx, C, ldc, rs, cs);
   } else {
@@ -88,10 +100,10 @@ __device__ inline void kmul_left(int M, int N, int K, const KW* kin, int ldk, co
   }
 }
 template <int MAXRM, bool THIN, class TW, class KW>
-__device__ inline void kmul_right(int M, int N, int K, const TW* X, int ldx, const KW* kin, int ldk, TW* C, int ldc,
-                                  const TW* rs = nullptr, const TW* cs = nullptr) {
+__device__ inline void kmul_right(int M, int N, int K, const TW* X, int ldx, const KW* kin, const uint4* kf, int ldk,
+                                  TW* C, int ldc, const TW* rs = nullptr, const TW* cs = nullptr) {
   if constexpr (std::is_same_v<TW, cf> && std::is_same_v<KW, float>) {
-    tc_cgemm<false>(M, N, K, reinterpret_cast<const float*>(X), ldx, kin, ldk, C, ldc, rs, cs);
+    tc_cgemm<false>(M, N, K, kf, reinterpret_cast<const float*>(X), ldx, C, ldc, rs, cs);
   } else if constexpr (THIN) {
     gemm_thin<MAXRM, TW>(M, N, K, X, ldx, kin, ldk, C, ldc, rs, cs);
   } else {
@@ -252,8 +264,8 @@ template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
 __device__ void wrap_fwd_kv(Ctx<KIND, T, KT, TW, KW>& c, TW* G, TW* W, int lt) {
   const int N = c.P.Ns;
   slice_diag(c, lt, +1);
-  kmul_left<MAXRM, false>(N, N, N, c.eK, N, G, N, W, N);                         // eK G
-  kmul_right<MAXRM, false>(N, N, N, W, N, c.eKinv, N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
+  kmul_left<MAXRM, false>(N, N, N, c.eK, kin_frag(c.P, KIN_EK, 0), N, G, N, W, N);                         // eK G
+  kmul_right<MAXRM, false>(N, N, N, W, N, c.eKinv, kin_frag(c.P, KIN_EKINV, 1), N, G, N, c.sm.dvec, c.sm.dinv); // D (.) eKinv D^-1
 }
 
 // G <- B_lt^{-1} G B_lt: WrapKV!("Backward","B"), src/tU/GreenMatrix.jl:78-83.
@@ -263,8 +275,8 @@ __device__ void wrap_bwd_kv(Ctx<KIND, T, KT, TW, KW>& c, TW* G, TW* W, int lt) {
   slice_diag(c, lt, -1);
   for (Walk w(N, N); w.ok(); w.next()) G[w.e] = (c.sm.dvec[w.i] * G[w.e]) * c.sm.dinv[w.j];
   __syncthreads();
-  kmul_left<MAXRM, false>(N, N, N, c.eKinv, N, G, N, W, N);
-  kmul_right<MAXRM, false>(N, N, N, W, N, c.eK, N, G, N);
+  kmul_left<MAXRM, false>(N, N, N, c.eKinv, kin_frag(c.P, KIN_EKINV, 0), N, G, N, W, N);
+  kmul_right<MAXRM, false>(N, N, N, W, N, c.eK, kin_frag(c.P, KIN_EK, 1), N, G, N);
 }
 
 // tV bond rotation of direction j on both sides of G:
@@ -969,7 +981,7 @@ __device__ TW* apply_slice_left(Ctx<KIND, T, KT, TW, KW>& c, TW* Y, TW* Y2, int 
     }
   } else {
     slice_diag(c, lt, +1);
-    kmul_left<MAXRM, true>(N, ns, N, c.eK, N, Y, N, Y2, N, c.sm.dvec);
+    kmul_left<MAXRM, true>(N, ns, N, c.eK, kin_frag(c.P, KIN_EK, 0), N, Y, N, Y2, N, c.sm.dvec);
   }
   return Y2;
 }
@@ -1001,7 +1013,7 @@ __device__ TW* apply_slice_right(Ctx<KIND, T, KT, TW, KW>& c, TW* Z, TW* Z2, int
       Z[e] = Z[e] * c.sm.dvec[col];
     }
     __syncthreads();
-    kmul_right<MAXRM, true>(ns, N, N, Z, ns, c.eK, N, Z2, ns);
+    kmul_right<MAXRM, true>(ns, N, N, Z, ns, c.eK, kin_frag(c.P, KIN_EK, 1), N, Z2, ns);
   }
   return Z2;
 }
@@ -1287,8 +1299,8 @@ __device__ void measure(Ctx<KIND, T, KT, TW, KW>& c, int t0) {
       }
     }
   }
-  kmul_left<MAXRM, false>(N, N, N, c.HalfeK, N, G0, N, W, N);
-  kmul_right<MAXRM, false>(N, N, N, W, N, c.HalfeKinv, N, G0, N);
+  kmul_left<MAXRM, false>(N, N, N, c.HalfeK, kin_frag(c.P, KIN_HALFEK, 0), N, G0, N, W, N);
+  kmul_right<MAXRM, false>(N, N, N, W, N, c.HalfeKinv, kin_frag(c.P, KIN_HALFEKINV, 1), N, G0, N);
   observables(c, G0);
 }
 
@@ -1508,15 +1520,15 @@ __device__ void mul_slice(Ctx<KIND, T, KT, TW, KW>& c, TW* X, TW* W, int lt, con
     if (right && !inv) {          // X D eK
       for (Walk w(N, N); w.ok(); w.next()) X[w.e] = X[w.e] * d[w.j];
       __syncthreads();
-      kmul_right<MAXRM, false>(N, N, N, X, N, c.eK, N, W, N);
+      kmul_right<MAXRM, false>(N, N, N, X, N, c.eK, kin_frag(c.P, KIN_EK, 1), N, W, N);
     } else if (right) {           // X eKinv D^-1
-      kmul_right<MAXRM, false>(N, N, N, X, N, c.eKinv, N, W, N, (const TW*)nullptr, d);
+      kmul_right<MAXRM, false>(N, N, N, X, N, c.eKinv, kin_frag(c.P, KIN_EKINV, 1), N, W, N, (const TW*)nullptr, d);
     } else if (!inv) {            // D eK X
-      kmul_left<MAXRM, false>(N, N, N, c.eK, N, X, N, W, N, d, (const TW*)nullptr);
+      kmul_left<MAXRM, false>(N, N, N, c.eK, kin_frag(c.P, KIN_EK, 0), N, X, N, W, N, d, (const TW*)nullptr);
     } else {                      // eKinv D^-1 X
       for (Walk w(N, N); w.ok(); w.next()) X[w.e] = d[w.i] * X[w.e];
       __syncthreads();
-      kmul_left<MAXRM, false>(N, N, N, c.eKinv, N, X, N, W, N);
+      kmul_left<MAXRM, false>(N, N, N, c.eKinv, kin_frag(c.P, KIN_EKINV, 0), N, X, N, W, N);
     }
     for (int e = threadIdx.x; e < N * N; e += blockDim.x) X[e] = W[e];
     __syncthreads();

@@ -56,13 +56,35 @@ __device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1
 constexpr int TC_WM = 3;   // m16 tiles per warp
 constexpr int TC_WN = 4;   // n8 tiles per warp
 
-// C (M x N complex) = rs .* (A B) .* cs with A real (M x K, lda) and B complex
-// (K x N, ldb complex elements) when LEFT, A complex (M x K, lda) and B real
-// (K x N, ldb) otherwise.  C must not alias A or B.  rs (M) and cs (N) may be
-// NULL.  All threads of the CTA call it; it ends with __syncthreads().
+// Pre-split kinetic matrices.  A real N x N kinetic matrix (column-major) is
+// constant over the sweep and shared by every chain, so its TF32 hi/lo split
+// is done once, into the order in which a warp's lanes consume it:
+//   left operand (A of kin X): m16 x k8 tile (mt, kt) of ceil(N/16) x
+//     ceil(N/8), lane (g, t): uint4 words 2 w and 2 w + 1 with
+//     w = (mt ceil(N/8) + kt) 32 + lane hold hi and lo of a0..a3 =
+//     A(16 mt + g, 8 kt + t), A(+8, 8 kt + t), A(16 mt + g, 8 kt + t + 4),
+//     A(+8, 8 kt + t + 4);
+//   right operand (B of X kin): k8 x n8 tile (kt, nt) of ceil(N/8) x
+//     ceil(N/8), lane (g, t): word (kt ceil(N/8) + nt) 32 + lane =
+//     (hi b0, hi b1, lo b0, lo b1), b0 = B(8 kt + t, 8 nt + g),
+//     b1 = B(8 kt + t + 4, 8 nt + g);
+// entries outside the matrix are 0.  The split is the one tc_cgemm applies
+// on the fly, so the products are bit for bit the same.
+__host__ __device__ inline size_t kin_frag_words(int N) {
+  const size_t m16 = (N + 15) / 16, k8 = (N + 7) / 8;
+  const size_t left = m16 * k8 * 64, right = k8 * k8 * 32;
+  return left > right ? left : right;
+}
+
+// C (M x N complex) = rs .* (kin X) .* cs when LEFT (M = K = the kinetic
+// matrix's order), rs .* (X kin) .* cs otherwise (K = N = its order), with
+// the real kinetic matrix kin given by its pre-split words kf (left layout
+// for LEFT, right layout otherwise) and X complex (K x N or M x K, ldx
+// complex elements).  C must not alias X.  rs (M) and cs (N) may be NULL.
+// All threads of the CTA call it; it ends with __syncthreads().
 template <bool LEFT>
-__device__ __noinline__ void tc_cgemm(int M, int N, int K, const float* __restrict__ A, int lda,
-                                      const float* __restrict__ B, int ldb, cf* __restrict__ C, int ldc,
+__device__ __noinline__ void tc_cgemm(int M, int N, int K, const uint4* __restrict__ kf,
+                                      const float* __restrict__ X, int ldx, cf* __restrict__ C, int ldc,
                                       const cf* rs, const cf* cs) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int g = lane >> 2, t = lane & 3;
@@ -81,69 +103,74 @@ __device__ __noinline__ void tc_cgemm(int M, int N, int K, const float* __restri
       for (int j = 0; j < TC_WN; ++j)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.0f;
-    // element offsets of this thread's fragment rows / columns (-1: outside)
-    int arow[TC_WM][2];   // A: real-view rows g and g + 8 of each m tile
+    // float offsets of this thread's fragment rows / columns of X (-1: outside)
+    int arow[TC_WM][2];   // right: A = X, complex row 8 mt + g, part h (rows g, g + 8 of the tile)
+    int bcol[TC_WN];      // left: B = X, complex column 4 nt + g / 2, part g & 1
+    if constexpr (!LEFT) {
 #pragma unroll
-    for (int i = 0; i < TC_WM; ++i)
+      for (int i = 0; i < TC_WM; ++i)
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int mt = mt0 + i;
-        if (LEFT) {
-          const int m = mt * 16 + g + 8 * h;
-          arow[i][h] = (mt < MT && m < M) ? m : -1;
-        } else {   // complex row 8 mt + g, part h
-          const int m = mt * 8 + g;
+        for (int h = 0; h < 2; ++h) {
+          const int mt = mt0 + i, m = mt * 8 + g;
           arow[i][h] = (mt < MT && m < M) ? 2 * m + h : -1;
         }
-      }
-    int bcol[TC_WN];   // B: real-view column g of each n tile
+    } else {
 #pragma unroll
-    for (int j = 0; j < TC_WN; ++j) {
-      const int nt = nt0 + j;
-      if (LEFT) {   // complex column 4 nt + g / 2, part g & 1
-        const int n = nt * 4 + (g >> 1);
-        bcol[j] = (nt < NT && n < N) ? 2 * n * ldb + (g & 1) : -1;
-      } else {
-        const int n = nt * 8 + g;
-        bcol[j] = (nt < NT && n < N) ? n * ldb : -1;
+      for (int j = 0; j < TC_WN; ++j) {
+        const int nt = nt0 + j, n = nt * 4 + (g >> 1);
+        bcol[j] = (nt < NT && n < N) ? 2 * n * ldx + (g & 1) : -1;
       }
     }
     for (int kt = 0; kt < KT; ++kt) {
       const int k0 = kt * 8 + t, k1 = k0 + 4;
       const bool kin0 = k0 < K, kin1 = k1 < K;
       uint32_t ah[TC_WM][4], al[TC_WM][4];
+      if constexpr (LEFT) {   // kinetic A: its lane's pre-split words
 #pragma unroll
-      for (int i = 0; i < TC_WM; ++i) {
-        float v[4];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int r = arow[i][h];
-          if (LEFT) {
-            v[h] = (r >= 0 && kin0) ? A[r + (size_t)k0 * lda] : 0.0f;
-            v[2 + h] = (r >= 0 && kin1) ? A[r + (size_t)k1 * lda] : 0.0f;
-          } else {
-            v[h] = (r >= 0 && kin0) ? A[r + (size_t)k0 * 2 * lda] : 0.0f;
-            v[2 + h] = (r >= 0 && kin1) ? A[r + (size_t)k1 * 2 * lda] : 0.0f;
+        for (int i = 0; i < TC_WM; ++i) {
+          const int mt = mt0 + i;
+          uint4 h = make_uint4(0u, 0u, 0u, 0u), l = h;
+          if (mt < MT) {
+            const uint4* w = kf + ((size_t)(mt * KT + kt) * 32 + lane) * 2;
+            h = w[0];
+            l = w[1];
           }
+          ah[i][0] = h.x; ah[i][1] = h.y; ah[i][2] = h.z; ah[i][3] = h.w;
+          al[i][0] = l.x; al[i][1] = l.y; al[i][2] = l.z; al[i][3] = l.w;
         }
-        // fragment order: a0 (row g, col t), a1 (row g+8, col t), a2 (row g, col t+4), a3 (row g+8, col t+4)
+      } else {                // complex A = X, split here
 #pragma unroll
-        for (int q = 0; q < 4; ++q) tf32_split(v[q], ah[i][q], al[i][q]);
+        for (int i = 0; i < TC_WM; ++i) {
+          float v[4];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int r = arow[i][h];
+            v[h] = (r >= 0 && kin0) ? X[r + (size_t)k0 * 2 * ldx] : 0.0f;
+            v[2 + h] = (r >= 0 && kin1) ? X[r + (size_t)k1 * 2 * ldx] : 0.0f;
+          }
+          // fragment order: a0 (row g, col t), a1 (row g+8, col t), a2 (row g, col t+4), a3 (row g+8, col t+4)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) tf32_split(v[q], ah[i][q], al[i][q]);
+        }
       }
       uint32_t bh[TC_WN][2], bl[TC_WN][2];
+      if constexpr (LEFT) {   // complex B = X, split here
 #pragma unroll
-      for (int j = 0; j < TC_WN; ++j) {
-        const int c = bcol[j];
-        float v0, v1;
-        if (LEFT) {
-          v0 = (c >= 0 && kin0) ? B[c + 2 * k0] : 0.0f;
-          v1 = (c >= 0 && kin1) ? B[c + 2 * k1] : 0.0f;
-        } else {
-          v0 = (c >= 0 && kin0) ? B[c + k0] : 0.0f;
-          v1 = (c >= 0 && kin1) ? B[c + k1] : 0.0f;
+        for (int j = 0; j < TC_WN; ++j) {
+          const int c = bcol[j];
+          const float v0 = (c >= 0 && kin0) ? X[c + 2 * k0] : 0.0f;
+          const float v1 = (c >= 0 && kin1) ? X[c + 2 * k1] : 0.0f;
+          tf32_split(v0, bh[j][0], bl[j][0]);
+          tf32_split(v1, bh[j][1], bl[j][1]);
         }
-        tf32_split(v0, bh[j][0], bl[j][0]);
-        tf32_split(v1, bh[j][1], bl[j][1]);
+      } else {                // kinetic B: its lane's pre-split word
+#pragma unroll
+        for (int j = 0; j < TC_WN; ++j) {
+          const int nt = nt0 + j;
+          uint4 v = make_uint4(0u, 0u, 0u, 0u);
+          if (nt < NT) v = kf[((size_t)kt * NT + nt) * 32 + lane];
+          bh[j][0] = v.x; bh[j][1] = v.y; bl[j][0] = v.z; bl[j][1] = v.w;
+        }
       }
 #pragma unroll
       for (int i = 0; i < TC_WM; ++i)
@@ -189,6 +216,34 @@ __device__ __noinline__ void tc_cgemm(int M, int N, int K, const float* __restri
       }
   }
   __syncthreads();
+}
+
+// Word e of the pre-split layouts of the N x N kinetic matrix kin: writes the
+// left-operand words 2e, 2e + 1 (e < ceil(N/16) ceil(N/8) 32) into left and
+// the right-operand word e (e < ceil(N/8)^2 32) into right.
+__device__ inline void kin_frag_word(const float* __restrict__ kin, int N, size_t e, uint4* __restrict__ left,
+                                     uint4* __restrict__ right) {
+  const int K8 = (N + 7) / 8, M16 = (N + 15) / 16;
+  const int lane = (int)(e & 31), g = lane >> 2, t = lane & 3;
+  const size_t tile = e >> 5;
+  auto at = [&](int r, int k) { return (r < N && k < N) ? kin[r + (size_t)k * N] : 0.0f; };
+  if (tile < (size_t)M16 * K8) {
+    const int mt = (int)(tile / K8), kt = (int)(tile % K8);
+    const int r = 16 * mt + g, k = 8 * kt + t;
+    const float v[4] = {at(r, k), at(r + 8, k), at(r, k + 4), at(r + 8, k + 4)};
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) tf32_split(v[q], h[q], l[q]);
+    left[2 * e] = make_uint4(h[0], h[1], h[2], h[3]);
+    left[2 * e + 1] = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+  if (tile < (size_t)K8 * K8) {
+    const int kt = (int)(tile / K8), nt = (int)(tile % K8);
+    uint32_t h0, l0, h1, l1;
+    tf32_split(at(8 * kt + t, 8 * nt + g), h0, l0);
+    tf32_split(at(8 * kt + t + 4, 8 * nt + g), h1, l1);
+    right[e] = make_uint4(h0, h1, l0, l1);
+  }
 }
 
 // One complex entry (re, im) of a cf (S = 2) or cdf (S = 4, hi + lo) array.
