@@ -788,8 +788,12 @@ __device__ int propose_window(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int jd
 // ratio and an accepted proposal's new vectors read G through that sum, and
 // G itself is rewritten once per KDQ_DELAY vectors (delayed_flush) instead
 // of once per acceptance: the N x N matrix streams through L2 KDQ_DELAY / k
-// times less often.  Decisions use the same windows as the FP64 sweep.
-#define KDQ_DELAY 8
+// times less often.  Decisions use the same windows as the FP64 sweep.  16
+// vectors (48 KB of shared memory at the largest lattice) keep two CTAs per
+// SM; the flush's cost is mostly its pass over G, so 16 instead of 8 nearly
+// halves it while the correction sums of the windows grow by 4 terms on
+// average.
+#define KDQ_DELAY 16
 template <class TW>
 struct Delay {
   TW U[KDQ_DELAY][KDQ_MAX_NS];

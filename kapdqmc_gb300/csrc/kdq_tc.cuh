@@ -209,9 +209,7 @@ __device__ __noinline__ void tc_cgemm(int M, int N, int K, const uint4* __restri
           cf v = e[q];
           if (rs) v = rs[row[q]] * v;
           if (cs) v = v * cs[col[q]];
-          const size_t o = 2 * (row[q] + (size_t)col[q] * ldc);
-          Cf[o] = v.x;
-          Cf[o + 1] = v.y;
+          *reinterpret_cast<float2*>(Cf + 2 * (row[q] + (size_t)col[q] * ldc)) = make_float2(v.x, v.y);
         }
       }
   }
@@ -303,7 +301,7 @@ __device__ __noinline__ void tc_zgemm(int M, int N, int K, const float* __restri
           const int n = (nt0 + j) * 8 + 2 * t + q;
           float re = 0.0f, im = 0.0f;
           if (SUB && arow[i] >= 0 && nt0 + j < NT && n < N) {
-            const size_t o = 2 * (arow[i] + (size_t)n * ldc);
+            const int o = 2 * (arow[i] + n * ldc);   // M, N <= KDQ_MAX_NS
             re = Cf[o];
             im = Cf[o + 1];
           }
@@ -358,9 +356,7 @@ __device__ __noinline__ void tc_zgemm(int M, int N, int K, const float* __restri
         for (int q = 0; q < 2; ++q) {
           const int n = (nt0 + j) * 8 + 2 * t + q;
           if (n >= N) continue;
-          const size_t o = 2 * (m + (size_t)n * ldc);
-          Cf[o] = acc[i][j][q];
-          Cf[o + 1] = acc[i][j][2 + q];
+          *reinterpret_cast<float2*>(Cf + 2 * (m + n * ldc)) = make_float2(acc[i][j][q], acc[i][j][2 + q]);
         }
       }
   }
