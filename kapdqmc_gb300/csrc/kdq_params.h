@@ -7,6 +7,7 @@
 #include "../../include/kapdqmc.h"
 
 #define KDQ_MAX_NS 192          // largest lattice (6 row groups of 32 per lane)
+#define KDQ_MAX_FIELD 768       // HS fields per slice (t-UV: Ns z with z <= 4)
 #define KDQ_MAX_OBS 12          // measurement columns per sweep row
 #define KDQ_THREADS 256         // threads per CTA (one CTA per chain)
 

@@ -277,6 +277,10 @@ int validate(const kdq_model_desc* m, int nchains, std::string& why) {
   if (m->kind == KDQ_TV && (m->g_complex || m->k_complex)) { why = "the tV sweep is real"; return 1; }
   if (m->kind == KDQ_TUV && m->k_complex) { why = "tUV kinetic matrices are real"; return 1; }
   const int nb = m->kind == KDQ_TV ? (m->Ns / 2) * m->z : m->Ns * m->z;
+  if (m->kind != KDQ_TU && nb > KDQ_MAX_FIELD) {
+    why = "too many bonds per slice (at most " + std::to_string(KDQ_MAX_FIELD) + ")";
+    return 1;
+  }
   if (m->kind != KDQ_TU)
     for (int b = 0; b < 2 * nb; ++b)
       if (m->bonds[b] < 1 || m->bonds[b] > m->Ns) { why = "bond index out of range"; return 1; }

@@ -152,6 +152,8 @@ struct Smem {
   int nxt[2];      // next proposal of a layer after a window (FP64)
   int newv;
   int bad;
+  int nacc;                     // acceptances of the current slice (thread 0)
+  uint8_t fld[KDQ_MAX_FIELD];   // the current slice's fields while its proposals run
 };
 
 template <int KIND, class T, class KT, class TW, class KW>
@@ -765,8 +767,7 @@ __device__ int propose_window(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt, int jd
     if (lane == 0) {
       sm.accept[par] = ja < W;
       sm.nxt[par] = m0 + nres;
-      c.ctl->n_prop += nres;
-      c.ctl->n_acc += (ja < W) ? 1 : 0;
+      sm.nacc += (ja < W) ? 1 : 0;
     }
   }
   __syncthreads();
@@ -798,6 +799,7 @@ template <class TW>
 struct Delay {
   TW U[KDQ_DELAY][KDQ_MAX_NS];
   TW W[KDQ_DELAY][KDQ_MAX_NS];
+  TW diag[KDQ_MAX_NS];   // diagonal of the stored G (refreshed at slice start and after each flush)
 };
 
 // G -= sum_{q < kd} U[q] W[q]^T.  Complex G: one N x N x kd product on the
@@ -835,6 +837,21 @@ __device__ __forceinline__ TW delayed_entry(const TW* G, int N, const Delay<TW>&
   return v;
 }
 
+// (G - U W)[i, i] from the shared-memory copy of G's diagonal
+template <class TW>
+__device__ __forceinline__ TW delayed_diag(const TW* gdiag, const Delay<TW>& db, int kd, int i) {
+  TW v = gdiag[i];
+  for (int q = 0; q < kd; ++q) madd(v, -db.U[q][i], db.W[q][i]);
+  return v;
+}
+
+// Copies the diagonal of the stored G into shared memory (all threads call it).
+template <class TW>
+__device__ __forceinline__ void load_gdiag(TW* gdiag, const TW* G, int N) {
+  for (int a = threadIdx.x; a < N; a += blockDim.x) gdiag[a] = G[a + (size_t)a * N];
+  __syncthreads();
+}
+
 // One window of proposals with delayed updates; kd (uniform over the CTA)
 // is the number of pending vector pairs.  Returns the next proposal index.
 template <int MAXRM, int KIND, class T, class KT, class TW, class KW>
@@ -857,12 +874,12 @@ __device__ int propose_window_delayed(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt
       const int sold = sl[f];
       const int tk = c.tk[m];
       sx = tk + (tk + 1 >= sold ? 2 : 1);   // k-th of {1..4}\{sold}
-      const T gxx = cvt<T>(delayed_entry(G, N, db, kd, x, x));
+      const T gxx = cvt<T>(delayed_diag(db.diag, db, kd, x));
       T gxy = zero<T>(), gyx = zero<T>(), gyy = zero<T>();
       if constexpr (RK == 2) {
         gxy = cvt<T>(delayed_entry(G, N, db, kd, x, y));
         gyx = cvt<T>(delayed_entry(G, N, db, kd, y, x));
-        gyy = cvt<T>(delayed_entry(G, N, db, kd, y, y));
+        gyy = cvt<T>(delayed_diag(db.diag, db, kd, y));
       }
       const double p = ratio_ss(c, lt, sold - 1, sx - 1, c.tu[m], gxx, gxy, gyx, gyy, r00, r01, r10, r11);
       bad = !isfinite(p);
@@ -889,8 +906,7 @@ __device__ int propose_window_delayed(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt
     if (lane == 0) {
       sm.accept[par] = ja < W;
       sm.nxt[par] = m0 + nres;
-      c.ctl->n_prop += nres;
-      c.ctl->n_acc += (ja < W) ? 1 : 0;
+      sm.nacc += (ja < W) ? 1 : 0;
     }
   }
   __syncthreads();
@@ -919,6 +935,7 @@ __device__ int propose_window_delayed(Ctx<KIND, T, KT, TW, KW>& c, TW* G, int lt
     kd += RK;
     if (kd + RK > KDQ_DELAY) {   // no room for another acceptance
       delayed_flush(G, N, db, kd);
+      load_gdiag(db.diag, G, N);
       kd = 0;
     }
   }
@@ -943,16 +960,29 @@ __device__ void update_layer(Ctx<KIND, T, KT, TW, KW>& c, int lt, int j, bool fw
   }
   load_tape(c, qs + off, n);
   const int logbase = (int)(c.ctl->log_pos);
+  // the slice's fields and acceptance count live in shared memory while its
+  // windows run (a window's decision then waits on no global round trip)
+  uint8_t* fs = c.sm.fld;
+  for (int e = threadIdx.x; e < pf; e += blockDim.x) fs[e] = sl[e];
+  if (threadIdx.x == 0) c.sm.nacc = 0;
+  __syncthreads();
   int par = 0;
   if constexpr (std::is_same_v<T, TW>) {
-    for (int m = 0; m < n; par ^= 1) m = propose_window<MAXRM>(c, c.G, lt, j, n, m, logbase, sl, par);
+    for (int m = 0; m < n; par ^= 1) m = propose_window<MAXRM>(c, c.G, lt, j, n, m, logbase, fs, par);
   } else {
     __shared__ Delay<TW> db;
     int kd = 0;
-    for (int m = 0; m < n; par ^= 1) m = propose_window_delayed<MAXRM>(c, c.G, lt, j, n, m, logbase, sl, par, db, kd);
+    load_gdiag(db.diag, c.G, P.Ns);
+    for (int m = 0; m < n; par ^= 1) m = propose_window_delayed<MAXRM>(c, c.G, lt, j, n, m, logbase, fs, par, db, kd);
     if (kd) delayed_flush(c.G, P.Ns, db, kd);
   }
-  if (threadIdx.x == 0) c.ctl->log_pos += n;
+  __syncthreads();
+  for (int e = threadIdx.x; e < pf; e += blockDim.x) sl[e] = fs[e];
+  if (threadIdx.x == 0) {
+    c.ctl->log_pos += n;
+    c.ctl->n_prop += n;
+    c.ctl->n_acc += c.sm.nacc;
+  }
   finish_tape(c, n);
   __syncthreads();
 }
