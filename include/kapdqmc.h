@@ -236,11 +236,14 @@ int kdq_grover_det_noalloc(const double* G, int32_t Ns, int32_t g_complex, int32
  * stabilisation chain, the measurement's kinetic factors) run as 3xTF32
  * tensor-core tiles with FP32 accumulation (FP32 CUDA-core products when
  * the hopping is complex), the rank-k updates of G in FP32, delayed and
- * applied in batches; the acceptance ratios stay FP64, and the thin QR
- * (Cholesky QR, Householder when a block is ill-conditioned), the inverse
- * and the recompute of G at every node run in double-float arithmetic (two
- * FP32 values, 48-bit significand, ~1e-14 relative); kdq_get_drift then
- * reports ||G_FP32-wrap - G_recompute||_F / ||G||_F.  Only the complex sweeps
+ * applied in batches of up to 16 vectors (complex G: as 3xTF32 tensor-core
+ * products); the acceptance ratios stay FP64; the thin QR (Cholesky QR,
+ * Householder when a block is ill-conditioned), BL BR and its inverse at
+ * every node run in double-float arithmetic (two FP32 values, 48-bit
+ * significand, ~1e-14 relative), and the two products that form the FP32 G
+ * from them, (BL BR)^-1 BL and BR X, as 3xTF32 tensor-core products (complex
+ * G); kdq_get_drift then reports ||G_FP32-wrap - G_recompute||_F / ||G||_F.
+ * Only the complex sweeps
  * (t-U, t-UV with U > 0) accept it: their HS factors cis(alpha eta) are
  * unitary, while the real factors exp(+-alpha eta) of t-V and real t-UV
  * amplify FP32 rounding in the wraps (KDQ_ERR_ARG).  No counterpart in the
