@@ -1,6 +1,8 @@
 // Split-precision (3xTF32) products of the mixed-precision sweep on the
 // tensor pipe: complex FP32 matrices times the real FP32 kinetic matrices
-// (eK, eKinv, HalfeK, HalfeKinv of a hopping matrix without flux).
+// (eK, eKinv, HalfeK, HalfeKinv of a hopping matrix without flux;
+// tc_cgemm), and complex times complex (tc_zgemm: the two products that
+// form G at a recompute, and the delayed rank-k flushes of G).
 //
 // Every FP32 operand x is split into two TF32 values, hi = tf32(x) and
 // lo = tf32(x - hi) (x - hi is exact in FP32), and each product A B is
@@ -8,8 +10,9 @@
 // term, ~2^-22 relative, is dropped): about FP32 accuracy from TF32 tensor
 // operations.  Tiles are mma.sync.m16n8k8 (TF32 inputs, FP32 accumulators);
 // the whole CTA computes one product, each warp a 3 x 4 block of 16 x 8
-// tiles, operands read through L1 (the kinetic matrix is shared by every
-// chain of the launch and stays in L2).
+// tiles, operands read through L1.  The kinetic matrices, constant and
+// shared by every chain, are split once into fragment order (kin_frag) and
+// stay in L2; the other operands are split as they are loaded.
 //
 // A complex matrix is used through a real view of its interleaved (re, im)
 // floats, arranged so that the real and imaginary part of one complex entry
@@ -23,8 +26,10 @@
 // C = rs[i] (A B)[i,j] cs[j] of the slice wraps and block products.
 //
 // Reference products (KAPDQMC): WrapKV! src/tU/GreenMatrix.jl:56-86 (and
-// src/tUV/GreenMatrix.jl:92-122), BM_F! src/tU/GreenMatrix.jl:10-27, and the
-// measurement wraps of phy_measure src/tU/phy_update.jl:154-182.
+// src/tUV/GreenMatrix.jl:92-122), BM_F! src/tU/GreenMatrix.jl:10-27, the
+// measurement wraps of phy_measure src/tU/phy_update.jl:154-182, the
+// products of get_G! src/public/Gupdate.jl:139-157 and the G update of
+// Gupdate! src/public/Gupdate.jl:5-11 (applied in batches).
 #pragma once
 #include <cstdint>
 
