@@ -20,9 +20,9 @@ also estimated live from the timed sweeps.
           buffers: fields uploaded, chain rebuilt, one sweep, fields and
           measurement rows read back, every step
 
-`--impl reference` times the C restatement of the reference algorithm on
-the host cores instead; `--workload c1|c2|c4|c5` selects the other
-configurations.
+`--impl reference` times the C restatement of the reference algorithm
+(t-U, t-V or t-UV, whichever the workload is) on the host cores instead;
+`--workload c1|c2|c4|c5` selects the other configurations.
 """
 from __future__ import annotations
 
