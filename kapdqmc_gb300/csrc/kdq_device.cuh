@@ -9,6 +9,10 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+// Largest order whose Gauss-Jordan / Cholesky determinant bookkeeping is
+// deferred past the pivot loop (the sweep's ns <= 96, SCEE regions <= 96).
+constexpr int GJ_DEFER_MAX = 96;
+
 namespace kdq {
 
 // ---------------------------------------------------------------- complex
@@ -480,6 +484,8 @@ template <class T>
 __device__ void chol_upper(int n, T* W, double tol, double* rinv, int* bad, double* log_out = nullptr) {
   const int tid = threadIdx.x, nt = blockDim.x;
   __shared__ double dmax;
+  __shared__ double s_r[GJ_DEFER_MAX];   // R_kk, logged after the loop (as in gj_inverse)
+  const bool defer = log_out && n <= GJ_DEFER_MAX;
   if (tid == 0) {
     double m = 0.0;
     for (int k = 0; k < n; ++k) m = fmax(m, re(W[k + (size_t)k * n]));
@@ -497,7 +503,10 @@ __device__ void chol_upper(int n, T* W, double tol, double* rinv, int* bad, doub
       const double r = sqrt(d);
       W[k + (size_t)k * n] = from_real<T>(r);
       rinv[k] = 1.0 / r;
-      lgs += log(r);
+      if (defer)
+        s_r[k] = r;
+      else if (log_out)
+        lgs += log(r);
     }
     __syncthreads();
     const double s = rinv[k];
@@ -509,6 +518,12 @@ __device__ void chol_upper(int n, T* W, double tol, double* rinv, int* bad, doub
       W[i + (size_t)j * n] = W[i + (size_t)j * n] - conjg(W[k + (size_t)i * n]) * W[k + (size_t)j * n];
     }
     __syncthreads();
+  }
+  if (defer) {
+    for (int k = tid; k < n; k += nt) s_r[k] = log(s_r[k]);
+    __syncthreads();
+    if (tid == 0)
+      for (int k = 0; k < n; ++k) lgs += s_r[k];
   }
   if (tid == 0 && log_out) *log_out = lgs;
 }
@@ -588,6 +603,15 @@ __device__ void gj_inverse(int n, T* M, T* f, int* swaps, int* bad, double* log_
                            cd* phase_out = nullptr) {
   const int tid = threadIdx.x, nt = blockDim.x;
   __shared__ int sp;
+  __shared__ T s_inv;                // 1 / pivot of the current step
+  __shared__ cd s_pv[GJ_DEFER_MAX];  // the pivots, for the determinant after the loop
+  __shared__ double s_lg[GJ_DEFER_MAX];
+  // the determinant's log and phase are formed after the elimination (each
+  // pivot's log and phase in parallel, summed and multiplied in pivot order
+  // by thread 0, the same operations in the same order as inside the loop),
+  // keeping the FP64 logarithm and quotients off the steps' serial path
+  const bool want = log_out || phase_out;
+  const bool defer = n <= GJ_DEFER_MAX;
   double lgs = 0.0;          // log |det M| (thread 0)
   cd phs = mkc(1.0, 0.0);    // det M / |det M| (thread 0)
   for (int k = 0; k < n; ++k) {
@@ -620,15 +644,21 @@ __device__ void gj_inverse(int n, T* M, T* f, int* swaps, int* bad, double* log_
       }
     __syncthreads();
     // scale the pivot row: M[k,k] <- 1, row k <- row k / pivot
-    const T inv = one<T>() / M[k + (size_t)k * n];
     if (tid == 0) {    // det M = (-1)^(row swaps) * product of the pivots
-      const cd pv = cvt<cd>(M[k + (size_t)k * n]);
-      const double a = sqrt(abs2(pv));
-      lgs += log(a);
-      phs = phs * (a > 0.0 ? pv / a : mkc(1.0, 0.0));
-      if (p != k) phs = -phs;
+      const T pk = M[k + (size_t)k * n];
+      s_inv = one<T>() / pk;
+      const cd pv = cvt<cd>(pk);
+      if (defer) {
+        s_pv[k] = pv;
+      } else if (want) {
+        const double a = sqrt(abs2(pv));
+        lgs += log(a);
+        phs = phs * (a > 0.0 ? pv / a : mkc(1.0, 0.0));
+        if (p != k) phs = -phs;
+      }
     }
-    __syncthreads();   // every thread has read the pivot before row k changes
+    __syncthreads();   // the pivot is read before row k changes
+    const T inv = s_inv;
     for (int c = tid; c < n; c += nt) {
       const T v = c == k ? one<T>() : M[k + (size_t)c * n];
       M[k + (size_t)c * n] = v * inv;
@@ -654,6 +684,21 @@ __device__ void gj_inverse(int n, T* M, T* f, int* swaps, int* bad, double* log_
         M[r + (size_t)p * n] = tmp;
       }
     __syncthreads();
+  }
+  if (want && defer) {
+    for (int k = tid; k < n; k += nt) {
+      const cd pv = s_pv[k];
+      const double a = sqrt(abs2(pv));
+      s_lg[k] = log(a);
+      s_pv[k] = a > 0.0 ? pv / a : mkc(1.0, 0.0);
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (int k = 0; k < n; ++k) {
+        lgs += s_lg[k];
+        phs = phs * s_pv[k];
+        if (swaps[k] != k) phs = -phs;
+      }
   }
   if (tid == 0) {
     if (log_out) *log_out = lgs;
